@@ -1,0 +1,362 @@
+"""Benchmark: TGV^2 Cartesian MRI reconstruction, 15 coils x 640 x 368 (readout-oversampling removal).
+
+One step = one full TgvMriOptimizer solve of the problem (max_iter = 1000 -> 1001 primal-dual
+iterations, the sample's alpha continuation reduction = 2e-8, alpha0 = 2 alpha1) on seeded synthetic
+data with the shapes of the reference's knee example (bin/mri_cartesian_test.py).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+value  : iterations/s with inputs already resident in HBM (device pointers through the C ABI).
+e2e    : iterations/s through the public Python API with pinned host buffers: operator set-up and
+         constant upload, setNoisyData (H2D), solve, getResult (D2H) inside every timed step.
+--impl reference : the reference algorithm on the host cores (the CPU oracle restatement, all
+         threads), a bounded sample of the same workload per step.
+Prints one JSON line (rank 0).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG_DIR = os.path.join(ROOT, "primal-dual-toolbox_gb300")
+for _p in (PKG_DIR, ROOT):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+C, H, W = 15, 640, 368
+MAX_ITER = 1000
+ITERS = MAX_ITER + 1
+REDUCTION = 2e-8
+METRIC = "TGV MRI 15c 640x368: iters/s and time to 1e-4 rel err, warm-start vs plain"
+WORKLOAD = "tgv2_cartesian_roos_15c_640x368_1001it"
+L2_FLUSH_BYTES = 256 << 20
+
+
+def _rank_info():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+def _problem(seed=0):
+    from primaldualtoolbox import synthetic
+
+    return synthetic.cartesian_case(C=C, H=H, W=W, roos=True, seed=seed)
+
+
+def _peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def _ncu_traffic():
+    """Per-launch DRAM bytes of each kernel from the committed ncu summary (profiles/dram_traffic.txt)."""
+    out = {}
+    path = os.path.join(ROOT, "profiles", "dram_traffic.txt")
+    if os.path.exists(path):
+        for line in open(path):
+            parts = line.split()
+            if len(parts) >= 2 and not line.startswith("#"):
+                try:
+                    out[parts[0]] = float(parts[1])
+                except ValueError:
+                    pass
+    return out
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms while the timed region runs."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if len(r) > 4 + i and r[4 + i] == "Active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def _phase_bytes(ns, G):
+    """Algorithmic bytes per launch of each kernel phase (each logical array read or written once)."""
+    Hi = H // 2
+    c8 = 8
+    return {
+        # ubar + sens rows in, t1 (sampled columns) out
+        "cart_rows_fwd": c8 * (Hi * W + C * Hi * W + C * ns * Hi),
+        # t1, f, r in; r, t2 out; mask of sampled columns
+        "cart_cols_prox": c8 * (C * ns * Hi + 3 * C * ns * H + C * ns * Hi) + 4 * ns * H,
+        # t2 + sens rows in, K^H r partial sums out
+        "cart_rows_adj": c8 * (C * ns * Hi + C * Hi * W + G * Hi * W),
+        # ub, vb(2), p(2), q(3), u, v(2), G khr partials in; ub, vb(2), p(2), q(3), u, v(2) out
+        "mri_image_step_tgv": c8 * Hi * W * (11 + G + 11),
+    }
+
+
+def run_ours(args):
+    import torch
+
+    import primaldualtoolbox as pdt
+
+    rank, world, local = _rank_info()
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    stream = torch.cuda.current_stream()
+    case = _problem(seed=rank)
+    ns = int((case["mask"] != 0).any(axis=0).sum())
+    dev = {k: torch.from_numpy(np.ascontiguousarray(case[k])).cuda() for k in ("rawdata", "sens", "mask")}
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+
+    op = pdt.mri.MriCartesianRemoveROOSOperator()
+    op.setCoilSens(dev["sens"])
+    op.setMask(dev["mask"])
+    opt = pdt.mri.TgvMriOptimizer_2c3c()
+    prm = opt.getParameters()
+    prm.max_iter, prm.reduction, prm.alpha1 = MAX_ITER, REDUCTION, case["alpha1"]
+    prm.alpha0 = 2 * prm.alpha1
+    opt.setOperator(op)
+    u0 = torch.empty((H // 2, W), dtype=torch.complex64, device="cuda")
+    op.adjoint(dev["rawdata"], out=u0, stream=stream)
+
+    def step():
+        flush.zero_()  # evict L2 between steps (inputs ~120 MB < 129 MB L2)
+        opt.setNoisyData(dev["rawdata"], stream=stream)  # r = 0
+        opt.setInput0(u0, stream=stream)  # u = ubar = A^H f, v = p = q = 0
+        opt.solve(stream=stream)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    n0 = pdt.launch_count()
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        for _ in range(args.steps):
+            step()
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+    launches = pdt.launch_count() - n0
+    dev_s = ev0.elapsed_time(ev1) / 1e3
+    t_max = dev_s
+    if dist:
+        t = torch.tensor([dev_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_max = float(t.item())
+    value = ITERS * args.steps * world / t_max
+
+    # per-kernel timing (CUDA events on the launching stream) for the roofline of the dominant kernel
+    phases = opt.profile(iters=50, stream=stream)
+    G = _coil_groups(ns)
+    bytes_per = _phase_bytes(ns, G)
+    per_iter_ms = sum(phases.values())
+    dom = max(phases, key=phases.get)
+    hbm, src = _peaks()
+    traffic = _ncu_traffic()
+    achieved = bytes_per.get(dom, 0) / (phases[dom] / 1e3) / 1e9
+    roof = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": hbm, "peak_source": src,
+            "unit": "GB/s", "frac": round(achieved / hbm, 4), "traffic": traffic.get(dom),
+            "algorithmic_bytes": bytes_per.get(dom), "launch_ms": round(phases[dom], 5),
+            "share": round(phases[dom] / per_iter_ms, 3)}
+    phase_info = {k: {"ms": round(v, 5), "GB/s": round(bytes_per.get(k, 0) / (v / 1e3) / 1e9, 1)}
+                  for k, v in phases.items()}
+
+    # e2e: the public API with pinned host buffers, every input uploaded and the result read back
+    host = {k: pdt.pinned_empty(case[k].shape, case[k].dtype) for k in ("rawdata", "sens", "mask")}
+    for k in host:
+        host[k][...] = case[k]
+    h2d = sum(host[k].nbytes for k in host)
+    d2h = (H // 2) * W * 8
+
+    def e2e_step():
+        flush.zero_()
+        o = pdt.mri.MriCartesianRemoveROOSOperator()
+        o.setCoilSens(host["sens"])
+        o.setMask(host["mask"])
+        s = pdt.mri.TgvMriOptimizer_2c3c()
+        p = s.getParameters()
+        p.max_iter, p.reduction, p.alpha1 = MAX_ITER, REDUCTION, case["alpha1"]
+        p.alpha0 = 2 * p.alpha1
+        s.setOperator(o)
+        s.setNoisyData(host["rawdata"])
+        s.solve()
+        return s.getResult()
+
+    e2e_step()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    e_steps = max(1, min(args.steps, 5))
+    t0 = time.perf_counter()
+    for _ in range(e_steps):
+        e2e_step()
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    if dist:
+        t = torch.tensor([e2e_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_val = ITERS * e_steps * world / e2e_s
+
+    line = None
+    if rank == 0:
+        cpu = _cpu_baseline(case, seconds=args.cpu_seconds)
+        line = {
+            "metric": METRIC, "value": round(value, 1), "unit": "iters/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(t_max / args.steps * 1e3, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "c64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "coils": C, "fe": H, "pe": W, "image": [H // 2, W],
+                       "iterations_per_step": ITERS, "reduction": REDUCTION, "sampled_pe_lines": ns,
+                       "accel": round(W / ns, 2), "l2": "flushed between steps (256 MB write)",
+                       "parallelism": f"replicas{world}"},
+            "e2e": {"value": round(e2e_val, 1), "unit": "iters/s", "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h), "steps": e_steps},
+            "gpu_launches": int(launches),
+            "roofline": roof,
+            "phases": phase_info,
+            "cpu_baseline": cpu,
+            "clocks": clk.summary(),
+            "wall_s": round(wall, 3),
+        }
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+    return line
+
+
+def _coil_groups(ns):
+    """The engine's coil-group count for the adjoint row phase (two waves over the SMs)."""
+    import torch
+
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    rb = 4
+    rows = (H // 2 + rb - 1) // rb
+    return max(1, min(C, (2 * sms + rows - 1) // rows))
+
+
+def _cpu_baseline(case, seconds=10.0, threads=None):
+    """The reference iteration on the host cores: the CPU oracle restatement (FP32 mirror), all threads."""
+    from oracle import oracle
+
+    threads = threads or os.cpu_count()
+    oracle.set_threads(threads)
+    it = 1
+    t0 = time.perf_counter()
+    oracle.op_solve("cartesian_roos", case["sens"], case["mask"], case["rawdata"], "tgv_mri",
+                    alpha0=case["alpha0"], alpha1=case["alpha1"], reduction=REDUCTION, max_iter=it - 1, prec=32)
+    per = time.perf_counter() - t0
+    n = max(2, int(seconds / max(per, 1e-3)))
+    t0 = time.perf_counter()
+    oracle.op_solve("cartesian_roos", case["sens"], case["mask"], case["rawdata"], "tgv_mri",
+                    alpha0=case["alpha0"], alpha1=case["alpha1"], reduction=REDUCTION, max_iter=n - 1, prec=32)
+    dt = time.perf_counter() - t0
+    return {"value": round(n / dt, 3), "unit": "iters/s", "cores": threads, "kind": "port",
+            "sample": f"{n} of the {ITERS} iterations of one solve (includes the initial A^H f), FP32 mirror"}
+
+
+def run_reference(args):
+    """--impl reference: the reference's algorithm on the host CPU (the oracle restatement; the reference's
+    own CUDA build needs ImageUtilities, which it does not ship)."""
+    rank, world, _ = _rank_info()
+    if rank != 0:
+        return None
+    from oracle import oracle
+
+    case = _problem(seed=0)
+    threads = os.cpu_count()
+    oracle.set_threads(threads)
+    sample_iters = 4
+
+    def step():
+        oracle.op_solve("cartesian_roos", case["sens"], case["mask"], case["rawdata"], "tgv_mri",
+                        alpha0=case["alpha0"], alpha1=case["alpha1"], reduction=REDUCTION,
+                        max_iter=sample_iters - 1, prec=32)
+
+    for _ in range(args.warmup):
+        step()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step()
+    dt = time.perf_counter() - t0
+    val = sample_iters * args.steps / dt
+    line = {"metric": METRIC, "value": round(val, 3), "unit": "iters/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(dt / args.steps * 1e3, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "c64", "data": "synthetic", "impl": "reference",
+            "config": {"workload": WORKLOAD, "coils": C, "fe": H, "pe": W, "iterations_per_step": sample_iters},
+            "cpu_baseline": {"value": round(val, 3), "unit": "iters/s", "cores": threads, "kind": "port",
+                             "sample": f"{sample_iters} iterations (incl. initial A^H f) of the 1001-iteration solve "
+                                       f"per step, FP32 mirror of the reference iteration"},
+            "e2e": {"value": round(val, 3), "unit": "iters/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return line
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,163 @@
+/* pdt.h -- C ABI of the GB300 primal-dual TV/TGV^2 engine (libpdt.so).
+ *
+ * The reference (VLOGroup/primal-dual-toolbox) exposes C++ class templates and a boost.python module;
+ * this header is the plain-C boundary those surfaces sit on here. Every entry point names the reference
+ * interface it replaces (file:line inside the reference project). All functions return a pdt_status;
+ * on failure pdt_last_error() returns a thread-local message that mirrors the text of the reference's
+ * IuException at the same throw site.
+ *
+ * Conventions
+ *   - Sizes are given in ImageUtilities order, fastest dimension first: an image is {W (phase-encode),
+ *     H (frequency-encode)}, Cartesian k-space is {W, H, coils}. A numpy array of shape (C, H, W) in C
+ *     order has exactly this memory layout.
+ *   - Complex data is interleaved float pairs (complex64 / float2).
+ *   - `is_device` = 1: pointers are device pointers on the current device; 0: host pointers (pinned or
+ *     pageable). The caller owns every buffer it passes; handles own constants and solver state.
+ *   - `stream` is a cudaStream_t (NULL = the legacy default stream). Calls enqueue work on `stream`
+ *     and return when host buffers may be reused; pdt_opt_solve with a NULL stream returns after the
+ *     solve has finished (the reference's solve() is synchronous through its timer).
+ *   - One handle is used by one thread at a time.
+ */
+#ifndef PDT_H
+#define PDT_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define PDT_API __attribute__((visibility("default")))
+#else
+#define PDT_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum pdt_status {
+  PDT_OK = 0,
+  PDT_ERR_INVALID_ARGUMENT = 1, /* null handle / pointer, unknown enum value, bad ndim */
+  PDT_ERR_SIZE = 2,             /* IU_SIZE_CHECK failures (e.g. mricartesianoperator.cu:177-179) */
+  PDT_ERR_CONSTANTS = 3,        /* constant count / index / type (operatorbase.h:241-256, 266-287, 493-502) */
+  PDT_ERR_CONFIG = 4,           /* OpConfig count or parse (operatorbase.h:219-228, 404-480) */
+  PDT_ERR_STATE = 5,            /* "No operator is set!", "No noisy data is set!" (tgvmrioptimizer.cu:96-110) */
+  PDT_ERR_CUDA = 6,             /* a CUDA runtime error */
+  PDT_ERR_UNSUPPORTED = 7,      /* a size or kind this build does not handle */
+  PDT_ERR_NUMERIC = 8,          /* non-finite values detected */
+  PDT_ERR_TIMEOUT = 9,          /* a bounded device wait gave up */
+  PDT_ERR_ALLOC = 10            /* device or pinned allocation failed */
+} pdt_status;
+
+typedef enum pdt_dtype {
+  PDT_F32 = 0, /* float  (reference floatX = float, python/pyDenoising.cpp:26-29) */
+  PDT_C64 = 1  /* float2 (reference complexX, python/pyMriReconstruction.cpp:39-42) */
+} pdt_dtype;
+
+typedef enum pdt_op_kind {
+  PDT_OP_CARTESIAN = 0,         /* MriCartesianOperator          (mricartesianoperator.h:31-70) */
+  PDT_OP_CARTESIAN_ROOS = 1,    /* MriCartesianRemoveROOSOperator (mricartesianoperator.h:72-118) */
+  PDT_OP_SAMPLING = 2,          /* MriSamplingOperator           (mrisamplingoperator.h:30-66) */
+  PDT_OP_RADIAL = 3,            /* MriRadialOperator             (mriradialoperator.h:35-95) */
+  PDT_OP_RADIAL_SINGLECOIL = 4  /* MriRadialSinglecoilOperator   (mriradialoperator.h:97-155) */
+} pdt_op_kind;
+
+typedef enum pdt_opt_kind {
+  PDT_OPT_TV = 0,      /* TvOptimizer         (tvoptimizer.h:47-121) */
+  PDT_OPT_TGV = 1,     /* TgvOptimizer        (tgvoptimizer.h:70-142) */
+  PDT_OPT_TV_OP = 2,   /* TvOptimizerWithOp   (tvoptimizerwithop.h:30-100) */
+  PDT_OPT_TGV_OP = 3,  /* TgvOptimizerWithOp  (tgvoptimizerwithop.h:30-113) */
+  PDT_OPT_TGV_MRI = 4  /* TgvMriOptimizer     (tgvmrioptimizer.h:73-150) */
+} pdt_opt_kind;
+
+/* One OpConfig entry (operatorbase.h:52-151: std::map<std::string, std::string>). */
+typedef struct pdt_kv {
+  const char* key;
+  const char* value;
+} pdt_kv;
+
+/* Union of TvParameters (tvoptimizer.h:31-45), TgvParameters (tgvoptimizer.h:34-66) and
+ * TgvMriParameters (tgvmrioptimizer.h:32-66); fields an optimizer does not use are ignored.
+ * Defaults as in the reference constructors: alpha0 = alpha1 = lambda = reduction = 1,
+ * max_iter = 1, check = 100. */
+typedef struct pdt_params {
+  double alpha0;
+  double alpha1;
+  double lambda;
+  double reduction;
+  uint32_t max_iter;
+  uint32_t check;
+} pdt_params;
+
+typedef struct pdt_op pdt_op;
+typedef struct pdt_opt pdt_opt;
+
+/* ---- library ------------------------------------------------------------------------------------ */
+PDT_API const char* pdt_last_error(void);  /* replaces IuException::what() across the ABI */
+PDT_API int pdt_version(void);
+/* Number of CUDA kernels this library has launched since it was loaded (graph replays count every
+ * kernel node). Used by benchmarks to prove the native path ran. */
+PDT_API uint64_t pdt_launch_count(void);
+PDT_API pdt_status pdt_host_alloc(size_t bytes, void** out); /* pinned host memory for fast H2D/D2H */
+PDT_API pdt_status pdt_host_free(void* p);
+PDT_API pdt_status pdt_stream_synchronize(void* stream);
+
+/* ---- operators (OperatorBase<InputType, OutputType>, operatorbase.h:196-507) ---------------------- */
+/* Constructor. Cartesian / sampling operators take no config (ncfg = 0); radial operators need exactly
+ * the four keys osf, sector_width, kernel_width, img_dim (mriradialoperator.cu:28-35). */
+PDT_API pdt_status pdt_op_create(pdt_op_kind kind, const pdt_kv* cfg, int ncfg, pdt_op** out);
+/* Releases the caller's reference; an optimizer that was given the operator keeps it alive
+ * (the reference shares it through std::shared_ptr, tgvmrioptimizer.h:121). */
+PDT_API pdt_status pdt_op_destroy(pdt_op* op);
+/* OperatorBase::addConstant (operatorbase.h:238-257): positional constants, copied to the device.
+ * Cartesian: #0 coil sensitivities C64 {W,H,C}, #1 mask F32 {W,H}. Sampling: #0 mask F32 {W,H}.
+ * Radial: #0 trajectory F32 {Ns,2}, #1 dcf F32 {Ns,1}, #2 coil sensitivities C64 {N,N,C} (multi-coil). */
+PDT_API pdt_status pdt_op_add_constant(pdt_op* op, pdt_dtype dtype, int ndim, const int64_t* size, const void* data,
+                               int is_device);
+/* OperatorBase::getInputSize / getOutputSize (operatorbase.h:328-340). */
+PDT_API pdt_status pdt_op_input_size(pdt_op* op, int out_ndim, const int64_t* out_size, int* in_ndim, int64_t* in_size);
+PDT_API pdt_status pdt_op_output_size(pdt_op* op, int in_ndim, const int64_t* in_size, int* out_ndim, int64_t* out_size);
+/* OperatorBase::forward / adjoint (operatorbase.h:297-312): constant-count and size checks, then
+ * executeForward / executeAdjoint. src and dst are both device or both host buffers. */
+PDT_API pdt_status pdt_op_forward(pdt_op* op, const void* src, int src_ndim, const int64_t* src_size, void* dst,
+                          int dst_ndim, const int64_t* dst_size, int is_device, void* stream);
+PDT_API pdt_status pdt_op_adjoint(pdt_op* op, const void* src, int src_ndim, const int64_t* src_size, void* dst,
+                          int dst_ndim, const int64_t* dst_size, int is_device, void* stream);
+/* OperatorBase::print (operatorbase.h:343-351), e.g. "MriCartesianOperator: Added constants: (2/2)". */
+PDT_API pdt_status pdt_op_describe(pdt_op* op, char* buf, size_t len);
+/* adjointnessCheck (mricartesianoperator.cu:267-282 and siblings): random u, p (seeded), returns
+ * <Au, p> and <u, A^H p> accumulated in double. */
+PDT_API pdt_status pdt_op_adjointness(pdt_op* op, uint64_t seed, double out[4]);
+
+/* ---- optimizers --------------------------------------------------------------------------------- */
+/* dtype: PDT_F32 for the real denoising optimizers (*_2f), PDT_C64 for complex ones. */
+PDT_API pdt_status pdt_opt_create(pdt_opt_kind kind, pdt_dtype dtype, pdt_opt** out);
+PDT_API pdt_status pdt_opt_destroy(pdt_opt* opt);
+/* getParameters() (tgvmrioptimizer.h:109-112): read and write the parameter struct. */
+PDT_API pdt_status pdt_opt_get_params(pdt_opt* opt, pdt_params* out);
+PDT_API pdt_status pdt_opt_set_params(pdt_opt* opt, const pdt_params* params);
+/* setOperator (tgvmrioptimizer.cu:55-60). */
+PDT_API pdt_status pdt_opt_set_operator(pdt_opt* opt, pdt_op* op);
+/* setNoisyData (tgvmrioptimizer.cu:81-91): copies f to the device and resets the k-space dual r to 0. */
+PDT_API pdt_status pdt_opt_set_noisy_data(pdt_opt* opt, const void* f, int ndim, const int64_t* size, int is_device,
+                                  void* stream);
+/* setInput0 (tgvmrioptimizer.cu:62-79): u = u-bar = input, v = v-bar = p = q = 0. */
+PDT_API pdt_status pdt_opt_set_input0(pdt_opt* opt, const void* u0, int ndim, const int64_t* size, int is_device,
+                              void* stream);
+/* solve (tgvmrioptimizer.cu:93-203, tvoptimizer.cu:76-125, tgvoptimizer.cu:80-141, ...): runs
+ * max_iter + 1 iterations from the current state (u0 = A^H f or f when no state is set). */
+PDT_API pdt_status pdt_opt_solve(pdt_opt* opt, int verbose, void* stream);
+/* getResult (tgvmrioptimizer.cu:48-52): size query, then a copy of u into dst. */
+PDT_API pdt_status pdt_opt_result_size(pdt_opt* opt, int* ndim, int64_t* size);
+PDT_API pdt_status pdt_opt_get_result(pdt_opt* opt, void* dst, int is_device, void* stream);
+/* No reference counterpart (the reference only prints the whole solve time, tgvmrioptimizer.cu:202):
+ * runs `iters` further iterations launch by launch with a CUDA event after every kernel phase on
+ * `stream` and returns each phase's mean duration in ms, phase names comma-separated in `names`.
+ * The iterations advance the optimizer state exactly like solve(). */
+PDT_API pdt_status pdt_opt_profile(pdt_opt* opt, int iters, void* stream, int max_phases, int* nphases, char* names,
+                                   size_t names_len, double* ms);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PDT_H */

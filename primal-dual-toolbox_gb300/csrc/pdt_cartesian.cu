@@ -1,0 +1,472 @@
+// pdt_cartesian.cu -- Cartesian multi-coil MRI operators (plain and readout-oversampling removal) and
+// the single-coil sampling operator, as three shared-memory FFT phases.
+//
+// Reference: MriCartesianOperator / MriCartesianRemoveROOSOperator (mricartesianoperator.cu:27-414)
+// and MriSamplingOperator (mrisamplingoperator.cu:58-88):
+//   forward  K u = mask . fftshift2( fft2( ifftshift2( pad(u) . sens_c ) ) / sqrt(W H) )
+//   adjoint  K^H k = crop( sum_c conj(sens_c) . fftshift2( ifft2( ifftshift2( mask . k_c ) ) / sqrt(W H) ) )
+// with ifftshift written as dst[(i + mid) % n] = src[i], mid = int((n+1)/2) (mricartesianoperator.cu:41-49),
+// fftshift2 as dst[(i + n/2) % n] = src[i], and the ROOS image occupying frequency-encode rows
+// [FE_idx, FE_idx + H/2) with FE_idx = unsigned(H * 0.25f + 1) (mricartesianoperator.cu:341).
+//
+// GB300 layout. W = phase-encode (contiguous), Hf = frequency-encode, C = coils. Shifts, padding and
+// cropping are folded into the FFT load/store index maps, and only phase-encode columns with a
+// non-zero mask entry ("sampled columns", ns of W) are ever transformed along Hf:
+//   rows_fwd  (row blocks x coils)   ubar . sens -> FFT along W -> t[c][s][yi] for sampled columns
+//   cols      (column blocks x coils) pruned FFT along Hf -> mask -> k-space dual prox -> mask -> IFFT
+//   rows_adj  (row blocks x coil groups) t -> IFFT along W -> conj(sens) . -> coil sum
+// The k-space dual r and the data f live in the compact layout [c][s][Hf] (sampled columns only);
+// the entries of unsampled columns never reach u in the reference either (the mask zeroes them).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <sstream>
+
+#include "pdt_device.cuh"
+#include "pdt_fftplan.h"
+#include "pdt_ops.h"
+
+namespace pdt {
+
+namespace {
+
+constexpr int kThreads = 256;
+
+struct CartDev {
+  int W, Hf, C, Hi, y0, ns;
+  int mxW, mxH;  // ifftshift mids: int((n+1)/2)
+  int oxW, oyH;  // fftshift mids: n/2
+  float scale;   // 1/sqrt(W*Hf)
+  int RB, CB, ldW, ldH;
+  const float2* sens;   // (W, Hf, C) or null (sampling operator)
+  const float* maskc;   // [ns][Hf] mask values of sampled columns, by output row
+  const int* fwd_slot;  // [ns] forward-FFT output slot of sampled column s
+  const int* col_x;     // [ns] k-space column of s
+  const int* slot2s;    // [W] inverse-FFT input slot -> s (or -1)
+  const float2* twW;
+  const float2* twH;
+  FftPlan planW, planH;
+};
+
+enum ColMode { COL_SOLVE = 0, COL_FWD_DENSE = 1, COL_ADJ_DENSE = 2, COL_ADJ_COMPACT = 3 };
+
+__device__ __forceinline__ int imod(int a, int n) {
+  a %= n;
+  return a < 0 ? a + n : a;
+}
+
+// Phase 1: rows of ubar (x sens_c) -> FFT along W; keep the sampled columns.
+__global__ void __launch_bounds__(kThreads) rows_fwd_kernel(CartDev d, const float2* __restrict__ ubar,
+                                                            float2* __restrict__ t1, int* __restrict__ tick) {
+  if (tick && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) atomicAdd(tick, 1);
+  extern __shared__ float2 sm[];
+  float2* tw = sm;
+  float2* A = tw + d.W;
+  float2* B = A + d.RB * d.ldW;
+  const int yi0 = blockIdx.x * d.RB;
+  const int c = blockIdx.y;
+  const int nr = min(d.RB, d.Hi - yi0);
+  for (int i = threadIdx.x; i < d.W; i += blockDim.x) tw[i] = d.twW[i];
+  for (int i = threadIdx.x; i < nr * d.W; i += blockDim.x) {
+    const int r = i / d.W, x = i - r * d.W;
+    const int yi = yi0 + r;
+    float2 v = ubar[(size_t)yi * d.W + x];
+    if (d.sens) v = cmul(v, d.sens[((size_t)c * d.Hf + yi + d.y0) * d.W + x]);  // prefft_kernel
+    int slot = x + d.mxW;
+    if (slot >= d.W) slot -= d.W;
+    A[r * d.ldW + slot] = v;
+  }
+  __syncthreads();
+  const float2* X = smem_fft(A, B, nr, d.ldW, d.planW, tw, false);
+  for (int i = threadIdx.x; i < d.ns * nr; i += blockDim.x) {
+    const int s = i / nr, r = i - s * nr;
+    t1[((size_t)c * d.ns + s) * d.Hi + yi0 + r] = X[r * d.ldW + d.fwd_slot[s]];
+  }
+}
+
+// Phase 2: per sampled column, FFT along Hf (input non-zero on the Hi image rows), mask, and -- in
+// solve mode -- the k-space dual prox r = (r + sigma (K u - f)) / (1 + sigma lambda) followed by the
+// adjoint's mask . r -> IFFT along Hf restricted to the image rows.
+__global__ void __launch_bounds__(kThreads) cols_kernel(CartDev d, int mode, const float2* t_in, float2* t_out,
+                                                        float2* __restrict__ r, const float2* __restrict__ fc,
+                                                        const float2* __restrict__ kin, float2* __restrict__ kout,
+                                                        float sigma, float lambda) {
+  extern __shared__ float2 sm[];
+  float2* tw = sm;
+  float2* A = tw + d.Hf;
+  float2* B = A + d.CB * d.ldH;
+  const int s0 = blockIdx.x * d.CB;
+  const int c = blockIdx.y;
+  const int ncb = min(d.CB, d.ns - s0);
+  const int Hf = d.Hf;
+  for (int i = threadIdx.x; i < Hf; i += blockDim.x) tw[i] = d.twH[i];
+
+  float2* Y;  // inverse-FFT input buffer
+  float2* Yo;
+  if (mode == COL_SOLVE || mode == COL_FWD_DENSE) {
+    for (int i = threadIdx.x; i < ncb * Hf; i += blockDim.x) {
+      const int cb = i / Hf, j = i - cb * Hf;
+      const int yf = imod(j - d.mxH, Hf);  // image row that lands in FFT slot j after ifftshift
+      const int yi = yf - d.y0;
+      float2 v = c2(0.f, 0.f);
+      if (yi >= 0 && yi < d.Hi) v = t_in[((size_t)c * d.ns + s0 + cb) * d.Hi + yi];
+      A[cb * d.ldH + j] = v;
+    }
+    __syncthreads();
+    float2* X = smem_fft(A, B, ncb, d.ldH, d.planH, tw, false);
+    Y = (X == A) ? B : A;
+    for (int i = threadIdx.x; i < ncb * Hf; i += blockDim.x) {
+      const int cb = i / Hf, ky = i - cb * Hf;
+      const int s = s0 + cb;
+      int ypos = ky + d.oyH;
+      if (ypos >= Hf) ypos -= Hf;
+      const float m = d.maskc[(size_t)s * Hf + ypos];
+      const float2 k = X[cb * d.ldH + ky] * d.scale * m;  // fft2(..)/sqrt(N), fftshift2, applyMask
+      if (mode == COL_FWD_DENSE) {
+        kout[((size_t)c * Hf + ypos) * d.W + d.col_x[s]] = k;
+      } else {
+        const size_t o = ((size_t)c * d.ns + s) * Hf + ypos;
+        // addWeighted(tmp, 1, f, -1) then TGV_prox_r_kernel (tgvmrioptimizer.cu:167-174)
+        const float2 rn = (r[o] + sigma * (k - fc[o])) / (1.0f + sigma * lambda);
+        r[o] = rn;
+        Y[cb * d.ldH + imod(ypos + d.mxH, Hf)] = rn * m;  // preifft_kernel
+      }
+    }
+    if (mode == COL_FWD_DENSE) return;
+    Yo = X;
+  } else {
+    Y = A;
+    Yo = B;
+    for (int i = threadIdx.x; i < ncb * Hf; i += blockDim.x) {
+      const int cb = i / Hf, ypos = i - cb * Hf;
+      const int s = s0 + cb;
+      const float m = d.maskc[(size_t)s * Hf + ypos];
+      const float2 v = (mode == COL_ADJ_DENSE) ? kin[((size_t)c * Hf + ypos) * d.W + d.col_x[s]]
+                                               : fc[((size_t)c * d.ns + s) * Hf + ypos];
+      Y[cb * d.ldH + imod(ypos + d.mxH, Hf)] = v * m;
+    }
+  }
+  __syncthreads();
+  const float2* Z = smem_fft(Y, Yo, ncb, d.ldH, d.planH, tw, true);
+  for (int i = threadIdx.x; i < ncb * Hf; i += blockDim.x) {
+    const int cb = i / Hf, j = i - cb * Hf;
+    int yf = j + d.oyH;
+    if (yf >= Hf) yf -= Hf;
+    const int yi = yf - d.y0;  // cropFOV
+    if (yi >= 0 && yi < d.Hi) t_out[((size_t)c * d.ns + s0 + cb) * d.Hi + yi] = Z[cb * d.ldH + j] * d.scale;
+  }
+}
+
+// Phase 3: per image row block and coil group, IFFT along W of the sampled columns, multiply by
+// conj(sens_c) and sum the group's coils in coil order (combineImg_kernel, mricartesianoperator.cu:99-126).
+__global__ void __launch_bounds__(kThreads) rows_adj_kernel(CartDev d, const float2* __restrict__ t2,
+                                                            float2* __restrict__ out, int G, long long gstride) {
+  extern __shared__ float2 sm[];
+  float2* tw = sm;
+  float2* A = tw + d.W;
+  float2* B = A + d.RB * d.ldW;
+  float2* acc = B + d.RB * d.ldW;
+  const int yi0 = blockIdx.x * d.RB;
+  const int g = blockIdx.y;
+  const int nr = min(d.RB, d.Hi - yi0);
+  const int c_begin = (int)((long long)g * d.C / G), c_end = (int)((long long)(g + 1) * d.C / G);
+  for (int i = threadIdx.x; i < d.W; i += blockDim.x) tw[i] = d.twW[i];
+  for (int i = threadIdx.x; i < nr * d.W; i += blockDim.x) acc[i] = c2(0.f, 0.f);
+  for (int c = c_begin; c < c_end; ++c) {
+    for (int i = threadIdx.x; i < nr * d.W; i += blockDim.x) {
+      const int j = i / nr, r = i - j * nr;
+      const int s = d.slot2s[j];
+      A[r * d.ldW + j] = (s >= 0) ? t2[((size_t)c * d.ns + s) * d.Hi + yi0 + r] : c2(0.f, 0.f);
+    }
+    __syncthreads();
+    const float2* Z = smem_fft(A, B, nr, d.ldW, d.planW, tw, true);
+    for (int i = threadIdx.x; i < nr * d.W; i += blockDim.x) {
+      const int r = i / d.W, j = i - r * d.W;
+      int x = j + d.oxW;
+      if (x >= d.W) x -= d.W;
+      float2 v = Z[r * d.ldW + j];
+      if (d.sens) v = cmulc(v, d.sens[((size_t)c * d.Hf + yi0 + r + d.y0) * d.W + x]);
+      acc[r * d.W + x] += v;
+    }
+    __syncthreads();
+  }
+  for (int i = threadIdx.x; i < nr * d.W; i += blockDim.x) {
+    const int r = i / d.W, x = i - r * d.W;
+    out[(size_t)g * gstride + (size_t)(yi0 + r) * d.W + x] = acc[i];
+  }
+}
+
+// dense user k-space (W, Hf, C) -> compact [c][s][Hf]
+__global__ void gather_kernel(CartDev d, const float2* __restrict__ dense, float2* __restrict__ compact) {
+  const size_t n = (size_t)d.C * d.ns * d.Hf;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const int ypos = (int)(i % d.Hf);
+    const size_t cs = i / d.Hf;
+    const int s = (int)(cs % d.ns), c = (int)(cs / d.ns);
+    compact[i] = dense[((size_t)c * d.Hf + ypos) * d.W + d.col_x[s]];
+  }
+}
+
+size_t rows_smem(const CartDev& d, bool with_acc) {
+  return sizeof(float2) * ((size_t)d.W + 2 * (size_t)d.RB * d.ldW + (with_acc ? (size_t)d.RB * d.W : 0));
+}
+size_t cols_smem(const CartDev& d) { return sizeof(float2) * ((size_t)d.Hf + 2 * (size_t)d.CB * d.ldH); }
+
+int g_num_sms = 0;
+int g_max_smem = 0;
+void query_device() {
+  if (g_num_sms) return;
+  int dev = 0;
+  PDT_CUDA_CHECK(cudaGetDevice(&dev));
+  PDT_CUDA_CHECK(cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev));
+  PDT_CUDA_CHECK(cudaDeviceGetAttribute(&g_max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  PDT_CUDA_CHECK(cudaFuncSetAttribute(rows_fwd_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, g_max_smem));
+  PDT_CUDA_CHECK(cudaFuncSetAttribute(rows_adj_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, g_max_smem));
+  PDT_CUDA_CHECK(cudaFuncSetAttribute(cols_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, g_max_smem));
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------------------------------------
+// Operator object
+// ------------------------------------------------------------------------------------------------
+class CartesianOp : public OpImpl, public SolverHooks {
+ public:
+  CartesianOp(pdt_op_kind kind)
+      : OpImpl(kind,
+               kind == PDT_OP_CARTESIAN        ? "MriCartesianOperator"
+               : kind == PDT_OP_CARTESIAN_ROOS ? "MriCartesianRemoveROOSOperator"
+                                               : "MriSamplingOperator",
+               kind == PDT_OP_SAMPLING ? 1u : 2u, {}) {}
+
+  // getInputSize / getOutputSize (mricartesianoperator.cu:183-194, 291-303; mrisamplingoperator.cu:40-51)
+  Dims input_size(const Dims& out) override {
+    if (out.size() < 2) throw Error(PDT_ERR_SIZE, name_ + ": output must have at least 2 dimensions");
+    if (kind_ == PDT_OP_CARTESIAN_ROOS) return {out[0], out[1] / 2};
+    if (kind_ == PDT_OP_SAMPLING) return out;
+    return {out[0], out[1]};
+  }
+  Dims output_size(const Dims& in) override {
+    (void)in;
+    if (kind_ == PDT_OP_SAMPLING) return in;
+    return constant(0, PDT_C64, 3).size;
+  }
+  SolverHooks* hooks() override { return this; }
+  Dims natural_input_size() override {
+    if (kind_ == PDT_OP_SAMPLING) return constant(0, PDT_F32, 2).size;
+    const Dims& m = constant(1, PDT_F32, 2).size;
+    return kind_ == PDT_OP_CARTESIAN_ROOS ? Dims{m[0], m[1] / 2} : m;
+  }
+
+  // SolverHooks
+  size_t compact_elems() override {
+    prepare();
+    return (size_t)dev_.C * dev_.ns * dev_.Hf;
+  }
+  void gather(const float2* dense, float2* compact, cudaStream_t st) override {
+    prepare();
+    if (dev_.ns == 0) return;
+    const size_t n = (size_t)dev_.C * dev_.ns * dev_.Hf;
+    const int blocks = (int)std::min<size_t>((n + 255) / 256, 4096);
+    gather_kernel<<<blocks, 256, 0, st>>>(dev_, dense, compact);
+    PDT_LAUNCH_CHECK();
+    count_launch();
+  }
+  int groups() override {
+    prepare();
+    return G_;
+  }
+  long long group_stride() override { return (long long)dev_.Hi * dev_.W; }
+  void round(const float2* ubar, float2* r, const float2* fc, float sigma, float lambda, float2* khr, int* tick,
+             cudaStream_t st, PhaseMarker* mk) override {
+    prepare();
+    if (dev_.ns == 0) {
+      launch_fill_zero(khr, sizeof(float2) * (size_t)G_ * dev_.Hi * dev_.W, st);
+      if (tick) launch_tick(tick, st);
+      return;
+    }
+    float2* t = scratch_.as<float2>();
+    launch_rows_fwd(ubar, t, tick, st);
+    if (mk) mk->mark("cart_rows_fwd", st);
+    launch_cols(COL_SOLVE, t, t, r, fc, nullptr, nullptr, sigma, lambda, st);
+    if (mk) mk->mark("cart_cols_prox", st);
+    launch_rows_adj(t, khr, G_, st);
+    if (mk) mk->mark("cart_rows_adj", st);
+  }
+  void adjoint_compact(const float2* fc, float2* img, cudaStream_t st) override {
+    prepare();
+    if (dev_.ns == 0) {
+      launch_fill_zero(img, sizeof(float2) * (size_t)dev_.Hi * dev_.W, st);
+      return;
+    }
+    float2* t = scratch_.as<float2>();
+    launch_cols(COL_ADJ_COMPACT, nullptr, t, nullptr, fc, nullptr, nullptr, 0.f, 0.f, st);
+    launch_rows_adj(t, img, 1, st);
+  }
+
+ protected:
+  // sizeCheck (mricartesianoperator.cu:174-181, 305-314; mrisamplingoperator.cu:32-38)
+  void size_check(const Dims& src, const Dims& dst) override {
+    if (kind_ == PDT_OP_SAMPLING) {
+      const Dims& m = constant(0, PDT_F32, 2).size;
+      size_check_eq(dst, m);
+      size_check_eq(src, m);
+      return;
+    }
+    const Dims& s = constant(0, PDT_C64, 3).size;
+    const Dims& m = constant(1, PDT_F32, 2).size;
+    size_check_eq(dst, s);
+    if (kind_ == PDT_OP_CARTESIAN_ROOS) {
+      if (src.size() != 2) throw Error(PDT_ERR_SIZE, name_ + ": image must be 2-D, got " + dims_str(src));
+      size_check_eq(Dims{src[0], src[1] * 2}, m);
+    } else {
+      size_check_eq(src, m);
+      size_check_eq(src, Dims{dst[0], dst[1]});
+    }
+  }
+  void execute_forward(const float2* src, float2* dst, cudaStream_t st) override {
+    prepare();
+    launch_fill_zero(dst, sizeof(float2) * (size_t)dev_.C * dev_.Hf * dev_.W, st);
+    if (dev_.ns == 0) return;
+    float2* t = scratch_.as<float2>();
+    launch_rows_fwd(src, t, nullptr, st);
+    launch_cols(COL_FWD_DENSE, t, nullptr, nullptr, nullptr, nullptr, dst, 0.f, 0.f, st);
+  }
+  void execute_adjoint(const float2* src, float2* dst, cudaStream_t st) override {
+    prepare();
+    if (dev_.ns == 0) {
+      launch_fill_zero(dst, sizeof(float2) * (size_t)dev_.Hi * dev_.W, st);
+      return;
+    }
+    float2* t = scratch_.as<float2>();
+    launch_cols(COL_ADJ_DENSE, nullptr, t, nullptr, nullptr, src, nullptr, 0.f, 0.f, st);
+    launch_rows_adj(t, dst, 1, st);
+  }
+  void invalidate() override { prepared_ = false; }
+
+ private:
+  void launch_rows_fwd(const float2* ubar, float2* t1, int* tick, cudaStream_t st) {
+    dim3 grid((dev_.Hi + dev_.RB - 1) / dev_.RB, dev_.C);
+    rows_fwd_kernel<<<grid, kThreads, rows_smem(dev_, false), st>>>(dev_, ubar, t1, tick);
+    PDT_LAUNCH_CHECK();
+    count_launch();
+  }
+  void launch_cols(int mode, const float2* tin, float2* tout, float2* r, const float2* fc, const float2* kin,
+                   float2* kout, float sigma, float lambda, cudaStream_t st) {
+    dim3 grid((dev_.ns + dev_.CB - 1) / dev_.CB, dev_.C);
+    cols_kernel<<<grid, kThreads, cols_smem(dev_), st>>>(dev_, mode, tin, tout, r, fc, kin, kout, sigma, lambda);
+    PDT_LAUNCH_CHECK();
+    count_launch();
+  }
+  void launch_rows_adj(const float2* t2, float2* out, int G, cudaStream_t st) {
+    dim3 grid((dev_.Hi + dev_.RB - 1) / dev_.RB, G);
+    rows_adj_kernel<<<grid, kThreads, rows_smem(dev_, true), st>>>(dev_, t2, out, G, (long long)dev_.Hi * dev_.W);
+    PDT_LAUNCH_CHECK();
+    count_launch();
+  }
+
+  // Builds the sampled-column tables, twiddles and FFT plans from the current constants.
+  void prepare() {
+    if (prepared_) return;
+    query_device();
+    const bool samp = kind_ == PDT_OP_SAMPLING;
+    Constant& mk = samp ? constant(0, PDT_F32, 2) : constant(1, PDT_F32, 2);
+    const int W = (int)mk.size[0], Hf = (int)mk.size[1];
+    int C = 1;
+    const float2* sens = nullptr;
+    if (!samp) {
+      Constant& sc = constant(0, PDT_C64, 3);
+      if (sc.size[0] != W || sc.size[1] != Hf)
+        throw Error(PDT_ERR_SIZE, name_ + ": coil sensitivities " + dims_str(sc.size) + " do not match mask " +
+                                      dims_str(mk.size));
+      C = (int)sc.size[2];
+      sens = sc.dev.as<float2>();
+    }
+    CartDev d{};
+    d.W = W;
+    d.Hf = Hf;
+    d.C = C;
+    if (kind_ == PDT_OP_CARTESIAN_ROOS) {
+      d.Hi = Hf / 2;
+      d.y0 = (int)(unsigned int)((float)(unsigned int)(2 * d.Hi) * 0.25f + 1.f);
+      if (d.y0 + d.Hi > Hf)
+        throw Error(PDT_ERR_SIZE, name_ + ": frequency-encode size " + std::to_string(Hf) + " too small");
+    } else {
+      d.Hi = Hf;
+      d.y0 = 0;
+    }
+    d.mxW = (int)(((float)W + 1.f) / 2.f);
+    d.mxH = (int)(((float)Hf + 1.f) / 2.f);
+    d.oxW = W / 2;
+    d.oyH = Hf / 2;
+    d.scale = (float)(1.0 / std::sqrt((double)W * (double)Hf));
+    d.sens = sens;
+    if (!make_fft_plan(W, &d.planW) || !make_fft_plan(Hf, &d.planH))
+      throw Error(PDT_ERR_UNSUPPORTED, name_ + ": cannot plan FFT sizes " + std::to_string(W) + " x " +
+                                           std::to_string(Hf));
+    // sampled columns
+    const float* mask = reinterpret_cast<const float*>(mk.host.data());
+    std::vector<int> col_x;
+    for (int x = 0; x < W; ++x)
+      for (int y = 0; y < Hf; ++y)
+        if (mask[(size_t)y * W + x] != 0.0f) {
+          col_x.push_back(x);
+          break;
+        }
+    d.ns = (int)col_x.size();
+    std::vector<int> fwd_slot(d.ns), slot2s(W, -1);
+    std::vector<float> maskc((size_t)d.ns * Hf);
+    for (int s = 0; s < d.ns; ++s) {
+      const int x = col_x[s];
+      fwd_slot[s] = ((x - d.oxW) % W + W) % W;
+      slot2s[(x + d.mxW) % W] = s;
+      for (int y = 0; y < Hf; ++y) maskc[(size_t)s * Hf + y] = mask[(size_t)y * W + x];
+    }
+    // launch shapes
+    d.ldW = W + 1;
+    d.ldH = Hf + 1;
+    d.RB = 4;
+    d.CB = 4;
+    while (d.RB > 1 && rows_smem(d, true) > (size_t)g_max_smem) d.RB /= 2;
+    while (d.CB > 1 && cols_smem(d) > (size_t)g_max_smem) d.CB /= 2;
+    if (rows_smem(d, true) > (size_t)g_max_smem || cols_smem(d) > (size_t)g_max_smem)
+      throw Error(PDT_ERR_UNSUPPORTED, name_ + ": FFT size too large for shared memory");
+    // device tables (one allocation, 16-byte aligned sub-arrays)
+    std::vector<float2> twW(W), twH(Hf);
+    fill_twiddles(W, twW.data());
+    fill_twiddles(Hf, twH.data());
+    const size_t need = 16 * 8 + sizeof(int) * (2 * (size_t)d.ns + W) + sizeof(float) * maskc.size() +
+                        sizeof(float2) * ((size_t)W + Hf);
+    tables_.ensure(need);
+    char* base = tables_.as<char>();
+    size_t off = 0;
+    auto put = [&](const void* src, size_t bytes) {
+      off = (off + 15) & ~(size_t)15;
+      char* dst = base + off;
+      if (bytes) PDT_CUDA_CHECK(cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice));
+      off += bytes;
+      return dst;
+    };
+    d.twW = reinterpret_cast<const float2*>(put(twW.data(), sizeof(float2) * W));
+    d.twH = reinterpret_cast<const float2*>(put(twH.data(), sizeof(float2) * Hf));
+    d.fwd_slot = reinterpret_cast<const int*>(put(fwd_slot.data(), sizeof(int) * d.ns));
+    d.col_x = reinterpret_cast<const int*>(put(col_x.data(), sizeof(int) * d.ns));
+    d.slot2s = reinterpret_cast<const int*>(put(slot2s.data(), sizeof(int) * W));
+    d.maskc = reinterpret_cast<const float*>(put(maskc.data(), sizeof(float) * maskc.size()));
+    scratch_.ensure(std::max<size_t>(1, (size_t)C * d.ns * d.Hi) * sizeof(float2));
+    // coil groups for the adjoint row phase: enough blocks for two waves
+    const int row_blocks = (d.Hi + d.RB - 1) / d.RB;
+    G_ = std::max(1, std::min(C, (2 * g_num_sms + row_blocks - 1) / row_blocks));
+    dev_ = d;
+    prepared_ = true;
+  }
+
+  bool prepared_ = false;
+  CartDev dev_{};
+  int G_ = 1;
+  DevBuf tables_, scratch_;
+};
+
+std::shared_ptr<OpImpl> make_cartesian_operator(pdt_op_kind kind) { return std::make_shared<CartesianOp>(kind); }
+
+}  // namespace pdt

@@ -1,0 +1,366 @@
+// pdt_image.cu -- fused image-side primal-dual steps (TV, TGV^2, TV/TGV with an operator).
+//
+// Each kernel does one whole iteration's image-side work for a 32 x 8 tile: it stages the over-relaxed
+// primal (u-bar, v-bar) plus a one-pixel halo in shared memory, recomputes the dual update on the halo
+// pixels it needs, and finishes the primal update from shared memory. The reference does the same
+// arithmetic in two to four separate launches (tgv_kernels.cuh:225-324, 432-467, 568-605, 647-686),
+// each re-reading its neighbours from global memory.
+//
+// Fields read at a neighbour (u-bar, v-bar, p, q -- and u, v for the primal-first TGV order) ping-pong
+// between an `in` and an `out` buffer so that tiles never read a neighbour's freshly written values.
+//
+// Arithmetic follows the reference kernels element by element:
+//   grad+  (dp,   tgv_kernels.cuh:40-50)   Neumann forward differences, zero at x = W-1 / y = H-1
+//   eps(v) (dp_sym, :25-38)                [dx vx, 0.5 (dy vx + dx vy), dy vy]
+//   div-   (dm,   :67-80)                  x==0: p(0); x==W-1: -p(W-2); else p(x) - p(x-1)
+//   div_h- (dm_sym, :104-134)
+//   projections 1 / max(1, |.| / alpha) with |q|^2 = |qxx|^2 + |qyy|^2 + 2 |qxy|^2 (:136-154)
+//   over-relaxation theta = 1: bar = 2 new - old.
+#include "pdt_device.cuh"
+#include "pdt_internal.h"
+
+namespace pdt {
+namespace {
+
+constexpr int TX = 32;
+constexpr int TY = 8;
+constexpr int NT = TX * TY;
+
+// div- of a 2-component field held in shared memory at local coordinates (lx, ly); (gx, gy) are the
+// global coordinates used for the boundary rules.
+template <class P, int LDX>
+__device__ __forceinline__ P div_minus(const P (*sx)[LDX], const P (*sy)[LDX], int lx, int ly, int gx, int gy, int W,
+                                       int H) {
+  P d = (gx > 0) ? ((gx < W - 1) ? sx[ly][lx] - sx[ly][lx - 1] : -sx[ly][lx - 1]) : sx[ly][lx];
+  d += (gy > 0) ? ((gy < H - 1) ? sy[ly][lx] - sy[ly - 1][lx] : -sy[ly - 1][lx]) : sy[ly][lx];
+  return d;
+}
+
+__device__ __forceinline__ float proj_scale(float n, float alpha) { return 1.0f / fmaxf(1.0f, n / alpha); }
+
+// ------------------------------------------------------------------------------------------------
+// TvOptimizer: p <- proj_1(p + sigma grad+ ub); u+ = (u + tau (div- p + lambda f)) / (1 + tau lambda).
+// ------------------------------------------------------------------------------------------------
+template <class P>
+__global__ void __launch_bounds__(NT) tv_step_kernel(int W, int H, ImgPtrs in, ImgPtrs out,
+                                                     const P* __restrict__ f, float tau, float sigma, float lambda) {
+  __shared__ P s_ub[TY + 2][TX + 2];  // [x0-1, x0+TX] x [y0-1, y0+TY]
+  __shared__ P s_px[TY + 1][TX + 1];  // [x0-1, x0+TX) x [y0-1, y0+TY)
+  __shared__ P s_py[TY + 1][TX + 1];
+  const int tid = threadIdx.x;
+  const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
+  const P* ub = static_cast<const P*>(in.ub);
+  const P* px = static_cast<const P*>(in.px);
+  const P* py = static_cast<const P*>(in.py);
+
+  for (int i = tid; i < (TX + 2) * (TY + 2); i += NT) {
+    const int ly = i / (TX + 2), lx = i - ly * (TX + 2);
+    const int gx = x0 - 1 + lx, gy = y0 - 1 + ly;
+    if (gx >= 0 && gx < W && gy >= 0 && gy < H) s_ub[ly][lx] = ub[(size_t)gy * W + gx];
+  }
+  __syncthreads();
+
+  for (int i = tid; i < (TX + 1) * (TY + 1); i += NT) {
+    const int ly = i / (TX + 1), lx = i - ly * (TX + 1);
+    if (lx == 0 && ly == 0) continue;  // the corner is never read by div-
+    const int gx = x0 - 1 + lx, gy = y0 - 1 + ly;
+    if (gx < 0 || gx >= W || gy < 0 || gy >= H) continue;
+    const int xp = lx + (gx < W - 1), yp = ly + (gy < H - 1);
+    const P c = s_ub[ly][lx];
+    const P gux = s_ub[ly][xp] - c, guy = s_ub[yp][lx] - c;
+    const size_t idx = (size_t)gy * W + gx;
+    const P a = px[idx] + sigma * gux;
+    const P b = py[idx] + sigma * guy;
+    const float s = proj_scale(sqrtf(abs2(a) + abs2(b)), 1.0f);
+    const P pa = a * s, pb = b * s;
+    s_px[ly][lx] = pa;
+    s_py[ly][lx] = pb;
+    if (lx > 0 && ly > 0) {
+      static_cast<P*>(out.px)[idx] = pa;
+      static_cast<P*>(out.py)[idx] = pb;
+    }
+  }
+  __syncthreads();
+
+  const int lx = tid % TX + 1, ly = tid / TX + 1;
+  const int gx = x0 + lx - 1, gy = y0 + ly - 1;
+  if (gx < W && gy < H) {
+    const size_t idx = (size_t)gy * W + gx;
+    P* u = static_cast<P*>(out.u);
+    const P uo = u[idx];
+    const P d = div_minus<P, TX + 1>(s_px, s_py, lx, ly, gx, gy, W, H);
+    P un = uo + tau * (d + lambda * f[idx]);
+    un = un * (1.0f / (1.0f + tau * lambda));
+    u[idx] = un;
+    static_cast<P*>(out.ub)[idx] = 2.0f * un - uo;
+  }
+}
+
+// ------------------------------------------------------------------------------------------------
+// TgvOptimizer (primal first, tgvoptimizer.cu:117-137):
+//   u+ = (u + tau (div- p + lambda f)) / (1 + tau lambda), v+ = v + tau (div_h- q + p)
+//   p  <- proj_a1(p + sigma (grad+ ub - vb)),             q  <- proj_a0(q + sigma eps(vb))
+// ------------------------------------------------------------------------------------------------
+template <class P>
+__global__ void __launch_bounds__(NT) tgv_denoise_step_kernel(int W, int H, ImgPtrs in, ImgPtrs out,
+                                                              const P* __restrict__ f, float tau, float sigma,
+                                                              float lambda, float alpha0, float alpha1) {
+  // old duals on [x0-1, x0+TX] x [y0-1, y0+TY]
+  __shared__ P s_px[TY + 2][TX + 2], s_py[TY + 2][TX + 2];
+  __shared__ P s_qxx[TY + 2][TX + 2], s_qyy[TY + 2][TX + 2], s_qxy[TY + 2][TX + 2];
+  // new over-relaxed primals on [x0, x0+TX] x [y0, y0+TY]
+  __shared__ P s_ub[TY + 1][TX + 1], s_vbx[TY + 1][TX + 1], s_vby[TY + 1][TX + 1];
+  const int tid = threadIdx.x;
+  const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
+
+  for (int i = tid; i < (TX + 2) * (TY + 2); i += NT) {
+    const int ly = i / (TX + 2), lx = i - ly * (TX + 2);
+    const int gx = x0 - 1 + lx, gy = y0 - 1 + ly;
+    if (gx >= 0 && gx < W && gy >= 0 && gy < H) {
+      const size_t idx = (size_t)gy * W + gx;
+      s_px[ly][lx] = static_cast<const P*>(in.px)[idx];
+      s_py[ly][lx] = static_cast<const P*>(in.py)[idx];
+      s_qxx[ly][lx] = static_cast<const P*>(in.qxx)[idx];
+      s_qyy[ly][lx] = static_cast<const P*>(in.qyy)[idx];
+      s_qxy[ly][lx] = static_cast<const P*>(in.qxy)[idx];
+    }
+  }
+  __syncthreads();
+
+  for (int i = tid; i < (TX + 1) * (TY + 1); i += NT) {
+    const int ly = i / (TX + 1), lx = i - ly * (TX + 1);
+    const int gx = x0 + lx, gy = y0 + ly;
+    if (gx >= W || gy >= H) continue;
+    const size_t idx = (size_t)gy * W + gx;
+    const int sx = lx + 1, sy = ly + 1;  // position in the dual tiles
+    // TV_primal_u_kernel (tgv_kernels.cuh:568-605)
+    const P uo = static_cast<const P*>(in.u)[idx];
+    const P d = div_minus<P, TX + 2>(s_px, s_py, sx, sy, gx, gy, W, H);
+    P un = uo + tau * (d + lambda * f[idx]);
+    un = un * (1.0f / (1.0f + tau * lambda));
+    const P ubn = 2.0f * un - uo;
+    // TGV_primal_v_kernel (tgv_kernels.cuh:647-686)
+    const P vxo = static_cast<const P*>(in.vx)[idx], vyo = static_cast<const P*>(in.vy)[idx];
+    const P dqxx = (gx > 0) ? ((gx < W - 1) ? s_qxx[sy][sx] - s_qxx[sy][sx - 1] : -s_qxx[sy][sx - 1]) : s_qxx[sy][sx];
+    const P dqyy = (gy > 0) ? ((gy < H - 1) ? s_qyy[sy][sx] - s_qyy[sy - 1][sx] : -s_qyy[sy - 1][sx]) : s_qyy[sy][sx];
+    const P dqxyx = (gx > 0) ? ((gx < W - 1) ? s_qxy[sy][sx] - s_qxy[sy][sx - 1] : -s_qxy[sy][sx - 1]) : s_qxy[sy][sx];
+    const P dqxyy = (gy > 0) ? ((gy < H - 1) ? s_qxy[sy][sx] - s_qxy[sy - 1][sx] : -s_qxy[sy - 1][sx]) : s_qxy[sy][sx];
+    const P vxn = vxo + tau * ((dqxx + dqxyy) + s_px[sy][sx]);
+    const P vyn = vyo + tau * ((dqyy + dqxyx) + s_py[sy][sx]);
+    const P vbxn = 2.0f * vxn - vxo, vbyn = 2.0f * vyn - vyo;
+    s_ub[ly][lx] = ubn;
+    s_vbx[ly][lx] = vbxn;
+    s_vby[ly][lx] = vbyn;
+    if (lx < TX && ly < TY) {
+      static_cast<P*>(out.u)[idx] = un;
+      static_cast<P*>(out.ub)[idx] = ubn;
+      static_cast<P*>(out.vx)[idx] = vxn;
+      static_cast<P*>(out.vy)[idx] = vyn;
+      static_cast<P*>(out.vbx)[idx] = vbxn;
+      static_cast<P*>(out.vby)[idx] = vbyn;
+    }
+  }
+  __syncthreads();
+
+  const int lx = tid % TX, ly = tid / TX;
+  const int gx = x0 + lx, gy = y0 + ly;
+  if (gx < W && gy < H) {
+    const size_t idx = (size_t)gy * W + gx;
+    const int xp = lx + (gx < W - 1), yp = ly + (gy < H - 1);
+    // TGV_dual_p_kernel (tgv_kernels.cuh:260-292)
+    const P c = s_ub[ly][lx];
+    const P a = s_px[ly + 1][lx + 1] + sigma * ((s_ub[ly][xp] - c) - s_vbx[ly][lx]);
+    const P b = s_py[ly + 1][lx + 1] + sigma * ((s_ub[yp][lx] - c) - s_vby[ly][lx]);
+    const float sp = proj_scale(sqrtf(abs2(a) + abs2(b)), alpha1);
+    static_cast<P*>(out.px)[idx] = a * sp;
+    static_cast<P*>(out.py)[idx] = b * sp;
+    // TGV_dual_q_kernel (tgv_kernels.cuh:225-258)
+    const P vx = s_vbx[ly][lx], vy = s_vby[ly][lx];
+    const P gxx = s_vbx[ly][xp] - vx;
+    const P gxy = 0.5f * (s_vbx[yp][lx] - vx + s_vby[ly][xp] - vy);
+    const P gyy = s_vby[yp][lx] - vy;
+    const P qa = s_qxx[ly + 1][lx + 1] + sigma * gxx;
+    const P qb = s_qyy[ly + 1][lx + 1] + sigma * gyy;
+    const P qc = s_qxy[ly + 1][lx + 1] + sigma * gxy;
+    const float sq = proj_scale(sqrtf(abs2(qa) + abs2(qb) + 2.0f * abs2(qc)), alpha0);
+    static_cast<P*>(out.qxx)[idx] = qa * sq;
+    static_cast<P*>(out.qyy)[idx] = qb * sq;
+    static_cast<P*>(out.qxy)[idx] = qc * sq;
+  }
+}
+
+// ------------------------------------------------------------------------------------------------
+// TgvMriOptimizer / TgvOptimizerWithOp / TvOptimizerWithOp image side (dual first, K^H r given).
+//   p <- proj_a1(p + sigma (grad+ ub - vb)),  q <- proj_a0(q + sigma eps(vb))
+//   u+ = u + tau (div- p - K^H r),            v+ = v + tau (div_h- q + p)
+// u and v are read only at their own pixel and update in place.
+// ------------------------------------------------------------------------------------------------
+template <bool TGV>
+__global__ void __launch_bounds__(NT) mri_image_step_kernel(int W, int H, ImgPtrs in, ImgPtrs out,
+                                                            const float2* __restrict__ khr, int G, long long gstride,
+                                                            float tau, float sigma,
+                                                            const float* __restrict__ alpha_tab,
+                                                            const int* __restrict__ iter) {
+  __shared__ float2 s_ub[TY + 2][TX + 2];
+  __shared__ float2 s_vbx[TGV ? TY + 2 : 1][TX + 2], s_vby[TGV ? TY + 2 : 1][TX + 2];
+  __shared__ float2 s_px[TY + 1][TX + 1], s_py[TY + 1][TX + 1];
+  __shared__ float2 s_qxx[TGV ? TY + 1 : 1][TX + 1], s_qyy[TGV ? TY + 1 : 1][TX + 1], s_qxy[TGV ? TY + 1 : 1][TX + 1];
+  const int tid = threadIdx.x;
+  const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
+  const float2* ub = static_cast<const float2*>(in.ub);
+
+  for (int i = tid; i < (TX + 2) * (TY + 2); i += NT) {
+    const int ly = i / (TX + 2), lx = i - ly * (TX + 2);
+    const int gx = x0 - 1 + lx, gy = y0 - 1 + ly;
+    if (gx >= 0 && gx < W && gy >= 0 && gy < H) {
+      const size_t idx = (size_t)gy * W + gx;
+      s_ub[ly][lx] = ub[idx];
+      if constexpr (TGV) {
+        s_vbx[ly][lx] = static_cast<const float2*>(in.vbx)[idx];
+        s_vby[ly][lx] = static_cast<const float2*>(in.vby)[idx];
+      }
+    }
+  }
+  float alpha0 = 1.f, alpha1 = 1.f;
+  if constexpr (TGV) {
+    const int k = *iter;
+    alpha0 = alpha_tab[2 * k];
+    alpha1 = alpha_tab[2 * k + 1];
+  }
+  __syncthreads();
+
+  for (int i = tid; i < (TX + 1) * (TY + 1); i += NT) {
+    const int ly = i / (TX + 1), lx = i - ly * (TX + 1);
+    if (lx == 0 && ly == 0) continue;
+    const int gx = x0 - 1 + lx, gy = y0 - 1 + ly;
+    if (gx < 0 || gx >= W || gy < 0 || gy >= H) continue;
+    const size_t idx = (size_t)gy * W + gx;
+    const int xp = lx + (gx < W - 1), yp = ly + (gy < H - 1);
+    const float2 c = s_ub[ly][lx];
+    float2 a = static_cast<const float2*>(in.px)[idx];
+    float2 b = static_cast<const float2*>(in.py)[idx];
+    if constexpr (TGV) {
+      a = a + sigma * ((s_ub[ly][xp] - c) - s_vbx[ly][lx]);
+      b = b + sigma * ((s_ub[yp][lx] - c) - s_vby[ly][lx]);
+    } else {
+      a = a + sigma * (s_ub[ly][xp] - c);
+      b = b + sigma * (s_ub[yp][lx] - c);
+    }
+    const float sp = proj_scale(sqrtf(abs2(a) + abs2(b)), alpha1);
+    a = a * sp;
+    b = b * sp;
+    s_px[ly][lx] = a;
+    s_py[ly][lx] = b;
+    const bool interior = lx > 0 && ly > 0;
+    if (interior) {
+      static_cast<float2*>(out.px)[idx] = a;
+      static_cast<float2*>(out.py)[idx] = b;
+    }
+    if constexpr (TGV) {
+      const float2 vx = s_vbx[ly][lx], vy = s_vby[ly][lx];
+      const float2 gxx = s_vbx[ly][xp] - vx;
+      const float2 gxy = 0.5f * (s_vbx[yp][lx] - vx + s_vby[ly][xp] - vy);
+      const float2 gyy = s_vby[yp][lx] - vy;
+      const float2 qa = static_cast<const float2*>(in.qxx)[idx] + sigma * gxx;
+      const float2 qb = static_cast<const float2*>(in.qyy)[idx] + sigma * gyy;
+      const float2 qc = static_cast<const float2*>(in.qxy)[idx] + sigma * gxy;
+      const float sq = proj_scale(sqrtf(abs2(qa) + abs2(qb) + 2.0f * abs2(qc)), alpha0);
+      const float2 na = qa * sq, nb = qb * sq, nc = qc * sq;
+      s_qxx[ly][lx] = na;
+      s_qyy[ly][lx] = nb;
+      s_qxy[ly][lx] = nc;
+      if (interior) {
+        static_cast<float2*>(out.qxx)[idx] = na;
+        static_cast<float2*>(out.qyy)[idx] = nb;
+        static_cast<float2*>(out.qxy)[idx] = nc;
+      }
+    }
+  }
+  __syncthreads();
+
+  const int lx = tid % TX + 1, ly = tid / TX + 1;
+  const int gx = x0 + lx - 1, gy = y0 + ly - 1;
+  if (gx < W && gy < H) {
+    const size_t idx = (size_t)gy * W + gx;
+    float2 kh = khr[idx];
+    for (int g = 1; g < G; ++g) kh += khr[idx + (size_t)g * gstride];
+    // TGV_primal_u_noprox_kernel (tgv_kernels.cuh:432-467)
+    float2* u = static_cast<float2*>(out.u);
+    const float2 uo = u[idx];
+    const float2 d = div_minus<float2, TX + 1>(s_px, s_py, lx, ly, gx, gy, W, H);
+    const float2 un = uo + tau * (d - kh);
+    u[idx] = un;
+    static_cast<float2*>(out.ub)[idx] = 2.0f * un - uo;
+    if constexpr (TGV) {
+      // TGV_primal_v_kernel (tgv_kernels.cuh:647-686)
+      float2* vxp = static_cast<float2*>(out.vx);
+      float2* vyp = static_cast<float2*>(out.vy);
+      const float2 vxo = vxp[idx], vyo = vyp[idx];
+      const float2 dqxx = (gx > 0) ? ((gx < W - 1) ? s_qxx[ly][lx] - s_qxx[ly][lx - 1] : -s_qxx[ly][lx - 1]) : s_qxx[ly][lx];
+      const float2 dqyy = (gy > 0) ? ((gy < H - 1) ? s_qyy[ly][lx] - s_qyy[ly - 1][lx] : -s_qyy[ly - 1][lx]) : s_qyy[ly][lx];
+      const float2 dqxyx = (gx > 0) ? ((gx < W - 1) ? s_qxy[ly][lx] - s_qxy[ly][lx - 1] : -s_qxy[ly][lx - 1]) : s_qxy[ly][lx];
+      const float2 dqxyy = (gy > 0) ? ((gy < H - 1) ? s_qxy[ly][lx] - s_qxy[ly - 1][lx] : -s_qxy[ly - 1][lx]) : s_qxy[ly][lx];
+      const float2 vxn = vxo + tau * ((dqxx + dqxyy) + s_px[ly][lx]);
+      const float2 vyn = vyo + tau * ((dqyy + dqxyx) + s_py[ly][lx]);
+      vxp[idx] = vxn;
+      vyp[idx] = vyn;
+      static_cast<float2*>(out.vbx)[idx] = 2.0f * vxn - vxo;
+      static_cast<float2*>(out.vby)[idx] = 2.0f * vyn - vyo;
+    }
+  }
+}
+
+__global__ void tick_kernel(int* tick) { atomicAdd(tick, 1); }
+
+inline dim3 tile_grid(int W, int H) { return dim3((W + TX - 1) / TX, (H + TY - 1) / TY); }
+
+}  // namespace
+
+void launch_tv_step(bool complex_, int W, int H, const ImgPtrs& in, const ImgPtrs& out, const void* f, float tau,
+                    float sigma, float lambda, cudaStream_t st) {
+  if (complex_)
+    tv_step_kernel<float2><<<tile_grid(W, H), NT, 0, st>>>(W, H, in, out, static_cast<const float2*>(f), tau, sigma,
+                                                            lambda);
+  else
+    tv_step_kernel<float><<<tile_grid(W, H), NT, 0, st>>>(W, H, in, out, static_cast<const float*>(f), tau, sigma,
+                                                           lambda);
+  PDT_LAUNCH_CHECK();
+  count_launch();
+}
+
+void launch_tgv_denoise_step(bool complex_, int W, int H, const ImgPtrs& in, const ImgPtrs& out, const void* f,
+                             float tau, float sigma, float lambda, float alpha0, float alpha1, cudaStream_t st) {
+  if (complex_)
+    tgv_denoise_step_kernel<float2><<<tile_grid(W, H), NT, 0, st>>>(W, H, in, out, static_cast<const float2*>(f),
+                                                                     tau, sigma, lambda, alpha0, alpha1);
+  else
+    tgv_denoise_step_kernel<float><<<tile_grid(W, H), NT, 0, st>>>(W, H, in, out, static_cast<const float*>(f), tau,
+                                                                    sigma, lambda, alpha0, alpha1);
+  PDT_LAUNCH_CHECK();
+  count_launch();
+}
+
+void launch_mri_image_step(bool tgv, int W, int H, const ImgPtrs& in, const ImgPtrs& out, const float2* khr, int G,
+                           long long gstride, float tau, float sigma, const float* alpha_tab, const int* iter,
+                           cudaStream_t st) {
+  if (tgv)
+    mri_image_step_kernel<true><<<tile_grid(W, H), NT, 0, st>>>(W, H, in, out, khr, G, gstride, tau, sigma,
+                                                                alpha_tab, iter);
+  else
+    mri_image_step_kernel<false><<<tile_grid(W, H), NT, 0, st>>>(W, H, in, out, khr, G, gstride, tau, sigma,
+                                                                 alpha_tab, iter);
+  PDT_LAUNCH_CHECK();
+  count_launch();
+}
+
+void launch_tick(int* tick, cudaStream_t st) {
+  tick_kernel<<<1, 1, 0, st>>>(tick);
+  PDT_LAUNCH_CHECK();
+  count_launch();
+}
+
+void launch_fill_zero(void* p, size_t bytes, cudaStream_t st) {
+  if (bytes) PDT_CUDA_CHECK(cudaMemsetAsync(p, 0, bytes, st));
+}
+
+}  // namespace pdt

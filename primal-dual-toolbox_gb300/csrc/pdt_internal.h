@@ -1,0 +1,101 @@
+// pdt_internal.h -- host-side declarations shared by the engine's translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <cstdint>
+#include <string>
+#include <stdexcept>
+#include <vector>
+
+#include "pdt.h"
+
+namespace pdt {
+
+// Error carried to the C ABI as (status, message).
+struct Error : std::runtime_error {
+  pdt_status code;
+  Error(pdt_status c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+#define PDT_CUDA_CHECK(call)                                                                         \
+  do {                                                                                               \
+    cudaError_t e_ = (call);                                                                         \
+    if (e_ != cudaSuccess)                                                                           \
+      throw ::pdt::Error(PDT_ERR_CUDA, std::string(#call) + " failed: " + cudaGetErrorString(e_));   \
+  } while (0)
+
+// Checks the launch that was just enqueued.
+#define PDT_LAUNCH_CHECK() PDT_CUDA_CHECK(cudaGetLastError())
+
+// Kernels launched by this library (graph replays add their kernel-node count).
+extern std::atomic<uint64_t> g_launches;
+inline void count_launch(uint64_t n = 1) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+// Owning device allocation.
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  ~DevBuf() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+  // (Re)allocates when the size changes; contents are undefined afterwards.
+  void ensure(size_t n) {
+    if (n == bytes && p) return;
+    release();
+    if (n == 0) return;
+    cudaError_t e = cudaMalloc(&p, n);
+    if (e != cudaSuccess) {
+      p = nullptr;
+      throw Error(PDT_ERR_ALLOC, "device allocation of " + std::to_string(n) + " bytes failed: " +
+                                     cudaGetErrorString(e));
+    }
+    bytes = n;
+  }
+  template <class T> T* as() const { return static_cast<T*>(p); }
+};
+
+// ---------------------------------------------------------------------------------------------
+// Image-side state: the primal u, v, their over-relaxations u-bar, v-bar and the duals p, q, each a
+// planar W x H array (Variable2 / Variable2sym of optimizer_helper.h:30-224 as separate planes).
+// ---------------------------------------------------------------------------------------------
+struct ImgPtrs {
+  void *u, *ub, *vx, *vy, *vbx, *vby, *px, *py, *qxx, *qyy, *qxy;
+};
+
+// Fused TvOptimizer iteration (tgv_kernels.cuh:294-324 then 568-605): reads u-bar and p from `in`,
+// writes p and u-bar to `out`, updates u in place (in.u == out.u).
+void launch_tv_step(bool complex_, int W, int H, const ImgPtrs& in, const ImgPtrs& out, const void* f, float tau,
+                    float sigma, float lambda, cudaStream_t st);
+
+// Fused TgvOptimizer iteration, primal first (tgvoptimizer.cu:117-137): every field ping-pongs.
+void launch_tgv_denoise_step(bool complex_, int W, int H, const ImgPtrs& in, const ImgPtrs& out, const void* f,
+                             float tau, float sigma, float lambda, float alpha0, float alpha1, cudaStream_t st);
+
+// Image side of one TgvMri / TgvWithOp / TvWithOp iteration after K^H r is known
+// (tgvmrioptimizer.cu:177-197): dual p, q then primal u, v, fused. khr holds G partial sums of K^H r
+// spaced gstride elements apart. alpha_tab[2k], alpha_tab[2k+1] = alpha0, alpha1 of iteration
+// k = *iter. tgv = false gives the TvOptimizerWithOp step (no v, q; unit-ball projection).
+void launch_mri_image_step(bool tgv, int W, int H, const ImgPtrs& in, const ImgPtrs& out, const float2* khr, int G,
+                           long long gstride, float tau, float sigma, const float* alpha_tab, const int* iter,
+                           cudaStream_t st);
+
+// Records a CUDA event after each phase of an iteration (per-kernel timing); null in normal runs.
+struct PhaseMarker {
+  virtual ~PhaseMarker() = default;
+  virtual void mark(const char* phase, cudaStream_t st) = 0;
+};
+
+// Element-wise helpers.
+void launch_fill_zero(void* p, size_t bytes, cudaStream_t st);
+// *tick += 1 (one thread).
+void launch_tick(int* tick, cudaStream_t st);
+
+}  // namespace pdt

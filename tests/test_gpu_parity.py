@@ -1,0 +1,237 @@
+"""GPU parity: libpdt.so (through the reference-shaped Python API over the C ABI) against the CPU oracle.
+
+Tolerances (FP32 engine):
+  * operators vs the FP64 oracle: rel-L2 <= 1e-5
+  * adjointness |<Au,p> - <u,A^H p>| / (||Au|| ||p||) <= 1e-5
+  * solvers vs the FP32-mirror oracle after the stated iteration count: rel-L2 <= 1e-4
+"""
+import numpy as np
+import pytest
+
+from conftest import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+OP_TOL = 1e-5
+SOLVE_TOL = 1e-4
+
+
+def _rand_c(rng, shape):
+    return (rng.standard_normal(shape) + 1j * rng.standard_normal(shape)).astype(np.complex64)
+
+
+def _make_op(pdt, kind, sens, mask):
+    if kind == "cartesian":
+        op = pdt.mri.MriCartesianOperator()
+    elif kind == "cartesian_roos":
+        op = pdt.mri.MriCartesianRemoveROOSOperator()
+    else:
+        op = pdt.mri.MriSamplingOperator()
+        op.setMask(mask)
+        return op
+    op.setCoilSens(sens)
+    op.setMask(mask)
+    return op
+
+
+SHAPES = [(5, 10, 10), (3, 16, 12), (4, 64, 48), (2, 46, 23), (3, 30, 7), (1, 1, 8), (2, 8, 1), (15, 640, 368)]
+
+
+@pytest.mark.parametrize("kind", ["cartesian", "cartesian_roos", "sampling"])
+@pytest.mark.parametrize("shape", SHAPES)
+def test_operator_matches_oracle(pdt, oracle, kind, shape):
+    C, H, W = shape
+    if kind == "cartesian_roos" and H < 4:
+        pytest.skip("ROOS needs H >= 4")
+    rng = np.random.default_rng(C * 1000 + H * 10 + W)
+    sens = _rand_c(rng, (C, H, W))
+    mask = (rng.random((H, W)) < 0.6).astype(np.float32)
+    if kind != "sampling" and H > 8:
+        mask[:, rng.random(W) < 0.3] = 0  # whole unsampled phase-encode lines
+    op = _make_op(pdt, kind, sens, mask)
+    Hi = H // 2 if kind == "cartesian_roos" else H
+    u = _rand_c(rng, (Hi, W))
+    k = _rand_c(rng, (H, W) if kind == "sampling" else (C, H, W))
+    fwd = op.forward(u)
+    adj = op.adjoint(k)
+    ref_f = oracle.op_apply(kind, sens, mask, u, prec=64)
+    ref_a = oracle.op_apply(kind, sens, mask, k, adjoint=True, prec=64)
+    assert fwd.shape == ref_f.shape and adj.shape == ref_a.shape
+    assert rel_l2(fwd, ref_f) <= OP_TOL
+    assert rel_l2(adj, ref_a) <= OP_TOL
+
+
+@pytest.mark.parametrize("kind", ["cartesian", "cartesian_roos", "sampling"])
+def test_adjointness(pdt, kind):
+    # tests/main_adjointness_test.cu:28-64 shapes: coil sens {10,10,5}, mask {10,10} in {0,1}
+    rng = np.random.default_rng(42)
+    sens = (rng.random((5, 10, 10)) + 1j * rng.random((5, 10, 10))).astype(np.complex64)
+    mask = rng.integers(0, 2, (10, 10)).astype(np.float32)
+    op = _make_op(pdt, kind, sens, mask)
+    lhs, rhs = op.adjointnessCheck(seed=42)
+    u = _rand_c(rng, (5 if kind == "cartesian_roos" else 10, 10))
+    p = _rand_c(rng, (10, 10) if kind == "sampling" else (5, 10, 10))
+    Au, Atp = op.forward(u), op.adjoint(p)
+    l2, r2 = np.vdot(p, Au), np.vdot(Atp, u)
+    scale = np.linalg.norm(Au) * np.linalg.norm(p)
+    assert abs(l2 - r2) / scale <= 1e-5
+    assert abs(lhs - rhs) / max(abs(lhs), 1e-30) <= 1e-5
+
+
+def test_tv_rof_config1(pdt, oracle):
+    """TvOptimizer_2f on the 512x512 ROF workload: lambda = 10, 500 -> 501 iterations."""
+    from primaldualtoolbox import synthetic
+
+    f, _ = synthetic.tv_phantom(512, 512, seed=0)
+    opt = pdt.denoising.TvOptimizer_2f()
+    opt.setNoisyData(f)
+    opt.getParameters().Lambda = 10
+    opt.getParameters().max_iter = 500
+    opt.solve()
+    u = opt.getResult()
+    ref = oracle.tv_solve(f, lam=10, max_iter=500, prec=32)
+    assert rel_l2(u, ref) <= SOLVE_TOL
+
+
+@pytest.mark.parametrize("shape", [(37, 53), (1, 17), (9, 1), (64, 64)])
+@pytest.mark.parametrize("cplx", [False, True])
+def test_tv_denoise_shapes(pdt, oracle, shape, cplx):
+    rng = np.random.default_rng(shape[0] * 100 + shape[1])
+    f = rng.random(shape).astype(np.float32)
+    if cplx:
+        f = (f + 1j * rng.random(shape)).astype(np.complex64)
+        opt = pdt.denoising.TvOptimizer_2c()
+    else:
+        opt = pdt.denoising.TvOptimizer_2f()
+    opt.setNoisyData(f)
+    opt.getParameters().Lambda = 5
+    opt.getParameters().max_iter = 100
+    opt.solve()
+    ref = oracle.tv_solve(f, lam=5, max_iter=100, prec=32)
+    assert rel_l2(opt.getResult(), ref) <= SOLVE_TOL
+
+
+@pytest.mark.parametrize("shape", [(48, 40), (33, 21), (1, 12)])
+@pytest.mark.parametrize("cplx", [False, True])
+def test_tgv_denoise(pdt, oracle, shape, cplx):
+    rng = np.random.default_rng(7)
+    f = rng.random(shape).astype(np.float32)
+    if cplx:
+        f = (f + 1j * rng.random(shape)).astype(np.complex64)
+        opt = pdt.denoising.TgvOptimizer_2c()
+    else:
+        opt = pdt.denoising.TgvOptimizer_2f()
+    opt.setNoisyData(f)
+    prm = opt.getParameters()
+    prm.Lambda, prm.alpha0, prm.alpha1, prm.max_iter = 8.0, 0.2, 0.1, 150
+    opt.solve()
+    ref = oracle.tgv_solve(f, lam=8.0, alpha0=0.2, alpha1=0.1, max_iter=150, prec=32)
+    assert rel_l2(opt.getResult(), ref) <= SOLVE_TOL
+
+
+def _cart_case(C=4, H=64, W=48, roos=True, seed=1):
+    from primaldualtoolbox import synthetic
+
+    return synthetic.cartesian_case(C=C, H=H, W=W, roos=roos, seed=seed)
+
+
+@pytest.mark.parametrize("roos", [True, False])
+def test_tgv_mri_small_1001_iterations(pdt, oracle, roos):
+    """TgvMriOptimizer_2c3c with the sample's schedule (reduction 2e-8, alpha0 = 2 alpha1), 1000 -> 1001 its."""
+    case = _cart_case(roos=roos)
+    kind = "cartesian_roos" if roos else "cartesian"
+    op = (pdt.mri.MriCartesianRemoveROOSOperator if roos else pdt.mri.MriCartesianOperator)()
+    op.setCoilSens(case["sens"])
+    op.setMask(case["mask"])
+    opt = pdt.mri.TgvMriOptimizer_2c3c()
+    prm = opt.getParameters()
+    prm.reduction, prm.max_iter, prm.alpha1 = 2e-8, 1000, case["alpha1"]
+    prm.alpha0 = 2 * prm.alpha1
+    opt.setOperator(op)
+    opt.setNoisyData(case["rawdata"])
+    opt.solve()
+    ref = oracle.op_solve(kind, case["sens"], case["mask"], case["rawdata"], "tgv_mri", alpha0=prm.alpha0,
+                          alpha1=prm.alpha1, reduction=prm.reduction, max_iter=1000, prec=32)
+    assert rel_l2(opt.getResult(), ref) <= SOLVE_TOL
+
+
+@pytest.mark.parametrize("variant", ["tgv_op", "tv_op"])
+def test_with_op_optimizers(pdt, oracle, variant):
+    case = _cart_case(C=3, H=32, W=24, roos=False, seed=3)
+    op = pdt.mri.MriCartesianOperator()
+    op.setCoilSens(case["sens"])
+    op.setMask(case["mask"])
+    opt = (pdt.mri.TgvOptimizer_2c3c if variant == "tgv_op" else pdt.mri.TvOptimizerWithOp_2c3c)()
+    prm = opt.getParameters()
+    prm.max_iter, prm.Lambda = 300, 2.0
+    if variant == "tgv_op":
+        prm.alpha1, prm.alpha0 = case["alpha1"], case["alpha0"]
+    opt.setOperator(op)
+    opt.setNoisyData(case["rawdata"])
+    opt.solve()
+    a0 = prm.alpha0 if variant == "tgv_op" else 1.0
+    a1 = prm.alpha1 if variant == "tgv_op" else 1.0
+    ref = oracle.op_solve("cartesian", case["sens"], case["mask"], case["rawdata"], variant, alpha0=a0, alpha1=a1,
+                          lam=2.0, max_iter=300, prec=32)
+    assert rel_l2(opt.getResult(), ref) <= SOLVE_TOL
+
+
+def test_sampling_operator_tgv_mri(pdt, oracle):
+    rng = np.random.default_rng(5)
+    H, W = 40, 36
+    mask = (rng.random((H, W)) < 0.4).astype(np.float32)
+    truth = _rand_c(rng, (H, W))
+    op = pdt.mri.MriSamplingOperator()
+    op.setMask(mask)
+    f = op.forward(truth)
+    opt = pdt.mri.TgvMriOptimizer_2c2c()
+    prm = opt.getParameters()
+    prm.max_iter, prm.alpha1, prm.alpha0, prm.reduction = 200, 0.05, 0.1, 0.1
+    opt.setOperator(op)
+    opt.setNoisyData(f)
+    opt.solve()
+    ref = oracle.op_solve("sampling", None, mask, f, "tgv_mri", alpha0=0.1, alpha1=0.05, reduction=0.1,
+                          max_iter=200, prec=32)
+    assert rel_l2(opt.getResult(), ref) <= SOLVE_TOL
+
+
+def test_tgv_mri_config2_full_size_short(pdt, oracle):
+    """Full 15 x 640 x 368 ROOS problem, 10 iterations, against the FP32 oracle."""
+    case = _cart_case(C=15, H=640, W=368, roos=True, seed=0)
+    op = pdt.mri.MriCartesianRemoveROOSOperator()
+    op.setCoilSens(case["sens"])
+    op.setMask(case["mask"])
+    opt = pdt.mri.TgvMriOptimizer_2c3c()
+    prm = opt.getParameters()
+    prm.reduction, prm.max_iter, prm.alpha1 = 2e-8, 9, case["alpha1"]
+    prm.alpha0 = 2 * prm.alpha1
+    opt.setOperator(op)
+    opt.setNoisyData(case["rawdata"])
+    opt.solve()
+    ref = oracle.op_solve("cartesian_roos", case["sens"], case["mask"], case["rawdata"], "tgv_mri",
+                          alpha0=prm.alpha0, alpha1=prm.alpha1, reduction=prm.reduction, max_iter=9, prec=32)
+    assert rel_l2(opt.getResult(), ref) <= SOLVE_TOL
+
+
+def test_solve_is_deterministic_and_resumable(pdt):
+    case = _cart_case(C=4, H=64, W=48, roos=True, seed=2)
+
+    def run(chunks):
+        op = pdt.mri.MriCartesianRemoveROOSOperator()
+        op.setCoilSens(case["sens"])
+        op.setMask(case["mask"])
+        opt = pdt.mri.TgvMriOptimizer_2c3c()
+        prm = opt.getParameters()
+        prm.alpha1, prm.alpha0 = case["alpha1"], case["alpha0"]
+        opt.setOperator(op)
+        opt.setNoisyData(case["rawdata"])
+        for n in chunks:
+            prm.max_iter = n - 1
+            opt.solve()
+        return opt.getResult()
+
+    a = run([60])
+    b = run([60])
+    assert np.array_equal(a, b)  # bitwise reproducible
+    c = run([25, 35])  # state persists across solve() calls (alpha constant at reduction 1)
+    assert rel_l2(c, a) <= 1e-6
