@@ -594,6 +594,8 @@ struct pdt_opt {
 
 static thread_local std::string t_last_error;
 
+void pdt::set_last_error(const std::string& msg) { t_last_error = msg; }
+
 template <class F>
 static pdt_status guarded(F&& fn) {
   try {

@@ -29,6 +29,9 @@ struct Error : std::runtime_error {
 // Checks the launch that was just enqueued.
 #define PDT_LAUNCH_CHECK() PDT_CUDA_CHECK(cudaGetLastError())
 
+// Sets the message pdt_last_error() returns on this thread.
+void set_last_error(const std::string& msg);
+
 // Kernels launched by this library (graph replays add their kernel-node count).
 extern std::atomic<uint64_t> g_launches;
 inline void count_launch(uint64_t n = 1) { g_launches.fetch_add(n, std::memory_order_relaxed); }
