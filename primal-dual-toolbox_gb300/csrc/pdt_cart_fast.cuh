@@ -1,0 +1,274 @@
+// pdt_cart_fast.cuh -- register-FFT kernels of the Cartesian operator for even W and H with a
+// compile-time two-level split (W = A * B, A, B <= 32). One warp owns one sequence (an image row or a
+// k-space column): lanes < A run the first-level B-point FFTs in registers, lanes < B the second-level
+// A-point FFTs, exchanging once through the warp's own shared-memory tile. The column kernel runs
+// forward FFT, mask, k-space dual prox and inverse FFT with two exchanges, because the inverse starts
+// from the registers the forward leaves (the shifts cancel for even H: slot k of the forward output is
+// slot k of the inverse input). Included by pdt_cartesian.cu after CartDev.
+#pragma once
+
+#include "pdt_regfft.cuh"
+
+namespace pdt {
+namespace {
+
+constexpr int kFastWarps = 8;  // sequences (warps) per block
+
+// Phase 1 (fast): rows of ubar . sens_c -> FFT along W -> sampled columns t1[c][s][yi].
+template <int A, int B>
+__global__ void __launch_bounds__(32 * kFastWarps) fr_rows_fwd(CartDev d, const float2* __restrict__ ubar,
+                                                               float2* __restrict__ t1, int* __restrict__ tick) {
+  using TL = TwoLevel<A, B>;
+  extern __shared__ float2 sm[];
+  float2* tw = sm;
+  float2* ex = tw + TL::n;
+  float2* stage = ex + kFastWarps * TL::xch;
+  int* fs2s = reinterpret_cast<int*>(stage + (size_t)d.ns * kFastWarps);
+  if (tick && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) atomicAdd(tick, 1);
+  for (int i = threadIdx.x; i < TL::n; i += blockDim.x) {
+    tw[i] = d.twW[i];
+    fs2s[i] = d.fslot2s[i];
+  }
+  __syncthreads();
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int yi0 = blockIdx.x * kFastWarps, yi = yi0 + w, c = blockIdx.y;
+  float2* myex = ex + w * TL::xch;
+  const bool ok = yi < d.Hi;
+  if (ok && lane < A) {
+    float2 v[B];
+    const float2* urow = ubar + (size_t)yi * TL::n;
+    const float2* srow = d.sens ? d.sens + ((size_t)c * d.Hf + yi + d.y0) * TL::n : nullptr;
+#pragma unroll
+    for (int b = 0; b < B; ++b) {
+      int x = lane + A * b - d.mxW;  // FFT slot j holds image column (j - mid) mod W
+      if (x < 0) x += TL::n;
+      float2 val = urow[x];
+      if (srow) val = cmul(val, srow[x]);
+      v[b] = val;
+    }
+    TL::fwd_step1(v, lane, myex, tw);
+  }
+  __syncwarp();
+  if (ok && lane < B) {
+    float2 u[A];
+    TL::fwd_step2(u, lane, myex, tw);
+#pragma unroll
+    for (int ka = 0; ka < A; ++ka) {
+      const int s = fs2s[lane + B * ka];
+      if (s >= 0) stage[s * kFastWarps + w] = u[ka];
+    }
+  }
+  __syncthreads();
+  const int nr = min(kFastWarps, d.Hi - yi0);
+  for (int i = threadIdx.x; i < d.ns * nr; i += blockDim.x) {
+    const int s = i / nr, r = i - s * nr;
+    t1[((size_t)c * d.ns + s) * d.Hi + yi0 + r] = stage[s * kFastWarps + r];
+  }
+}
+
+// Phase 2 (fast): per sampled column, FFT along H -> mask -> (prox) -> mask -> IFFT along H.
+template <int A, int B>
+__global__ void __launch_bounds__(32 * kFastWarps) fr_cols(CartDev d, int mode, const float2* t_in, float2* t_out,
+                                                           float2* __restrict__ r, const float2* __restrict__ fc,
+                                                           const float2* __restrict__ kin, float2* __restrict__ kout,
+                                                           float sigma, float lambda) {
+  using TL = TwoLevel<A, B>;
+  extern __shared__ float2 sm[];
+  float2* tw = sm;
+  float2* ex = tw + TL::n;
+  for (int i = threadIdx.x; i < TL::n; i += blockDim.x) tw[i] = d.twH[i];
+  __syncthreads();
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int s = blockIdx.x * kFastWarps + w, c = blockIdx.y;
+  const bool ok = s < d.ns;
+  float2* myex = ex + w * TL::xch;
+  constexpr int Hf = TL::n;
+  const size_t colc = ((size_t)c * d.ns + s);
+  float2 u[A];
+  if (mode == COL_SOLVE || mode == COL_FWD_DENSE) {
+    if (ok && lane < A) {
+      float2 v[B];
+#pragma unroll
+      for (int b = 0; b < B; ++b) {
+        int yf = lane + A * b - d.mxH;
+        if (yf < 0) yf += Hf;
+        const int yi = yf - d.y0;
+        v[b] = (yi >= 0 && yi < d.Hi) ? t_in[colc * d.Hi + yi] : c2(0.f, 0.f);
+      }
+      TL::fwd_step1(v, lane, myex, tw);
+    }
+    __syncwarp();
+    if (ok && lane < B) {
+      TL::fwd_step2(u, lane, myex, tw);
+      const float* mrow = d.maskc + (size_t)s * Hf;
+#pragma unroll
+      for (int ka = 0; ka < A; ++ka) {
+        int ypos = lane + B * ka + d.oyH;
+        if (ypos >= Hf) ypos -= Hf;
+        const float m = mrow[ypos];
+        const float2 kv = u[ka] * (d.scale * m);
+        if (mode == COL_FWD_DENSE) {
+          kout[((size_t)c * Hf + ypos) * d.W + d.col_x[s]] = kv;
+        } else {
+          const size_t o = colc * Hf + ypos;
+          const float2 rn = (r[o] + sigma * (kv - fc[o])) / (1.0f + sigma * lambda);
+          r[o] = rn;
+          u[ka] = rn * m;
+        }
+      }
+    }
+    if (mode == COL_FWD_DENSE) return;
+    __syncwarp();
+  } else if (ok && lane < B) {
+    const float* mrow = d.maskc + (size_t)s * Hf;
+#pragma unroll
+    for (int ka = 0; ka < A; ++ka) {
+      int ypos = lane + B * ka + d.oyH;
+      if (ypos >= Hf) ypos -= Hf;
+      const float2 v = (mode == COL_ADJ_DENSE) ? kin[((size_t)c * Hf + ypos) * d.W + d.col_x[s]] : fc[colc * Hf + ypos];
+      u[ka] = v * mrow[ypos];
+    }
+  }
+  if (ok && lane < B) TL::inv_step1(u, lane, myex, tw);
+  __syncwarp();
+  if (ok && lane < A) {
+    float2 v[B];
+    TL::inv_step2(v, lane, myex, tw);
+#pragma unroll
+    for (int b = 0; b < B; ++b) {
+      int yf = lane + A * b + d.oyH;
+      if (yf >= Hf) yf -= Hf;
+      const int yi = yf - d.y0;
+      if (yi >= 0 && yi < d.Hi) t_out[colc * d.Hi + yi] = v[b] * d.scale;
+    }
+  }
+}
+
+// Phase 3 (fast): per image row and coil group, IFFT along W of the sampled columns, conj(sens_c)
+// multiply and the group's coil sum in registers (coil order), written as one partial image.
+template <int A, int B>
+__global__ void __launch_bounds__(32 * kFastWarps) fr_rows_adj(CartDev d, const float2* __restrict__ t2,
+                                                               float2* __restrict__ out, int G, long long gstride) {
+  using TL = TwoLevel<A, B>;
+  extern __shared__ float2 sm[];
+  float2* tw = sm;
+  float2* ex = tw + TL::n;
+  float2* stage = ex + kFastWarps * TL::xch;
+  int* as2s = reinterpret_cast<int*>(stage + (size_t)d.ns * kFastWarps);
+  for (int i = threadIdx.x; i < TL::n; i += blockDim.x) {
+    tw[i] = d.twW[i];
+    as2s[i] = d.slot2s[i];
+  }
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int yi0 = blockIdx.x * kFastWarps, yi = yi0 + w, g = blockIdx.y;
+  const int nr = min(kFastWarps, d.Hi - yi0);
+  const int c_begin = (int)((long long)g * d.C / G), c_end = (int)((long long)(g + 1) * d.C / G);
+  float2* myex = ex + w * TL::xch;
+  const bool ok = w < nr;
+  float2 acc[B];
+#pragma unroll
+  for (int b = 0; b < B; ++b) acc[b] = c2(0.f, 0.f);
+  for (int c = c_begin; c < c_end; ++c) {
+    __syncthreads();  // stage (and, first time, the tables) ready for reuse
+    for (int i = threadIdx.x; i < d.ns * nr; i += blockDim.x) {
+      const int s = i / nr, rr = i - s * nr;
+      stage[s * kFastWarps + rr] = t2[((size_t)c * d.ns + s) * d.Hi + yi0 + rr];
+    }
+    __syncthreads();
+    if (ok && lane < B) {
+      float2 u[A];
+#pragma unroll
+      for (int ka = 0; ka < A; ++ka) {
+        const int s = as2s[lane + B * ka];
+        u[ka] = s >= 0 ? stage[s * kFastWarps + w] : c2(0.f, 0.f);
+      }
+      TL::inv_step1(u, lane, myex, tw);
+    }
+    __syncwarp();
+    if (ok && lane < A) {
+      float2 v[B];
+      TL::inv_step2(v, lane, myex, tw);
+      const float2* srow = d.sens ? d.sens + ((size_t)c * d.Hf + yi + d.y0) * TL::n : nullptr;
+#pragma unroll
+      for (int b = 0; b < B; ++b) {
+        int x = lane + A * b + d.oxW;
+        if (x >= TL::n) x -= TL::n;
+        acc[b] += srow ? cmulc(v[b], srow[x]) : v[b];
+      }
+    }
+    __syncwarp();
+  }
+  if (ok && lane < A) {
+    float2* orow = out + (size_t)g * gstride + (size_t)yi * TL::n;
+#pragma unroll
+    for (int b = 0; b < B; ++b) {
+      int x = lane + A * b + d.oxW;
+      if (x >= TL::n) x -= TL::n;
+      orow[x] = acc[b];
+    }
+  }
+}
+
+typedef void (*FrRowsFwdFn)(CartDev, const float2*, float2*, int*);
+typedef void (*FrColsFn)(CartDev, int, const float2*, float2*, float2*, const float2*, const float2*, float2*, float,
+                         float);
+typedef void (*FrRowsAdjFn)(CartDev, const float2*, float2*, int, long long);
+
+struct FastRowKernels {
+  FrRowsFwdFn fwd = nullptr;
+  FrRowsAdjFn adj = nullptr;
+  int A = 0, B = 0;
+};
+struct FastColKernels {
+  FrColsFn cols = nullptr;
+  int A = 0, B = 0;
+};
+
+template <int A, int B>
+FastRowKernels row_kernels() {
+  FastRowKernels k;
+  k.fwd = fr_rows_fwd<A, B>;
+  k.adj = fr_rows_adj<A, B>;
+  k.A = A;
+  k.B = B;
+  return k;
+}
+template <int A, int B>
+FastColKernels col_kernels() {
+  FastColKernels k;
+  k.cols = fr_cols<A, B>;
+  k.A = A;
+  k.B = B;
+  return k;
+}
+
+// Lengths with a compiled two-level split.
+#define PDT_FAST_SIZES(X) X(32, 4, 8) X(48, 6, 8) X(64, 8, 8) X(96, 8, 12) X(128, 8, 16) X(192, 12, 16) \
+  X(256, 16, 16) X(320, 16, 20) X(368, 16, 23) X(384, 16, 24) X(512, 16, 32) X(640, 32, 20) X(768, 32, 24)
+
+FastRowKernels find_row_kernels(int n) {
+#define PDT_ROWCASE(N, A, B) \
+  if (n == N) return row_kernels<A, B>();
+  PDT_FAST_SIZES(PDT_ROWCASE)
+#undef PDT_ROWCASE
+  return FastRowKernels();
+}
+FastColKernels find_col_kernels(int n) {
+#define PDT_COLCASE(N, A, B) \
+  if (n == N) return col_kernels<A, B>();
+  PDT_FAST_SIZES(PDT_COLCASE)
+#undef PDT_COLCASE
+  return FastColKernels();
+}
+
+size_t fast_rows_smem(const CartDev& d, int A, int B) {
+  const size_t n = (size_t)A * B, xch = (size_t)B * (A + 1);
+  return sizeof(float2) * (n + kFastWarps * xch + (size_t)d.ns * kFastWarps) + sizeof(int) * n;
+}
+size_t fast_cols_smem(int A, int B) {
+  const size_t n = (size_t)A * B, xch = (size_t)B * (A + 1);
+  return sizeof(float2) * (n + kFastWarps * xch);
+}
+
+}  // namespace
+}  // namespace pdt

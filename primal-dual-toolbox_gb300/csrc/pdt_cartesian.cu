@@ -43,6 +43,7 @@ struct CartDev {
   const int* fwd_slot;  // [ns] forward-FFT output slot of sampled column s
   const int* col_x;     // [ns] k-space column of s
   const int* slot2s;    // [W] inverse-FFT input slot -> s (or -1)
+  const int* fslot2s;   // [W] forward-FFT output slot -> s (or -1)
   const float2* twW;
   const float2* twH;
   FftPlan planW, planH;
@@ -226,6 +227,11 @@ void query_device() {
 }
 
 }  // namespace
+}  // namespace pdt
+
+#include "pdt_cart_fast.cuh"
+
+namespace pdt {
 
 // ------------------------------------------------------------------------------------------------
 // Operator object
@@ -346,6 +352,13 @@ class CartesianOp : public OpImpl, public SolverHooks {
 
  private:
   void launch_rows_fwd(const float2* ubar, float2* t1, int* tick, cudaStream_t st) {
+    if (frow_.fwd) {
+      dim3 grid((dev_.Hi + kFastWarps - 1) / kFastWarps, dev_.C);
+      frow_.fwd<<<grid, 32 * kFastWarps, fast_rows_smem(dev_, frow_.A, frow_.B), st>>>(dev_, ubar, t1, tick);
+      PDT_LAUNCH_CHECK();
+      count_launch();
+      return;
+    }
     dim3 grid((dev_.Hi + dev_.RB - 1) / dev_.RB, dev_.C);
     rows_fwd_kernel<<<grid, kThreads, rows_smem(dev_, false), st>>>(dev_, ubar, t1, tick);
     PDT_LAUNCH_CHECK();
@@ -353,12 +366,28 @@ class CartesianOp : public OpImpl, public SolverHooks {
   }
   void launch_cols(int mode, const float2* tin, float2* tout, float2* r, const float2* fc, const float2* kin,
                    float2* kout, float sigma, float lambda, cudaStream_t st) {
+    if (fcol_.cols) {
+      dim3 grid((dev_.ns + kFastWarps - 1) / kFastWarps, dev_.C);
+      fcol_.cols<<<grid, 32 * kFastWarps, fast_cols_smem(fcol_.A, fcol_.B), st>>>(dev_, mode, tin, tout, r, fc, kin,
+                                                                                  kout, sigma, lambda);
+      PDT_LAUNCH_CHECK();
+      count_launch();
+      return;
+    }
     dim3 grid((dev_.ns + dev_.CB - 1) / dev_.CB, dev_.C);
     cols_kernel<<<grid, kThreads, cols_smem(dev_), st>>>(dev_, mode, tin, tout, r, fc, kin, kout, sigma, lambda);
     PDT_LAUNCH_CHECK();
     count_launch();
   }
   void launch_rows_adj(const float2* t2, float2* out, int G, cudaStream_t st) {
+    if (frow_.adj) {
+      dim3 grid((dev_.Hi + kFastWarps - 1) / kFastWarps, G);
+      frow_.adj<<<grid, 32 * kFastWarps, fast_rows_smem(dev_, frow_.A, frow_.B), st>>>(dev_, t2, out, G,
+                                                                                      (long long)dev_.Hi * dev_.W);
+      PDT_LAUNCH_CHECK();
+      count_launch();
+      return;
+    }
     dim3 grid((dev_.Hi + dev_.RB - 1) / dev_.RB, G);
     rows_adj_kernel<<<grid, kThreads, rows_smem(dev_, true), st>>>(dev_, t2, out, G, (long long)dev_.Hi * dev_.W);
     PDT_LAUNCH_CHECK();
@@ -414,11 +443,12 @@ class CartesianOp : public OpImpl, public SolverHooks {
           break;
         }
     d.ns = (int)col_x.size();
-    std::vector<int> fwd_slot(d.ns), slot2s(W, -1);
+    std::vector<int> fwd_slot(d.ns), slot2s(W, -1), fslot2s(W, -1);
     std::vector<float> maskc((size_t)d.ns * Hf);
     for (int s = 0; s < d.ns; ++s) {
       const int x = col_x[s];
       fwd_slot[s] = ((x - d.oxW) % W + W) % W;
+      fslot2s[fwd_slot[s]] = s;
       slot2s[(x + d.mxW) % W] = s;
       for (int y = 0; y < Hf; ++y) maskc[(size_t)s * Hf + y] = mask[(size_t)y * W + x];
     }
@@ -435,7 +465,7 @@ class CartesianOp : public OpImpl, public SolverHooks {
     std::vector<float2> twW(W), twH(Hf);
     fill_twiddles(W, twW.data());
     fill_twiddles(Hf, twH.data());
-    const size_t need = 16 * 8 + sizeof(int) * (2 * (size_t)d.ns + W) + sizeof(float) * maskc.size() +
+    const size_t need = 16 * 8 + sizeof(int) * (2 * (size_t)d.ns + 2 * (size_t)W) + sizeof(float) * maskc.size() +
                         sizeof(float2) * ((size_t)W + Hf);
     tables_.ensure(need);
     char* base = tables_.as<char>();
@@ -452,10 +482,22 @@ class CartesianOp : public OpImpl, public SolverHooks {
     d.fwd_slot = reinterpret_cast<const int*>(put(fwd_slot.data(), sizeof(int) * d.ns));
     d.col_x = reinterpret_cast<const int*>(put(col_x.data(), sizeof(int) * d.ns));
     d.slot2s = reinterpret_cast<const int*>(put(slot2s.data(), sizeof(int) * W));
+    d.fslot2s = reinterpret_cast<const int*>(put(fslot2s.data(), sizeof(int) * W));
     d.maskc = reinterpret_cast<const float*>(put(maskc.data(), sizeof(float) * maskc.size()));
     scratch_.ensure(std::max<size_t>(1, (size_t)C * d.ns * d.Hi) * sizeof(float2));
+    // register-FFT kernels where the length has a compiled split
+    frow_ = find_row_kernels(W);
+    fcol_ = find_col_kernels(Hf);
+    if (frow_.fwd && fast_rows_smem(d, frow_.A, frow_.B) > (size_t)g_max_smem) frow_ = FastRowKernels();
+    if (fcol_.cols && fast_cols_smem(fcol_.A, fcol_.B) > (size_t)g_max_smem) fcol_ = FastColKernels();
+    if (frow_.fwd) {
+      PDT_CUDA_CHECK(cudaFuncSetAttribute(frow_.fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, g_max_smem));
+      PDT_CUDA_CHECK(cudaFuncSetAttribute(frow_.adj, cudaFuncAttributeMaxDynamicSharedMemorySize, g_max_smem));
+    }
+    if (fcol_.cols)
+      PDT_CUDA_CHECK(cudaFuncSetAttribute(fcol_.cols, cudaFuncAttributeMaxDynamicSharedMemorySize, g_max_smem));
     // coil groups for the adjoint row phase: enough blocks for two waves
-    const int row_blocks = (d.Hi + d.RB - 1) / d.RB;
+    const int row_blocks = frow_.fwd ? (d.Hi + kFastWarps - 1) / kFastWarps : (d.Hi + d.RB - 1) / d.RB;
     G_ = std::max(1, std::min(C, (2 * g_num_sms + row_blocks - 1) / row_blocks));
     dev_ = d;
     prepared_ = true;
@@ -463,6 +505,8 @@ class CartesianOp : public OpImpl, public SolverHooks {
 
   bool prepared_ = false;
   CartDev dev_{};
+  FastRowKernels frow_;
+  FastColKernels fcol_;
   int G_ = 1;
   DevBuf tables_, scratch_;
 };

@@ -39,3 +39,72 @@ extern "C" int emu_fft(float* data, int n, int nseq, int inverse) {
     }
   return 0;
 }
+
+// ---- register FFTs and the two-level transform (pdt_regfft.cuh) ------------------------------------
+#include "../../primal-dual-toolbox_gb300/csrc/pdt_regfft.cuh"
+
+template <int A, int B>
+static void twolevel(float* data, int inverse) {
+  using T = pdt::TwoLevel<A, B>;
+  constexpr int n = A * B;
+  std::vector<float2> tw(n), ex(T::xch);
+  pdt::fill_twiddles(n, tw.data());
+  std::vector<float2> x(n);
+  for (int i = 0; i < n; ++i) x[i] = {data[2 * i], data[2 * i + 1]};
+  if (!inverse) {
+    for (int a = 0; a < A; ++a) {
+      float2 v[B];
+      for (int b = 0; b < B; ++b) v[b] = x[a + A * b];
+      T::fwd_step1(v, a, ex.data(), tw.data());
+    }
+    for (int kb = 0; kb < B; ++kb) {
+      float2 u[A];
+      T::fwd_step2(u, kb, ex.data(), tw.data());
+      for (int ka = 0; ka < A; ++ka) x[kb + B * ka] = u[ka];
+    }
+  } else {
+    std::vector<float2> z(n);
+    for (int kb = 0; kb < B; ++kb) {
+      float2 u[A];
+      for (int ka = 0; ka < A; ++ka) u[ka] = x[kb + B * ka];
+      T::inv_step1(u, kb, ex.data(), tw.data());
+    }
+    for (int a = 0; a < A; ++a) {
+      float2 v[B];
+      T::inv_step2(v, a, ex.data(), tw.data());
+      for (int b = 0; b < B; ++b) z[a + A * b] = v[b];
+    }
+    x = z;
+  }
+  for (int i = 0; i < n; ++i) {
+    data[2 * i] = x[i].x;
+    data[2 * i + 1] = x[i].y;
+  }
+}
+
+template <int N>
+static void regfft(float* data, int inverse) {
+  std::vector<float2> tw(N);
+  pdt::fill_twiddles(N, tw.data());
+  float2 v[N];
+  for (int i = 0; i < N; ++i) v[i] = {data[2 * i], data[2 * i + 1]};
+  pdt::reg_fft<N, 1>(v, tw.data(), inverse ? 1.f : -1.f);
+  for (int i = 0; i < N; ++i) {
+    data[2 * i] = v[i].x;
+    data[2 * i + 1] = v[i].y;
+  }
+}
+
+#define EMU_REG(N) if (n == N) { regfft<N>(data, inverse); return 0; }
+extern "C" int emu_regfft(float* data, int n, int inverse) {
+  EMU_REG(2) EMU_REG(3) EMU_REG(4) EMU_REG(5) EMU_REG(7) EMU_REG(8) EMU_REG(9) EMU_REG(10) EMU_REG(12)
+  EMU_REG(16) EMU_REG(20) EMU_REG(23) EMU_REG(24) EMU_REG(32) EMU_REG(11) EMU_REG(13) EMU_REG(6)
+  return 1;
+}
+
+#define EMU_TL(A, B) if (a == A && b == B) { twolevel<A, B>(data, inverse); return 0; }
+extern "C" int emu_twolevel(float* data, int a, int b, int inverse) {
+  EMU_TL(16, 23) EMU_TL(32, 20) EMU_TL(16, 20) EMU_TL(16, 16) EMU_TL(12, 16) EMU_TL(16, 24) EMU_TL(8, 8)
+  EMU_TL(16, 12) EMU_TL(8, 16) EMU_TL(32, 24) EMU_TL(16, 32) EMU_TL(8, 12) EMU_TL(8, 20)
+  return 1;
+}

@@ -36,3 +36,38 @@ def test_device_fft_matches_numpy(emu, n, inverse):
     ref = np.fft.ifft(x64, axis=1) * n if inverse else np.fft.fft(x64, axis=1)
     err = np.abs(y - ref).max() / np.abs(ref).max()
     assert err < 2e-6 * max(1.0, np.log2(max(n, 2)))
+
+
+REG_SIZES = [2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12, 13, 16, 20, 23, 24, 32]
+
+
+@pytest.mark.parametrize("n", REG_SIZES)
+@pytest.mark.parametrize("inverse", [0, 1])
+def test_register_fft_matches_numpy(emu, n, inverse):
+    emu.emu_regfft.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
+    rng = np.random.default_rng(100 + n)
+    x = (rng.standard_normal(n) + 1j * rng.standard_normal(n)).astype(np.complex64)
+    y = x.copy()
+    assert emu.emu_regfft(y.ctypes.data, n, inverse) == 0
+    x64 = x.astype(np.complex128)
+    ref = np.fft.ifft(x64) * n if inverse else np.fft.fft(x64)
+    assert np.abs(y - ref).max() / np.abs(ref).max() < 3e-6
+
+
+TWO_LEVEL = [(16, 23), (32, 20), (16, 20), (16, 16), (12, 16), (16, 24), (8, 8), (16, 12), (8, 16), (32, 24),
+             (16, 32), (8, 12), (8, 20)]
+
+
+@pytest.mark.parametrize("ab", TWO_LEVEL)
+@pytest.mark.parametrize("inverse", [0, 1])
+def test_two_level_fft_matches_numpy(emu, ab, inverse):
+    a, b = ab
+    n = a * b
+    emu.emu_twolevel.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+    rng = np.random.default_rng(n + inverse)
+    x = (rng.standard_normal(n) + 1j * rng.standard_normal(n)).astype(np.complex64)
+    y = x.copy()
+    assert emu.emu_twolevel(y.ctypes.data, a, b, inverse) == 0
+    x64 = x.astype(np.complex128)
+    ref = np.fft.ifft(x64) * n if inverse else np.fft.fft(x64)
+    assert np.abs(y - ref).max() / np.abs(ref).max() < 5e-6

@@ -34,7 +34,9 @@ def _make_op(pdt, kind, sens, mask):
     return op
 
 
-SHAPES = [(5, 10, 10), (3, 16, 12), (4, 64, 48), (2, 46, 23), (3, 30, 7), (1, 1, 8), (2, 8, 1), (15, 640, 368)]
+# generic-path sizes (odd, prime, tiny) and sizes with a compiled register-FFT split
+SHAPES = [(5, 10, 10), (3, 16, 12), (4, 64, 48), (2, 46, 23), (3, 30, 7), (1, 1, 8), (2, 8, 1), (15, 640, 368),
+          (2, 192, 256), (3, 320, 320), (2, 384, 128), (2, 96, 512), (2, 768, 32)]
 
 
 @pytest.mark.parametrize("kind", ["cartesian", "cartesian_roos", "sampling"])
@@ -76,6 +78,22 @@ def test_adjointness(pdt, kind):
     scale = np.linalg.norm(Au) * np.linalg.norm(p)
     assert abs(l2 - r2) / scale <= 1e-5
     assert abs(lhs - rhs) / max(abs(lhs), 1e-30) <= 1e-5
+
+
+def test_operator_on_reference_mask_fixture(pdt, oracle):
+    """data/mask_cartesian_random4.npy (768 x 384, 117 lines) with 4 random coil maps, ROOS operator."""
+    import os
+
+    cols = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "mask_random4_lines.npy"))
+    mask = np.zeros((768, 384), dtype=np.float32)
+    mask[:, cols] = 1
+    rng = np.random.default_rng(3)
+    sens = _rand_c(rng, (4, 768, 384))
+    op = _make_op(pdt, "cartesian_roos", sens, mask)
+    u = _rand_c(rng, (384, 384))
+    k = _rand_c(rng, (4, 768, 384))
+    assert rel_l2(op.forward(u), oracle.op_apply("cartesian_roos", sens, mask, u, prec=64)) <= OP_TOL
+    assert rel_l2(op.adjoint(k), oracle.op_apply("cartesian_roos", sens, mask, k, adjoint=True, prec=64)) <= OP_TOL
 
 
 def test_tv_rof_config1(pdt, oracle):
