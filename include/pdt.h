@@ -156,6 +156,17 @@ PDT_API pdt_status pdt_opt_get_result(pdt_opt* opt, void* dst, int is_device, vo
 PDT_API pdt_status pdt_opt_profile(pdt_opt* opt, int iters, void* stream, int max_phases, int* nphases, char* names,
                                    size_t names_len, double* ms);
 
+/* ---- batched solves ------------------------------------------------------------------------------ */
+/* No counterpart in the reference (which solves one reconstruction per call): a batch advances many
+ * independent optimizers together -- uneven sizes, coil counts, masks and iteration counts -- as parallel
+ * branches of one captured CUDA graph, equivalent to calling pdt_opt_solve on each. Every optimizer
+ * needs its own operator; optimizers must outlive the batch. */
+typedef struct pdt_batch pdt_batch;
+PDT_API pdt_status pdt_batch_create(pdt_batch** out);
+PDT_API pdt_status pdt_batch_destroy(pdt_batch* b);
+PDT_API pdt_status pdt_batch_add(pdt_batch* b, pdt_opt* opt);
+PDT_API pdt_status pdt_batch_solve(pdt_batch* b, int verbose, void* stream);
+
 /* ---- allocation-free entry point ---------------------------------------------------------------- */
 /* No counterpart in the reference. The Cartesian forward operator (MriCartesianOperator, or with
  * roos = 1 MriCartesianRemoveROOSOperator) for callers that cannot allocate device memory: code inside

@@ -54,6 +54,14 @@ def lib():
         L.orc_op_solve.argtypes = [i, i, i, i, i, vp, vp, vp, vp, vp, i, d, d, d, d, u, vp]
         L.orc_alpha_schedule_f32.argtypes = [ctypes.c_float, ctypes.c_float, ctypes.c_float, u, u,
                                              ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]
+        L.orc_radial_apply.argtypes = [i, i, i, d, i, i, i, vp, vp, vp, vp, vp]
+        L.orc_radial_solve.argtypes = [i, i, d, i, i, i, vp, vp, vp, vp, vp, vp, i, d, d, d, d, u]
+        L.orc_radial_grid_size.argtypes = [i, d]
+        L.orc_radial_grid_size.restype = i
+        L.orc_kb_beta.argtypes = [i, d]
+        L.orc_kb_beta.restype = d
+        L.orc_kb_deapod.argtypes = [i, i, i, d]
+        L.orc_kb_deapod.restype = d
         L.orc_tgv_energy_f64.restype = d
         L.orc_tgv_energy_f64.argtypes = [i, i, i, i, vp, vp, vp, vp, vp, vp, d, d]
         _lib = L
@@ -170,3 +178,39 @@ def tgv_energy(kind, sens, mask, f, u, vx, vy, alpha0, alpha1):
     C = 1 if k == 2 else s.shape[0]
     arrs = [np.ascontiguousarray(a, dtype=np.complex128) for a in (f, u, vx, vy)]
     return lib().orc_tgv_energy_f64(k, W, Hf, C, _ptr(s), _ptr(mask), *[_ptr(a) for a in arrs], alpha0, alpha1)
+
+
+def _radial_args(traj, dcf, sens, prec):
+    traj = np.ascontiguousarray(traj, dtype=_re(prec)).reshape(2, -1)
+    Ns = traj.shape[1]
+    dcf = np.ascontiguousarray(dcf, dtype=_re(prec)).reshape(-1)
+    assert dcf.size == Ns
+    s = None if sens is None else np.ascontiguousarray(sens, dtype=_cx(prec))
+    C = 1 if s is None else s.shape[0]
+    return traj, dcf, s, C, Ns
+
+
+def radial_apply(traj, dcf, sens, src, N, osf, kw, mode="forward", prec=64):
+    """Radial multi-coil (sens (C,N,N)) or single-coil (sens None) operator. traj (2, Ns): row 0 pairs with
+    image x, row 1 with y; dcf (1, Ns) or (Ns,). mode: forward | adjoint | ndft."""
+    traj, dcf, s, C, Ns = _radial_args(traj, dcf, sens, prec)
+    src = np.ascontiguousarray(src, dtype=_cx(prec))
+    m = {"forward": 0, "adjoint": 1, "ndft": 2}[mode]
+    dst = np.zeros((N, N) if m == 1 else (C, Ns), dtype=_cx(prec))
+    lib().orc_radial_apply(prec, m, N, osf, kw, C, Ns, _ptr(traj), _ptr(dcf), _ptr(s), _ptr(src), _ptr(dst))
+    return dst
+
+
+def radial_solve(traj, dcf, sens, f, N, osf, kw, variant="tgv_mri", alpha0=1.0, alpha1=1.0, reduction=1.0, lam=1.0,
+                 max_iter=1, u0=None, prec=32):
+    traj, dcf, s, C, Ns = _radial_args(traj, dcf, sens, prec)
+    f = np.ascontiguousarray(f, dtype=_cx(prec))
+    u0 = None if u0 is None else np.ascontiguousarray(u0, dtype=_cx(prec))
+    u = np.zeros((N, N), dtype=_cx(prec))
+    lib().orc_radial_solve(prec, N, osf, kw, C, Ns, _ptr(traj), _ptr(dcf), _ptr(s), _ptr(f), _ptr(u0), _ptr(u),
+                           VARIANT[variant], alpha0, alpha1, reduction, lam, int(max_iter))
+    return u
+
+
+def radial_grid_size(N, osf):
+    return lib().orc_radial_grid_size(N, osf)

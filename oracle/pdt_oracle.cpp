@@ -29,6 +29,7 @@
 #include <cstring>
 #include <vector>
 #include <algorithm>
+#include <cmath>
 #ifdef _OPENMP
 #include <omp.h>
 #endif
@@ -378,6 +379,8 @@ struct CartOp {
   }
   size_t img_n() const { return (size_t)W * Hi; }
   size_t ksp_n() const { return (size_t)W * Hf * C; }
+  int img_w() const { return W; }
+  int img_h() const { return Hi; }
 
   // forward: mricartesianoperator.cu:320-365 (ROOS) / 196-225 (plain); mrisamplingoperator.cu:59-70
   void forward(const cx<R>* u, cx<R>* k) const {
@@ -450,6 +453,166 @@ struct CartOp {
   }
 };
 
+
+// ------------------------------------------------------------------------------------------------
+// Radial operators (MriRadialOperator / MriRadialSinglecoilOperator, mriradialoperator.cu:27-321).
+// The reference delegates to gpuNUFFT (github.com/andyschwarzl/gpuNUFFT, submodule pin not recorded,
+// .gitmodules:4-6), which is absent here; this restates its published method (Knoll et al., ISMRM 2014:
+// Kaiser-Bessel gridding on an osf-oversampled grid, deapodisation, density compensation) with the
+// Kaiser-Bessel shape of Beatty et al. (IEEE TMI 2005): beta = pi sqrt((W/osf)^2 (osf - 1/2)^2 - 0.8).
+// Convention (parity with gpuNUFFT is unpinned; see the tests):
+//   A u [c, j] = w_j / N * sum_{x,y} sens_c(x,y) u(x,y) exp(-2 pi i (k0_j (x - N/2) + k1_j (y - N/2)))
+// approximated by: deapodise, zero-pad into G = ceil(osf N) (even), FFT, interpolate with the separable
+// kernel at kappa = k G; the adjoint is its exact transpose. Trajectory constant {Ns, 2} is planar
+// (k0 for every sample, then k1); k0 pairs with image x (fastest), k1 with y.
+// ------------------------------------------------------------------------------------------------
+inline int radial_grid_size(int N, double osf) {
+  int G = (int)std::ceil(osf * N - 1e-9);
+  return G + (G & 1);
+}
+inline double kb_beta(int kw, double osf) {
+  const double a = (double)kw / osf * (osf - 0.5);
+  return M_PI * std::sqrt(std::max(a * a - 0.8, 1e-12));
+}
+inline double kb_kernel(double d, int kw, double beta) {
+  const double t = 2.0 * d / kw;
+  if (std::fabs(t) > 1.0) return 0.0;
+  return std::cyl_bessel_i(0.0, beta * std::sqrt(1.0 - t * t));
+}
+// deap(m) = integral of the kernel times cos(2 pi t m / G) over its support (composite Simpson, 4000 panels).
+inline double kb_deapod(int m, int G, int kw, double beta) {
+  const int P = 4000;
+  const double a = -0.5 * kw, h = (double)kw / P;
+  double s = 0;
+  for (int i = 0; i <= P; ++i) {
+    const double t = a + i * h;
+    const double f = kb_kernel(t, kw, beta) * std::cos(2.0 * M_PI * t * m / G);
+    s += f * ((i == 0 || i == P) ? 1.0 : (i & 1) ? 4.0 : 2.0);
+  }
+  return s * h / 3.0;
+}
+
+template <class R>
+struct RadialOp {
+  int N, G, kw, C, Ns;
+  double beta;
+  const cx<R>* sens;  // (N, N, C) or null
+  std::vector<double> k0, k1, w, deap;
+  std::vector<int> gx0, gy0;
+  std::vector<double> wx, wy;  // [j][kw]
+  RadialOp(int N_, double osf, int kw_, int C_, int Ns_, const R* traj, const R* dcf, const cx<R>* sens_)
+      : N(N_), kw(kw_), C(sens_ ? C_ : 1), Ns(Ns_), sens(sens_) {
+    G = radial_grid_size(N, osf);
+    beta = kb_beta(kw, osf);
+    k0.resize(Ns);
+    k1.resize(Ns);
+    w.resize(Ns);
+    gx0.resize(Ns);
+    gy0.resize(Ns);
+    wx.resize((size_t)Ns * kw);
+    wy.resize((size_t)Ns * kw);
+    for (int j = 0; j < Ns; ++j) {
+      k0[j] = traj[j];
+      k1[j] = traj[Ns + j];
+      w[j] = dcf[j];
+      const double ax = k0[j] * G, ay = k1[j] * G;
+      gx0[j] = (int)std::ceil(ax - 0.5 * kw);
+      gy0[j] = (int)std::ceil(ay - 0.5 * kw);
+      for (int t = 0; t < kw; ++t) {
+        wx[(size_t)j * kw + t] = kb_kernel(gx0[j] + t - ax, kw, beta);
+        wy[(size_t)j * kw + t] = kb_kernel(gy0[j] + t - ay, kw, beta);
+      }
+    }
+    deap.resize(N);
+    for (int x = 0; x < N; ++x) deap[x] = kb_deapod(x - N / 2, G, kw, beta);
+  }
+  size_t img_n() const { return (size_t)N * N; }
+  size_t ksp_n() const { return (size_t)C * Ns; }
+  int img_w() const { return N; }
+  int img_h() const { return N; }
+  int wrap(int g) const { g %= G; return g < 0 ? g + G : g; }
+
+  void forward(const cx<R>* u, cx<R>* k) const {
+    std::vector<cd> grid((size_t)G * G * C);
+    const double sc = 1.0 / N;
+    for (int c = 0; c < C; ++c)
+      for (int y = 0; y < N; ++y)
+        for (int x = 0; x < N; ++x) {
+          const size_t i = x + (size_t)N * y;
+          cd v = {(double)u[i].x, (double)u[i].y};
+          if (sens) v = cmul(v, cd{(double)sens[i + (size_t)N * N * c].x, (double)sens[i + (size_t)N * N * c].y});
+          const double f = sc / (deap[x] * deap[y]);
+          grid[wrap(x - N / 2) + (size_t)G * (wrap(y - N / 2) + (size_t)G * c)] = v * f;
+        }
+    fft2_unscaled(grid.data(), C, -1);
+    for (int c = 0; c < C; ++c)
+      for (int j = 0; j < Ns; ++j) {
+        cd a = {0, 0};
+        for (int ty = 0; ty < kw; ++ty)
+          for (int tx = 0; tx < kw; ++tx) {
+            const double wt = wx[(size_t)j * kw + tx] * wy[(size_t)j * kw + ty];
+            a += grid[wrap(gx0[j] + tx) + (size_t)G * (wrap(gy0[j] + ty) + (size_t)G * c)] * wt;
+          }
+        a = a * w[j];
+        k[j + (size_t)Ns * c] = {(R)a.x, (R)a.y};
+      }
+  }
+  void adjoint(const cx<R>* k, cx<R>* u) const {
+    std::vector<cd> grid((size_t)G * G * C, cd{0, 0});
+    for (int c = 0; c < C; ++c)
+      for (int j = 0; j < Ns; ++j) {
+        const cd s = cd{(double)k[j + (size_t)Ns * c].x, (double)k[j + (size_t)Ns * c].y} * w[j];
+        for (int ty = 0; ty < kw; ++ty)
+          for (int tx = 0; tx < kw; ++tx) {
+            const double wt = wx[(size_t)j * kw + tx] * wy[(size_t)j * kw + ty];
+            grid[wrap(gx0[j] + tx) + (size_t)G * (wrap(gy0[j] + ty) + (size_t)G * c)] += s * wt;
+          }
+      }
+    fft2_unscaled(grid.data(), C, +1);
+    const double sc = 1.0 / N;
+    for (int y = 0; y < N; ++y)
+      for (int x = 0; x < N; ++x) {
+        const size_t i = x + (size_t)N * y;
+        const double f = sc / (deap[x] * deap[y]);
+        cd acc = {0, 0};
+        for (int c = 0; c < C; ++c) {
+          const cd g = grid[wrap(x - N / 2) + (size_t)G * (wrap(y - N / 2) + (size_t)G * c)] * f;
+          acc += sens ? cmulc(g, cd{(double)sens[i + (size_t)N * N * c].x, (double)sens[i + (size_t)N * N * c].y}) : g;
+        }
+        u[i] = {(R)acc.x, (R)acc.y};
+      }
+  }
+  // exact non-uniform DFT of the same operator (accuracy oracle)
+  void ndft_forward(const cx<R>* u, cx<R>* k) const {
+#pragma omp parallel for schedule(static)
+    for (int j = 0; j < Ns; ++j)
+      for (int c = 0; c < C; ++c) {
+        double ar = 0, ai = 0;
+        for (int y = 0; y < N; ++y)
+          for (int x = 0; x < N; ++x) {
+            const size_t i = x + (size_t)N * y;
+            cd v = {(double)u[i].x, (double)u[i].y};
+            if (sens) v = cmul(v, cd{(double)sens[i + (size_t)N * N * c].x, (double)sens[i + (size_t)N * N * c].y});
+            const double ph = -2.0 * M_PI * (k0[j] * (x - N / 2) + k1[j] * (y - N / 2));
+            ar += v.x * std::cos(ph) - v.y * std::sin(ph);
+            ai += v.x * std::sin(ph) + v.y * std::cos(ph);
+          }
+        k[j + (size_t)Ns * c] = {(R)(ar * w[j] / N), (R)(ai * w[j] / N)};
+      }
+  }
+
+ private:
+  void fft2_unscaled(cd* d, int nb, int sign) const {
+#pragma omp parallel for schedule(static)
+    for (long long t = 0; t < (long long)nb * G; ++t) fft1(d + (size_t)t * G, 1, G, sign);
+#pragma omp parallel for schedule(static)
+    for (long long t = 0; t < (long long)nb * G; ++t) {
+      const long long b = t / G, x = t % G;
+      fft1(d + (size_t)b * G * G + x, (size_t)G, G, sign);
+    }
+  }
+};
+
 // ------------------------------------------------------------------------------------------------
 // Solvers.
 // ------------------------------------------------------------------------------------------------
@@ -511,11 +674,11 @@ inline void alpha_schedule(R a0, R a1, R reduction, unsigned max_iter, unsigned 
 
 // variant: 0 = TgvMriOptimizer (tgvmrioptimizer.cu:93-203), 1 = TgvOptimizerWithOp
 // (tgvoptimizerwithop.cu:89-179), 2 = TvOptimizerWithOp (tvoptimizerwithop.cu:86-164).
-template <class R>
-void op_solve(const CartOp<R>& op, const cx<R>* f, const cx<R>* u0, cx<R>* uout, int variant, R alpha0, R alpha1,
+template <class R, class Op>
+void op_solve(const Op& op, const cx<R>* f, const cx<R>* u0, cx<R>* uout, int variant, R alpha0, R alpha1,
               R reduction, R lambda, unsigned max_iter, cx<R>* state_out) {
   typedef cx<R> P;
-  const int W = op.W, H = op.Hi;
+  const int W = op.img_w(), H = op.img_h();
   ImgState<P> s(W, H);
   const size_t nk = op.ksp_n(), ni = op.img_n();
   std::vector<P> r(nk, pzero<P>()), tmp(nk);
@@ -677,11 +840,11 @@ void orc_op_solve(int prec, int kind, int W, int Hf, int C, const void* sens, co
                   double lambda, unsigned max_iter, void* state_out) {
   if (prec == 32) {
     CartOp<float> op(kind, W, Hf, C, (const cx<float>*)sens, (const float*)mask);
-    op_solve<float>(op, (const cx<float>*)f, (const cx<float>*)u0, (cx<float>*)uout, variant, (float)alpha0,
+    op_solve<float, CartOp<float>>(op, (const cx<float>*)f, (const cx<float>*)u0, (cx<float>*)uout, variant, (float)alpha0,
                     (float)alpha1, (float)reduction, (float)lambda, max_iter, (cx<float>*)state_out);
   } else {
     CartOp<double> op(kind, W, Hf, C, (const cx<double>*)sens, (const double*)mask);
-    op_solve<double>(op, (const cx<double>*)f, (const cx<double>*)u0, (cx<double>*)uout, variant, alpha0, alpha1,
+    op_solve<double, CartOp<double>>(op, (const cx<double>*)f, (const cx<double>*)u0, (cx<double>*)uout, variant, alpha0, alpha1,
                      reduction, lambda, max_iter, (cx<double>*)state_out);
   }
 }
@@ -697,5 +860,41 @@ double orc_tgv_energy_f64(int kind, int W, int Hf, int C, const double* sens, co
   return tgv_energy<double>(op, (const cx<double>*)f, (const cx<double>*)u, (const cx<double>*)vx,
                             (const cx<double>*)vy, alpha0, alpha1);
 }
+
+// Radial operators. mode: 0 forward (NUFFT), 1 adjoint, 2 exact NDFT forward. sens may be null (single coil).
+// traj {Ns, 2} planar, dcf {Ns}. Pointers are float (prec 32) or double (prec 64).
+void orc_radial_apply(int prec, int mode, int N, double osf, int kw, int C, int Ns, const void* traj, const void* dcf,
+                      const void* sens, const void* src, void* dst) {
+  if (prec == 32) {
+    RadialOp<float> op(N, osf, kw, C, Ns, (const float*)traj, (const float*)dcf, (const cx<float>*)sens);
+    if (mode == 0) op.forward((const cx<float>*)src, (cx<float>*)dst);
+    else if (mode == 1) op.adjoint((const cx<float>*)src, (cx<float>*)dst);
+    else op.ndft_forward((const cx<float>*)src, (cx<float>*)dst);
+  } else {
+    RadialOp<double> op(N, osf, kw, C, Ns, (const double*)traj, (const double*)dcf, (const cx<double>*)sens);
+    if (mode == 0) op.forward((const cx<double>*)src, (cx<double>*)dst);
+    else if (mode == 1) op.adjoint((const cx<double>*)src, (cx<double>*)dst);
+    else op.ndft_forward((const cx<double>*)src, (cx<double>*)dst);
+  }
+}
+
+void orc_radial_solve(int prec, int N, double osf, int kw, int C, int Ns, const void* traj, const void* dcf,
+                      const void* sens, const void* f, const void* u0, void* uout, int variant, double alpha0,
+                      double alpha1, double reduction, double lambda, unsigned max_iter) {
+  if (prec == 32) {
+    RadialOp<float> op(N, osf, kw, C, Ns, (const float*)traj, (const float*)dcf, (const cx<float>*)sens);
+    op_solve<float, RadialOp<float>>(op, (const cx<float>*)f, (const cx<float>*)u0, (cx<float>*)uout, variant,
+                                     (float)alpha0, (float)alpha1, (float)reduction, (float)lambda, max_iter, nullptr);
+  } else {
+    RadialOp<double> op(N, osf, kw, C, Ns, (const double*)traj, (const double*)dcf, (const cx<double>*)sens);
+    op_solve<double, RadialOp<double>>(op, (const cx<double>*)f, (const cx<double>*)u0, (cx<double>*)uout, variant,
+                                       alpha0, alpha1, reduction, lambda, max_iter, nullptr);
+  }
+}
+
+// Kaiser-Bessel helpers exposed for tests: grid size, beta, deapodisation.
+int orc_radial_grid_size(int N, double osf) { return radial_grid_size(N, osf); }
+double orc_kb_beta(int kw, double osf) { return kb_beta(kw, osf); }
+double orc_kb_deapod(int m, int G, int kw, double beta) { return kb_deapod(m, G, kw, beta); }
 
 }  // extern "C"

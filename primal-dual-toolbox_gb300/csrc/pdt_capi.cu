@@ -256,13 +256,30 @@ class OptImpl {
     if (!has_f_) throw Error(PDT_ERR_STATE, "No noisy data is set!");
   }
 
-  void solve(bool verbose, cudaStream_t st) {
+  // A solve split in three: plan() enqueues the set-up on `st` and returns the per-iteration body,
+  // the iterations run (graph replay or direct), finish() records the new state parity.
+  struct Plan {
+    int n = 0;
+    int p0 = 0;
+    uint64_t key = 0;
+    bool verbose = false;
+    std::function<void(int, cudaStream_t)> body;
+  };
+
+  Plan plan(bool verbose, cudaStream_t st) {
     check_ready();
-    if (with_op())
-      solve_with_op(verbose, st);
-    else
-      solve_denoise(verbose, st);
+    return with_op() ? plan_with_op(verbose, st) : plan_denoise(verbose, st);
   }
+  void finish(const Plan& p) {
+    parity_ = p.p0 ^ (p.n & 1);
+    if (p.verbose && !with_op()) print_iters(p.n);
+  }
+  void solve(bool verbose, cudaStream_t st) {
+    Plan p = plan(verbose, st);
+    run_iterations(graph_, p.key, p.n, profiling_ ? p.n + 2 : kGraphIters, p.body, st, capture_stream());
+    finish(p);
+  }
+  const OpImpl* op_ptr() const { return op_.get(); }
 
   Dims result_size() const {
     if (!has_state_) throw Error(PDT_ERR_STATE, "There is no result yet!");
@@ -400,7 +417,7 @@ class OptImpl {
   }
 
   // TvOptimizer::solve (tvoptimizer.cu:76-125) / TgvOptimizer::solve (tgvoptimizer.cu:80-141).
-  void solve_denoise(bool verbose, cudaStream_t st) {
+  Plan plan_denoise(bool verbose, cudaStream_t st) {
     if (!has_state_) {
       if (verbose) std::cout << "Initialization with f" << std::endl;
       set_input0(f_.p, fsize_, true, st);
@@ -412,9 +429,12 @@ class OptImpl {
     const float lambda = (float)params_.lambda;
     const float a0 = (float)params_.alpha0, a1 = (float)params_.alpha1;
     if (verbose) print_params();
-    const int n = (int)params_.max_iter + 1;
+    Plan pl;
+    pl.n = (int)params_.max_iter + 1;
+    pl.p0 = parity_;
+    pl.verbose = verbose;
     const int p0 = parity_;
-    auto body = [&](int par, cudaStream_t s) {
+    pl.body = [=](int par, cudaStream_t s) {
       const int in = p0 ^ par, out = in ^ 1;
       if (is_tgv)
         launch_tgv_denoise_step(cplx_, W_, H_, ptrs(in), ptrs(out), f_.p, tau, sigma, lambda, a0, a1, s);
@@ -422,16 +442,14 @@ class OptImpl {
         launch_tv_step(cplx_, W_, H_, ptrs(in), ptrs(out), f_.p, tau, sigma, lambda, s);
       if (prof_) prof_->mark(is_tgv ? "tgv_denoise_step" : "tv_step", s);
     };
-    const uint64_t key = graph_key({(uintptr_t)img_.p, (uintptr_t)f_.p, (uintptr_t)W_, (uintptr_t)H_, (uintptr_t)p0,
-                                    (uintptr_t)cplx_, fbits(lambda), fbits(a0), fbits(a1)});
-    run_iterations(graph_, key, n, profiling_ ? n + 2 : kGraphIters, body, st, capture_stream());
-    parity_ = p0 ^ (n & 1);
-    if (verbose) print_iters(n);
+    pl.key = graph_key({(uintptr_t)img_.p, (uintptr_t)f_.p, (uintptr_t)W_, (uintptr_t)H_, (uintptr_t)p0,
+                        (uintptr_t)cplx_, fbits(lambda), fbits(a0), fbits(a1)});
+    return pl;
   }
 
   // TgvMriOptimizer::solve (tgvmrioptimizer.cu:93-203), TgvOptimizerWithOp::solve
   // (tgvoptimizerwithop.cu:89-179), TvOptimizerWithOp::solve (tvoptimizerwithop.cu:86-164).
-  void solve_with_op(bool verbose, cudaStream_t st) {
+  Plan plan_with_op(bool verbose, cudaStream_t st) {
     SolverHooks* hk = op_->hooks();
     if (!has_state_) {
       if (verbose) std::cout << "Initialization with A^T(f)" << std::endl;
@@ -500,19 +518,21 @@ class OptImpl {
     const int p0 = parity_;
     const float* atab = alpha_.as<float>();
     float2* khr = khr_.as<float2>();
-    auto body = [&](int par, cudaStream_t s) {
+    Plan pl;
+    pl.n = n;
+    pl.p0 = p0;
+    pl.verbose = verbose;
+    pl.body = [=](int par, cudaStream_t s) {
       const int in = p0 ^ par, out = in ^ 1;
       hk->round(static_cast<const float2*>(field(F_UB, in)), r_.as<float2>(), fc_.as<float2>(), sigma, lambda, khr,
                 iter, s, prof_);
       launch_mri_image_step(is_tgv, W_, H_, ptrs(in), ptrs(out), khr, G, gstride, tau, sigma, atab, iter, s);
       if (prof_) prof_->mark(is_tgv ? "mri_image_step_tgv" : "mri_image_step_tv", s);
     };
-    const uint64_t key = graph_key({(uintptr_t)img_.p, (uintptr_t)r_.p, (uintptr_t)fc_.p, (uintptr_t)khr_.p,
-                                    (uintptr_t)alpha_.p, (uintptr_t)op_.get(), (uintptr_t)W_, (uintptr_t)H_,
-                                    (uintptr_t)G, (uintptr_t)p0, (uintptr_t)is_tgv, fbits(lambda), fbits(tau),
-                                    (uintptr_t)version_});
-    run_iterations(graph_, key, n, profiling_ ? n + 2 : kGraphIters, body, st, capture_stream());
-    parity_ = p0 ^ (n & 1);
+    pl.key = graph_key({(uintptr_t)img_.p, (uintptr_t)r_.p, (uintptr_t)fc_.p, (uintptr_t)khr_.p,
+                        (uintptr_t)alpha_.p, (uintptr_t)op_.get(), (uintptr_t)W_, (uintptr_t)H_, (uintptr_t)G,
+                        (uintptr_t)p0, (uintptr_t)is_tgv, fbits(lambda), fbits(tau), (uintptr_t)version_});
+    return pl;
   }
 
   void ensure_fc(SolverHooks* hk, cudaStream_t st) {
@@ -545,6 +565,7 @@ class OptImpl {
   }
 
   // Identity of a captured iteration graph: every pointer and scalar baked into its kernel nodes.
+ public:
   static uintptr_t fbits(float v) {
     uint32_t b;
     std::memcpy(&b, &v, 4);
@@ -555,6 +576,8 @@ class OptImpl {
     for (uintptr_t v : vals) h = (h ^ (uint64_t)v) * 0x100000001b3ull;
     return h;
   }
+
+ private:
 
   static constexpr int kGraphIters = 20;
 
@@ -578,6 +601,119 @@ class OptImpl {
   cudaStream_t own_ = nullptr, cap_ = nullptr;
 };
 
+
+// ------------------------------------------------------------------------------------------------
+// Batched solve: independent reconstructions advance together. Every problem's iteration body runs on
+// its own branch of one captured CUDA graph (forked worker streams), so the small kernels of many
+// problems execute concurrently and fill the GPU; chunks of kBatchIters iterations replay the graph.
+// ------------------------------------------------------------------------------------------------
+class BatchImpl {
+ public:
+  ~BatchImpl() {
+    graph_.reset();
+    for (auto s : workers_) cudaStreamDestroy(s);
+    for (auto e : events_) cudaEventDestroy(e);
+    if (cap_) cudaStreamDestroy(cap_);
+  }
+  void add(OptImpl* o) {
+    if (o->op_ptr())
+      for (OptImpl* q : opts_)
+        if (q->op_ptr() == o->op_ptr())
+          throw Error(PDT_ERR_INVALID_ARGUMENT, "optimizers in one batch need distinct operators (an operator's "
+                                                "scratch serves one solve at a time)");
+    for (OptImpl* q : opts_)
+      if (q == o) throw Error(PDT_ERR_INVALID_ARGUMENT, "optimizer already in the batch");
+    opts_.push_back(o);
+  }
+  size_t size() const { return opts_.size(); }
+
+  void solve(bool verbose, cudaStream_t st) {
+    if (opts_.empty()) return;
+    std::vector<OptImpl::Plan> plans;
+    plans.reserve(opts_.size());
+    for (OptImpl* o : opts_) plans.push_back(o->plan(verbose, st));
+    ensure_streams();
+    int nmin = plans[0].n;
+    uint64_t key = 7;
+    for (auto& p : plans) {
+      nmin = std::min(nmin, p.n);
+      key = OptImpl::graph_key({(uintptr_t)key, (uintptr_t)p.key});
+    }
+    const int full = nmin / kBatchIters;
+    if (full > 0) {
+      if (!graph_.exec || graph_.key != key) {
+        graph_.reset();
+        const uint64_t before = g_launches.load();
+        PDT_CUDA_CHECK(cudaStreamBeginCapture(cap_, cudaStreamCaptureModeThreadLocal));
+        try {
+          fork_join(cap_, [&](size_t i, cudaStream_t w) {
+            for (int it = 0; it < kBatchIters; ++it) plans[i].body(it & 1, w);
+          });
+        } catch (...) {
+          cudaGraph_t dummy = nullptr;
+          cudaStreamEndCapture(cap_, &dummy);
+          if (dummy) cudaGraphDestroy(dummy);
+          throw;
+        }
+        cudaGraph_t graph = nullptr;
+        PDT_CUDA_CHECK(cudaStreamEndCapture(cap_, &graph));
+        graph_.kernels = g_launches.load() - before;
+        g_launches.fetch_sub(graph_.kernels);
+        cudaError_t e = cudaGraphInstantiate(&graph_.exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess) throw Error(PDT_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+        graph_.key = key;
+      }
+      for (int i = 0; i < full; ++i) {
+        PDT_CUDA_CHECK(cudaGraphLaunch(graph_.exec, st));
+        count_launch(graph_.kernels);
+      }
+    }
+    // remaining iterations of every problem (uneven max_iter), concurrently
+    fork_join(st, [&](size_t i, cudaStream_t w) {
+      for (int it = full * kBatchIters; it < plans[i].n; ++it) plans[i].body(it & 1, w);
+    });
+    for (size_t i = 0; i < opts_.size(); ++i) opts_[i]->finish(plans[i]);
+  }
+
+ private:
+  static constexpr int kBatchIters = 10;  // even: every replay returns each problem to its parity
+  static constexpr int kMaxStreams = 32;
+
+  void ensure_streams() {
+    const size_t want = std::min<size_t>(opts_.size(), kMaxStreams);
+    if (!cap_) PDT_CUDA_CHECK(cudaStreamCreateWithFlags(&cap_, cudaStreamNonBlocking));
+    while (workers_.size() < want) {
+      cudaStream_t s;
+      PDT_CUDA_CHECK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+      workers_.push_back(s);
+    }
+    while (events_.size() < workers_.size() + 1) {
+      cudaEvent_t e;
+      PDT_CUDA_CHECK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+      events_.push_back(e);
+    }
+  }
+  // Runs fn(problem, worker stream) for every problem on worker streams forked from and joined back into `on`.
+  template <class F>
+  void fork_join(cudaStream_t on, F&& fn) {
+    const size_t P = std::min(workers_.size(), opts_.size());
+    PDT_CUDA_CHECK(cudaEventRecord(events_[0], on));
+    for (size_t w = 0; w < P; ++w) PDT_CUDA_CHECK(cudaStreamWaitEvent(workers_[w], events_[0], 0));
+    for (size_t i = 0; i < opts_.size(); ++i) fn(i, workers_[i % P]);
+    for (size_t w = 0; w < P; ++w) {
+      PDT_CUDA_CHECK(cudaEventRecord(events_[w + 1], workers_[w]));
+      PDT_CUDA_CHECK(cudaStreamWaitEvent(on, events_[w + 1], 0));
+    }
+  }
+
+  std::vector<OptImpl*> opts_;
+  std::vector<cudaStream_t> workers_;
+  std::vector<cudaEvent_t> events_;
+  cudaStream_t cap_ = nullptr;
+  IterGraph graph_;
+};
+
 }  // namespace pdt
 
 // ==================================================================================================
@@ -590,6 +726,9 @@ struct pdt_op {
 };
 struct pdt_opt {
   std::unique_ptr<OptImpl> impl;
+};
+struct pdt_batch {
+  std::unique_ptr<BatchImpl> impl;
 };
 
 static thread_local std::string t_last_error;
@@ -884,6 +1023,36 @@ pdt_status pdt_opt_get_result(pdt_opt* opt, void* dst, int is_device, void* stre
     opt->impl->result_size();  // "There is no result yet!" before touching the device
     cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : opt->impl->own_stream();
     opt->impl->get_result(dst, is_device != 0, st);
+    if (!stream) PDT_CUDA_CHECK(cudaStreamSynchronize(st));
+  });
+}
+
+pdt_status pdt_batch_create(pdt_batch** out) {
+  return guarded([&] {
+    need(out, "out");
+    auto h = std::make_unique<pdt_batch>();
+    h->impl = std::make_unique<BatchImpl>();
+    *out = h.release();
+  });
+}
+
+pdt_status pdt_batch_destroy(pdt_batch* b) {
+  return guarded([&] { delete b; });
+}
+
+pdt_status pdt_batch_add(pdt_batch* b, pdt_opt* opt) {
+  return guarded([&] {
+    need(b, "batch");
+    need(opt, "optimizer");
+    b->impl->add(opt->impl.get());
+  });
+}
+
+pdt_status pdt_batch_solve(pdt_batch* b, int verbose, void* stream) {
+  return guarded([&] {
+    need(b, "batch");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    b->impl->solve(verbose != 0, st);
     if (!stream) PDT_CUDA_CHECK(cudaStreamSynchronize(st));
   });
 }

@@ -7,7 +7,11 @@
 // slot k of the inverse input). Included by pdt_cartesian.cu after CartDev.
 #pragma once
 
+#include <cooperative_groups.h>
+
 #include "pdt_regfft.cuh"
+
+namespace cg = cooperative_groups;
 
 namespace pdt {
 namespace {
@@ -101,19 +105,39 @@ __global__ void __launch_bounds__(32 * kFastWarps) fr_cols(CartDev d, int mode, 
     if (ok && lane < B) {
       TL::fwd_step2(u, lane, myex, tw);
       const float* mrow = d.maskc + (size_t)s * Hf;
+      // chunks of loads -> math -> stores: r is read and written in place, so the compiler cannot hoist
+      // a later load above an earlier store; batching keeps CH loads in flight per lane
+      constexpr int CH = A < 8 ? A : 8;
 #pragma unroll
-      for (int ka = 0; ka < A; ++ka) {
-        int ypos = lane + B * ka + d.oyH;
-        if (ypos >= Hf) ypos -= Hf;
-        const float m = mrow[ypos];
-        const float2 kv = u[ka] * (d.scale * m);
+      for (int k0 = 0; k0 < A; k0 += CH) {
+        int yp[CH];
+        float m[CH];
+        float2 fv[CH], rv[CH];
+#pragma unroll
+        for (int q = 0; q < CH; ++q) {
+          int ypos = lane + B * (k0 + q) + d.oyH;
+          if (ypos >= Hf) ypos -= Hf;
+          yp[q] = ypos;
+          m[q] = mrow[ypos];
+        }
         if (mode == COL_FWD_DENSE) {
-          kout[((size_t)c * Hf + ypos) * d.W + d.col_x[s]] = kv;
+#pragma unroll
+          for (int q = 0; q < CH; ++q)
+            kout[((size_t)c * Hf + yp[q]) * d.W + d.col_x[s]] = u[k0 + q] * (d.scale * m[q]);
         } else {
-          const size_t o = colc * Hf + ypos;
-          const float2 rn = (r[o] + sigma * (kv - fc[o])) / (1.0f + sigma * lambda);
-          r[o] = rn;
-          u[ka] = rn * m;
+#pragma unroll
+          for (int q = 0; q < CH; ++q) {
+            fv[q] = fc[colc * Hf + yp[q]];
+            rv[q] = r[colc * Hf + yp[q]];
+          }
+#pragma unroll
+          for (int q = 0; q < CH; ++q) {
+            const float2 kv = u[k0 + q] * (d.scale * m[q]);
+            rv[q] = (rv[q] + sigma * (kv - fv[q])) / (1.0f + sigma * lambda);
+            u[k0 + q] = rv[q] * m[q];
+          }
+#pragma unroll
+          for (int q = 0; q < CH; ++q) r[colc * Hf + yp[q]] = rv[q];
         }
       }
     }
@@ -144,35 +168,67 @@ __global__ void __launch_bounds__(32 * kFastWarps) fr_cols(CartDev d, int mode, 
   }
 }
 
-// Phase 3 (fast): per image row and coil group, IFFT along W of the sampled columns, conj(sens_c)
-// multiply and the group's coil sum in registers (coil order), written as one partial image.
+// Phase 3 (fast): per image row block, IFFT along W of the sampled columns, conj(sens_c) multiply and
+// the coil sum. A cluster of G blocks shares the row block, each block taking one coil group and
+// accumulating in its shared memory; the blocks then reduce the G partial rows through distributed
+// shared memory in rank order (deterministic) and write one K^H r plane. With G = 1 it is a plain launch.
 template <int A, int B>
 __global__ void __launch_bounds__(32 * kFastWarps) fr_rows_adj(CartDev d, const float2* __restrict__ t2,
-                                                               float2* __restrict__ out, int G, long long gstride) {
+                                                               float2* __restrict__ out) {
   using TL = TwoLevel<A, B>;
+  constexpr int W = TL::n;
   extern __shared__ float2 sm[];
   float2* tw = sm;
-  float2* ex = tw + TL::n;
+  float2* ex = tw + W;
   float2* stage = ex + kFastWarps * TL::xch;
-  int* as2s = reinterpret_cast<int*>(stage + (size_t)d.ns * kFastWarps);
-  for (int i = threadIdx.x; i < TL::n; i += blockDim.x) {
+  float2* red = stage + (size_t)d.ns * kFastWarps;  // kFastWarps rows x W: this block's coil-group sum
+  int* as2s = reinterpret_cast<int*>(red + (size_t)kFastWarps * W);
+  cg::cluster_group cluster = cg::this_cluster();
+  const int G = (int)cluster.num_blocks();
+  const int g = (int)cluster.block_rank();
+  for (int i = threadIdx.x; i < W; i += blockDim.x) {
     tw[i] = d.twW[i];
     as2s[i] = d.slot2s[i];
   }
+  for (int i = threadIdx.x; i < kFastWarps * W; i += blockDim.x) red[i] = c2(0.f, 0.f);
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int yi0 = blockIdx.x * kFastWarps, yi = yi0 + w, g = blockIdx.y;
+  const int yi0 = blockIdx.x * kFastWarps, yi = yi0 + w;
   const int nr = min(kFastWarps, d.Hi - yi0);
   const int c_begin = (int)((long long)g * d.C / G), c_end = (int)((long long)(g + 1) * d.C / G);
   float2* myex = ex + w * TL::xch;
   const bool ok = w < nr;
-  float2 acc[B];
+  // prefetch of the next coil's sampled columns (ns * nr values spread over the block)
+  constexpr int PF = 8;
+  float2 pf[PF];
+  auto fetch = [&](int c) {
 #pragma unroll
-  for (int b = 0; b < B; ++b) acc[b] = c2(0.f, 0.f);
+    for (int q = 0; q < PF; ++q) {
+      const int i = threadIdx.x + q * (int)blockDim.x;
+      if (i < d.ns * nr) {
+        const int s = i / nr, rr = i - s * nr;
+        pf[q] = t2[((size_t)c * d.ns + s) * d.Hi + yi0 + rr];
+      }
+    }
+  };
+  const bool pf_all = d.ns * nr <= PF * (int)blockDim.x;
+  if (c_begin < c_end && pf_all) fetch(c_begin);
   for (int c = c_begin; c < c_end; ++c) {
-    __syncthreads();  // stage (and, first time, the tables) ready for reuse
-    for (int i = threadIdx.x; i < d.ns * nr; i += blockDim.x) {
-      const int s = i / nr, rr = i - s * nr;
-      stage[s * kFastWarps + rr] = t2[((size_t)c * d.ns + s) * d.Hi + yi0 + rr];
+    __syncthreads();  // stage free (and, first time, tables and red ready)
+    if (pf_all) {
+#pragma unroll
+      for (int q = 0; q < PF; ++q) {
+        const int i = threadIdx.x + q * (int)blockDim.x;
+        if (i < d.ns * nr) {
+          const int s = i / nr, rr = i - s * nr;
+          stage[s * kFastWarps + rr] = pf[q];
+        }
+      }
+      if (c + 1 < c_end) fetch(c + 1);
+    } else {
+      for (int i = threadIdx.x; i < d.ns * nr; i += blockDim.x) {
+        const int s = i / nr, rr = i - s * nr;
+        stage[s * kFastWarps + rr] = t2[((size_t)c * d.ns + s) * d.Hi + yi0 + rr];
+      }
     }
     __syncthreads();
     if (ok && lane < B) {
@@ -188,31 +244,32 @@ __global__ void __launch_bounds__(32 * kFastWarps) fr_rows_adj(CartDev d, const 
     if (ok && lane < A) {
       float2 v[B];
       TL::inv_step2(v, lane, myex, tw);
-      const float2* srow = d.sens ? d.sens + ((size_t)c * d.Hf + yi + d.y0) * TL::n : nullptr;
+      const float2* srow = d.sens ? d.sens + ((size_t)c * d.Hf + yi + d.y0) * W : nullptr;
+      float2* rrow = red + (size_t)w * W;
 #pragma unroll
       for (int b = 0; b < B; ++b) {
         int x = lane + A * b + d.oxW;
-        if (x >= TL::n) x -= TL::n;
-        acc[b] += srow ? cmulc(v[b], srow[x]) : v[b];
+        if (x >= W) x -= W;
+        rrow[x] += srow ? cmulc(v[b], srow[x]) : v[b];
       }
     }
     __syncwarp();
   }
-  if (ok && lane < A) {
-    float2* orow = out + (size_t)g * gstride + (size_t)yi * TL::n;
-#pragma unroll
-    for (int b = 0; b < B; ++b) {
-      int x = lane + A * b + d.oxW;
-      if (x >= TL::n) x -= TL::n;
-      orow[x] = acc[b];
-    }
+  cluster.sync();  // every block's coil-group rows complete
+  const int total = nr * W;
+  const int beg = (int)((long long)g * total / G), end = (int)((long long)(g + 1) * total / G);
+  for (int i = beg + threadIdx.x; i < end; i += blockDim.x) {
+    float2 acc = c2(0.f, 0.f);
+    for (int q = 0; q < G; ++q) acc += cluster.map_shared_rank(red, q)[i];
+    out[(size_t)(yi0 + i / W) * W + i % W] = acc;
   }
+  cluster.sync();  // keep this block's shared memory alive until the other blocks have read it
 }
 
 typedef void (*FrRowsFwdFn)(CartDev, const float2*, float2*, int*);
 typedef void (*FrColsFn)(CartDev, int, const float2*, float2*, float2*, const float2*, const float2*, float2*, float,
                          float);
-typedef void (*FrRowsAdjFn)(CartDev, const float2*, float2*, int, long long);
+typedef void (*FrRowsAdjFn)(CartDev, const float2*, float2*);
 
 struct FastRowKernels {
   FrRowsFwdFn fwd = nullptr;
@@ -264,6 +321,9 @@ FastColKernels find_col_kernels(int n) {
 size_t fast_rows_smem(const CartDev& d, int A, int B) {
   const size_t n = (size_t)A * B, xch = (size_t)B * (A + 1);
   return sizeof(float2) * (n + kFastWarps * xch + (size_t)d.ns * kFastWarps) + sizeof(int) * n;
+}
+size_t fast_rows_adj_smem(const CartDev& d, int A, int B) {
+  return fast_rows_smem(d, A, B) + sizeof(float2) * (size_t)kFastWarps * A * B;
 }
 size_t fast_cols_smem(int A, int B) {
   const size_t n = (size_t)A * B, xch = (size_t)B * (A + 1);

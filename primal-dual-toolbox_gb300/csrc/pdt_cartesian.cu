@@ -280,7 +280,7 @@ class CartesianOp : public OpImpl, public SolverHooks {
   }
   int groups() override {
     prepare();
-    return G_;
+    return frow_.adj ? 1 : G_;  // the register-FFT path reduces the coil groups inside a cluster
   }
   long long group_stride() override { return (long long)dev_.Hi * dev_.W; }
   void round(const float2* ubar, float2* r, const float2* fc, float sigma, float lambda, float2* khr, int* tick,
@@ -296,7 +296,7 @@ class CartesianOp : public OpImpl, public SolverHooks {
     if (mk) mk->mark("cart_rows_fwd", st);
     launch_cols(COL_SOLVE, t, t, r, fc, nullptr, nullptr, sigma, lambda, st);
     if (mk) mk->mark("cart_cols_prox", st);
-    launch_rows_adj(t, khr, G_, st);
+    launch_rows_adj(t, khr, frow_.adj ? G_ : G_, st);
     if (mk) mk->mark("cart_rows_adj", st);
   }
   void adjoint_compact(const float2* fc, float2* img, cudaStream_t st) override {
@@ -351,6 +351,9 @@ class CartesianOp : public OpImpl, public SolverHooks {
   void invalidate() override { prepared_ = false; }
 
  private:
+  // coil groups per row block on the register-FFT path: a portable cluster of at most 8 blocks
+  static int fast_cluster(int G) { return std::max(1, std::min(G, 8)); }
+
   void launch_rows_fwd(const float2* ubar, float2* t1, int* tick, cudaStream_t st) {
     if (frow_.fwd) {
       dim3 grid((dev_.Hi + kFastWarps - 1) / kFastWarps, dev_.C);
@@ -381,10 +384,21 @@ class CartesianOp : public OpImpl, public SolverHooks {
   }
   void launch_rows_adj(const float2* t2, float2* out, int G, cudaStream_t st) {
     if (frow_.adj) {
-      dim3 grid((dev_.Hi + kFastWarps - 1) / kFastWarps, G);
-      frow_.adj<<<grid, 32 * kFastWarps, fast_rows_smem(dev_, frow_.A, frow_.B), st>>>(dev_, t2, out, G,
-                                                                                      (long long)dev_.Hi * dev_.W);
-      PDT_LAUNCH_CHECK();
+      // the coil groups of one row block form a thread-block cluster and reduce in shared memory
+      const int cl = fast_cluster(G);
+      cudaLaunchConfig_t cfg = {};
+      cfg.gridDim = dim3((dev_.Hi + kFastWarps - 1) / kFastWarps, cl);
+      cfg.blockDim = dim3(32 * kFastWarps);
+      cfg.dynamicSmemBytes = fast_rows_adj_smem(dev_, frow_.A, frow_.B);
+      cfg.stream = st;
+      cudaLaunchAttribute attr[1];
+      attr[0].id = cudaLaunchAttributeClusterDimension;
+      attr[0].val.clusterDim.x = 1;
+      attr[0].val.clusterDim.y = cl;
+      attr[0].val.clusterDim.z = 1;
+      cfg.attrs = attr;
+      cfg.numAttrs = 1;
+      PDT_CUDA_CHECK(cudaLaunchKernelEx(&cfg, frow_.adj, dev_, t2, out));
       count_launch();
       return;
     }
@@ -490,9 +504,11 @@ class CartesianOp : public OpImpl, public SolverHooks {
     fcol_ = find_col_kernels(Hf);
     if (frow_.fwd && fast_rows_smem(d, frow_.A, frow_.B) > (size_t)g_max_smem) frow_ = FastRowKernels();
     if (fcol_.cols && fast_cols_smem(fcol_.A, fcol_.B) > (size_t)g_max_smem) fcol_ = FastColKernels();
+    if (frow_.fwd && fast_rows_adj_smem(d, frow_.A, frow_.B) > (size_t)g_max_smem) frow_ = FastRowKernels();
     if (frow_.fwd) {
       PDT_CUDA_CHECK(cudaFuncSetAttribute(frow_.fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, g_max_smem));
       PDT_CUDA_CHECK(cudaFuncSetAttribute(frow_.adj, cudaFuncAttributeMaxDynamicSharedMemorySize, g_max_smem));
+      PDT_CUDA_CHECK(cudaFuncSetAttribute(frow_.adj, cudaFuncAttributeNonPortableClusterSizeAllowed, 0));
     }
     if (fcol_.cols)
       PDT_CUDA_CHECK(cudaFuncSetAttribute(fcol_.cols, cudaFuncAttributeMaxDynamicSharedMemorySize, g_max_smem));

@@ -208,16 +208,58 @@ __global__ void __launch_bounds__(NT) mri_image_step_kernel(int W, int H, ImgPtr
   const int tid = threadIdx.x;
   const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
   const float2* ub = static_cast<const float2*>(in.ub);
+  const float2 z = c2(0.f, 0.f);
 
+  // Every global load of this thread is issued before the first barrier: its own pixel's duals and
+  // primals (dual-region position (lx, ly), lx, ly >= 1), one halo dual position (left column / top row),
+  // and its share of the u-bar / v-bar staging.
+  const int lx = tid % TX + 1, ly = tid / TX + 1;
+  const int gx = x0 + lx - 1, gy = y0 + ly - 1;
+  const bool own = gx < W && gy < H;
+  const size_t idx = (size_t)gy * W + gx;
+  float2 opx = z, opy = z, oqxx = z, oqyy = z, oqxy = z, ou = z, ovx = z, ovy = z, okh = z;
+  if (own) {
+    opx = static_cast<const float2*>(in.px)[idx];
+    opy = static_cast<const float2*>(in.py)[idx];
+    ou = static_cast<const float2*>(out.u)[idx];
+    okh = khr[idx];
+    for (int g = 1; g < G; ++g) okh += khr[idx + (size_t)g * gstride];
+    if constexpr (TGV) {
+      oqxx = static_cast<const float2*>(in.qxx)[idx];
+      oqyy = static_cast<const float2*>(in.qyy)[idx];
+      oqxy = static_cast<const float2*>(in.qxy)[idx];
+      ovx = static_cast<const float2*>(out.vx)[idx];
+      ovy = static_cast<const float2*>(out.vy)[idx];
+    }
+  }
+  // halo dual positions: top row (hy = 0, hx = 1..TX) then left column (hx = 0, hy = 1..TY)
+  int hx = -1, hy = -1;
+  if (tid < TX + TY) {
+    hx = tid < TX ? tid + 1 : 0;
+    hy = tid < TX ? 0 : tid - TX + 1;
+  }
+  const int hgx = x0 - 1 + hx, hgy = y0 - 1 + hy;
+  const bool halo = hx >= 0 && hgx >= 0 && hgx < W && hgy >= 0 && hgy < H;
+  const size_t hidx = (size_t)hgy * W + hgx;
+  float2 hpx = z, hpy = z, hqxx = z, hqyy = z, hqxy = z;
+  if (halo) {
+    hpx = static_cast<const float2*>(in.px)[hidx];
+    hpy = static_cast<const float2*>(in.py)[hidx];
+    if constexpr (TGV) {
+      hqxx = static_cast<const float2*>(in.qxx)[hidx];
+      hqyy = static_cast<const float2*>(in.qyy)[hidx];
+      hqxy = static_cast<const float2*>(in.qxy)[hidx];
+    }
+  }
   for (int i = tid; i < (TX + 2) * (TY + 2); i += NT) {
-    const int ly = i / (TX + 2), lx = i - ly * (TX + 2);
-    const int gx = x0 - 1 + lx, gy = y0 - 1 + ly;
-    if (gx >= 0 && gx < W && gy >= 0 && gy < H) {
-      const size_t idx = (size_t)gy * W + gx;
-      s_ub[ly][lx] = ub[idx];
+    const int sy = i / (TX + 2), sx = i - sy * (TX + 2);
+    const int ggx = x0 - 1 + sx, ggy = y0 - 1 + sy;
+    if (ggx >= 0 && ggx < W && ggy >= 0 && ggy < H) {
+      const size_t j = (size_t)ggy * W + ggx;
+      s_ub[sy][sx] = ub[j];
       if constexpr (TGV) {
-        s_vbx[ly][lx] = static_cast<const float2*>(in.vbx)[idx];
-        s_vby[ly][lx] = static_cast<const float2*>(in.vby)[idx];
+        s_vbx[sy][sx] = static_cast<const float2*>(in.vbx)[j];
+        s_vby[sy][sx] = static_cast<const float2*>(in.vby)[j];
       }
     }
   }
@@ -229,83 +271,70 @@ __global__ void __launch_bounds__(NT) mri_image_step_kernel(int W, int H, ImgPtr
   }
   __syncthreads();
 
-  for (int i = tid; i < (TX + 1) * (TY + 1); i += NT) {
-    const int ly = i / (TX + 1), lx = i - ly * (TX + 1);
-    if (lx == 0 && ly == 0) continue;
-    const int gx = x0 - 1 + lx, gy = y0 - 1 + ly;
-    if (gx < 0 || gx >= W || gy < 0 || gy >= H) continue;
-    const size_t idx = (size_t)gy * W + gx;
-    const int xp = lx + (gx < W - 1), yp = ly + (gy < H - 1);
-    const float2 c = s_ub[ly][lx];
-    float2 a = static_cast<const float2*>(in.px)[idx];
-    float2 b = static_cast<const float2*>(in.py)[idx];
+  // dual update at dual-region position (qx, qy) with global (qgx, qgy)
+  auto dual = [&](int qx, int qy, int qgx, int qgy, float2 pxo, float2 pyo, float2 qxxo, float2 qyyo, float2 qxyo,
+                  bool write, size_t qidx) {
+    const int xp = qx + (qgx < W - 1), yp = qy + (qgy < H - 1);
+    const float2 c = s_ub[qy][qx];
+    float2 a, b;
     if constexpr (TGV) {
-      a = a + sigma * ((s_ub[ly][xp] - c) - s_vbx[ly][lx]);
-      b = b + sigma * ((s_ub[yp][lx] - c) - s_vby[ly][lx]);
+      a = pxo + sigma * ((s_ub[qy][xp] - c) - s_vbx[qy][qx]);
+      b = pyo + sigma * ((s_ub[yp][qx] - c) - s_vby[qy][qx]);
     } else {
-      a = a + sigma * (s_ub[ly][xp] - c);
-      b = b + sigma * (s_ub[yp][lx] - c);
+      a = pxo + sigma * (s_ub[qy][xp] - c);
+      b = pyo + sigma * (s_ub[yp][qx] - c);
     }
     const float sp = proj_scale(sqrtf(abs2(a) + abs2(b)), alpha1);
     a = a * sp;
     b = b * sp;
-    s_px[ly][lx] = a;
-    s_py[ly][lx] = b;
-    const bool interior = lx > 0 && ly > 0;
-    if (interior) {
-      static_cast<float2*>(out.px)[idx] = a;
-      static_cast<float2*>(out.py)[idx] = b;
+    s_px[qy][qx] = a;
+    s_py[qy][qx] = b;
+    if (write) {
+      static_cast<float2*>(out.px)[qidx] = a;
+      static_cast<float2*>(out.py)[qidx] = b;
     }
     if constexpr (TGV) {
-      const float2 vx = s_vbx[ly][lx], vy = s_vby[ly][lx];
-      const float2 gxx = s_vbx[ly][xp] - vx;
-      const float2 gxy = 0.5f * (s_vbx[yp][lx] - vx + s_vby[ly][xp] - vy);
-      const float2 gyy = s_vby[yp][lx] - vy;
-      const float2 qa = static_cast<const float2*>(in.qxx)[idx] + sigma * gxx;
-      const float2 qb = static_cast<const float2*>(in.qyy)[idx] + sigma * gyy;
-      const float2 qc = static_cast<const float2*>(in.qxy)[idx] + sigma * gxy;
+      const float2 vx = s_vbx[qy][qx], vy = s_vby[qy][qx];
+      const float2 gxx = s_vbx[qy][xp] - vx;
+      const float2 gxy = 0.5f * (s_vbx[yp][qx] - vx + s_vby[qy][xp] - vy);
+      const float2 gyy = s_vby[yp][qx] - vy;
+      const float2 qa = qxxo + sigma * gxx;
+      const float2 qb = qyyo + sigma * gyy;
+      const float2 qc = qxyo + sigma * gxy;
       const float sq = proj_scale(sqrtf(abs2(qa) + abs2(qb) + 2.0f * abs2(qc)), alpha0);
       const float2 na = qa * sq, nb = qb * sq, nc = qc * sq;
-      s_qxx[ly][lx] = na;
-      s_qyy[ly][lx] = nb;
-      s_qxy[ly][lx] = nc;
-      if (interior) {
-        static_cast<float2*>(out.qxx)[idx] = na;
-        static_cast<float2*>(out.qyy)[idx] = nb;
-        static_cast<float2*>(out.qxy)[idx] = nc;
+      s_qxx[qy][qx] = na;
+      s_qyy[qy][qx] = nb;
+      s_qxy[qy][qx] = nc;
+      if (write) {
+        static_cast<float2*>(out.qxx)[qidx] = na;
+        static_cast<float2*>(out.qyy)[qidx] = nb;
+        static_cast<float2*>(out.qxy)[qidx] = nc;
       }
     }
-  }
+  };
+  if (own) dual(lx, ly, gx, gy, opx, opy, oqxx, oqyy, oqxy, true, idx);
+  if (halo) dual(hx, hy, hgx, hgy, hpx, hpy, hqxx, hqyy, hqxy, false, hidx);
   __syncthreads();
 
-  const int lx = tid % TX + 1, ly = tid / TX + 1;
-  const int gx = x0 + lx - 1, gy = y0 + ly - 1;
-  if (gx < W && gy < H) {
-    const size_t idx = (size_t)gy * W + gx;
-    float2 kh = khr[idx];
-    for (int g = 1; g < G; ++g) kh += khr[idx + (size_t)g * gstride];
+  if (own) {
     // TGV_primal_u_noprox_kernel (tgv_kernels.cuh:432-467)
-    float2* u = static_cast<float2*>(out.u);
-    const float2 uo = u[idx];
     const float2 d = div_minus<float2, TX + 1>(s_px, s_py, lx, ly, gx, gy, W, H);
-    const float2 un = uo + tau * (d - kh);
-    u[idx] = un;
-    static_cast<float2*>(out.ub)[idx] = 2.0f * un - uo;
+    const float2 un = ou + tau * (d - okh);
+    static_cast<float2*>(out.u)[idx] = un;
+    static_cast<float2*>(out.ub)[idx] = 2.0f * un - ou;
     if constexpr (TGV) {
       // TGV_primal_v_kernel (tgv_kernels.cuh:647-686)
-      float2* vxp = static_cast<float2*>(out.vx);
-      float2* vyp = static_cast<float2*>(out.vy);
-      const float2 vxo = vxp[idx], vyo = vyp[idx];
       const float2 dqxx = (gx > 0) ? ((gx < W - 1) ? s_qxx[ly][lx] - s_qxx[ly][lx - 1] : -s_qxx[ly][lx - 1]) : s_qxx[ly][lx];
       const float2 dqyy = (gy > 0) ? ((gy < H - 1) ? s_qyy[ly][lx] - s_qyy[ly - 1][lx] : -s_qyy[ly - 1][lx]) : s_qyy[ly][lx];
       const float2 dqxyx = (gx > 0) ? ((gx < W - 1) ? s_qxy[ly][lx] - s_qxy[ly][lx - 1] : -s_qxy[ly][lx - 1]) : s_qxy[ly][lx];
       const float2 dqxyy = (gy > 0) ? ((gy < H - 1) ? s_qxy[ly][lx] - s_qxy[ly - 1][lx] : -s_qxy[ly - 1][lx]) : s_qxy[ly][lx];
-      const float2 vxn = vxo + tau * ((dqxx + dqxyy) + s_px[ly][lx]);
-      const float2 vyn = vyo + tau * ((dqyy + dqxyx) + s_py[ly][lx]);
-      vxp[idx] = vxn;
-      vyp[idx] = vyn;
-      static_cast<float2*>(out.vbx)[idx] = 2.0f * vxn - vxo;
-      static_cast<float2*>(out.vby)[idx] = 2.0f * vyn - vyo;
+      const float2 vxn = ovx + tau * ((dqxx + dqxyy) + s_px[ly][lx]);
+      const float2 vyn = ovy + tau * ((dqyy + dqxyx) + s_py[ly][lx]);
+      static_cast<float2*>(out.vx)[idx] = vxn;
+      static_cast<float2*>(out.vy)[idx] = vyn;
+      static_cast<float2*>(out.vbx)[idx] = 2.0f * vxn - ovx;
+      static_cast<float2*>(out.vby)[idx] = 2.0f * vyn - ovy;
     }
   }
 }

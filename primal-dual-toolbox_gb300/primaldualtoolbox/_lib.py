@@ -30,7 +30,8 @@ EXPORTED = ["pdt_last_error", "pdt_version", "pdt_launch_count", "pdt_host_alloc
             "pdt_op_output_size", "pdt_op_forward", "pdt_op_adjoint", "pdt_op_describe", "pdt_op_adjointness",
             "pdt_opt_create", "pdt_opt_destroy", "pdt_opt_get_params", "pdt_opt_set_params", "pdt_opt_set_operator",
             "pdt_opt_set_noisy_data", "pdt_opt_set_input0", "pdt_opt_solve", "pdt_opt_result_size",
-            "pdt_opt_get_result", "pdt_opt_profile", "pdt_cartesian_forward_noalloc"]
+            "pdt_opt_get_result", "pdt_opt_profile", "pdt_batch_create", "pdt_batch_destroy", "pdt_batch_add",
+            "pdt_batch_solve", "pdt_cartesian_forward_noalloc"]
 
 
 class PdtError(RuntimeError):
@@ -83,6 +84,10 @@ def _load():
     L.pdt_opt_get_result.argtypes = [vp, vp, i, vp]
     L.pdt_opt_profile.argtypes = [vp, i, vp, i, ctypes.POINTER(i), ctypes.c_char_p, ctypes.c_size_t,
                                   ctypes.POINTER(ctypes.c_double)]
+    L.pdt_batch_create.argtypes = [ctypes.POINTER(vp)]
+    L.pdt_batch_destroy.argtypes = [vp]
+    L.pdt_batch_add.argtypes = [vp, vp]
+    L.pdt_batch_solve.argtypes = [vp, i, vp]
     L.pdt_cartesian_forward_noalloc.argtypes = [i, vp, vp, i, i, i, vp, vp, vp]
     for name in EXPORTED:
         if name not in ("pdt_last_error", "pdt_version", "pdt_launch_count"):

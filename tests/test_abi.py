@@ -88,10 +88,17 @@ def test_parameters_defaults_and_write_through(pdt):
         t.max_iter = -1
 
 
-def test_radial_config_validation(pdt):
-    with pytest.raises(pdt.PdtError) as e:
+def test_radial_config_errors(pdt):
+    """OperatorBase(..., config, 4, 4) and getConfigDouble/Int (mriradialoperator.cu:28-35)."""
+    with pytest.raises(pdt.PdtError, match=r"\(min: 4 max: 4\) required, got \(3\)"):
         pdt.mri.MriRadialOperator({"osf": 2, "sector_width": 8, "kernel_width": 3})
-    assert e.value.status_name in ("PDT_ERR_CONFIG", "PDT_ERR_UNSUPPORTED")
+    with pytest.raises(pdt.PdtError, match="could not parse configuration parameter 'osf'"):
+        pdt.mri.MriRadialOperator({"osf": "two", "sector_width": 8, "kernel_width": 3, "img_dim": 64})
+    # img_dim given as a float, as bin/mri_radial_test.py does (nFE/2), parses like the reference's stringstream
+    op = pdt.mri.MriRadialOperator({"osf": 2, "sector_width": 8, "kernel_width": 3, "img_dim": 64 / 2})
+    assert str(op) == "MriRadialOperator: Added constants: (0/3)"
+    assert str(pdt.mri.MriRadialSinglecoilOperator(
+        {"osf": 2, "sector_width": 8, "kernel_width": 3, "img_dim": 32})) == "MriRadialOperator: Added constants: (0/2)"
 
 
 def test_launch_count_starts_at_zero_without_gpu(pdt):
