@@ -44,6 +44,24 @@ def _rank_info():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
 
 
+def max_over_ranks(value, dist=None):
+    """Maximum of a per-rank float over all ranks (identity without a process group). Replicas only: the
+    data path has no collective; this is the timing barrier's max-over-ranks."""
+    if dist is None or not dist.is_initialized() or dist.get_world_size() == 1:
+        return float(value)
+    import torch
+
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(value)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(iters_per_step, steps, world, t_max):
+    """Whole-job iterations/s: every rank solves its own reconstruction (weak scaling)."""
+    return iters_per_step * steps * world / t_max
+
+
 def _problem(seed=0):
     from primaldualtoolbox import synthetic
 
@@ -190,12 +208,8 @@ def run_ours(args):
         wall = time.perf_counter() - t0
     launches = pdt.launch_count() - n0
     dev_s = ev0.elapsed_time(ev1) / 1e3
-    t_max = dev_s
-    if dist:
-        t = torch.tensor([dev_s], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_max = float(t.item())
-    value = ITERS * args.steps * world / t_max
+    t_max = max_over_ranks(dev_s, dist)
+    value = replica_throughput(ITERS, args.steps, world, t_max)
 
     # per-kernel timing (CUDA events on the launching stream) for the roofline of the dominant kernel
     phases = opt.profile(iters=50, stream=stream)
@@ -212,6 +226,10 @@ def run_ours(args):
             "share": round(phases[dom] / per_iter_ms, 3)}
     phase_info = {k: {"ms": round(v, 5), "GB/s": round(bytes_per.get(k, 0) / (v / 1e3) / 1e9, 1)}
                   for k, v in phases.items()}
+
+    conv = None
+    if args.accuracy:
+        conv = {"plain": time_to_accuracy(pdt, torch, case, dev, stream, t_max / args.steps / ITERS)}
 
     # e2e: the public API with pinned host buffers, every input uploaded and the result read back
     host = {k: pdt.pinned_empty(case[k].shape, case[k].dtype) for k in ("rawdata", "sens", "mask")}
@@ -243,12 +261,8 @@ def run_ours(args):
     for _ in range(e_steps):
         e2e_step()
     torch.cuda.synchronize()
-    e2e_s = time.perf_counter() - t0
-    if dist:
-        t = torch.tensor([e2e_s], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e_val = ITERS * e_steps * world / e2e_s
+    e2e_s = max_over_ranks(time.perf_counter() - t0, dist)
+    e2e_val = replica_throughput(ITERS, e_steps, world, e2e_s)
 
     line = None
     if rank == 0:
@@ -266,7 +280,9 @@ def run_ours(args):
             "gpu_launches": int(launches),
             "roofline": roof,
             "phases": phase_info,
+            "tuning": op.tuning(),
             "cpu_baseline": cpu,
+            "time_to_1e-4": conv,
             "clocks": clk.summary(),
             "wall_s": round(wall, 3),
         }
@@ -275,6 +291,59 @@ def run_ours(args):
         dist.barrier()
         dist.destroy_process_group()
     return line
+
+
+def time_to_accuracy(pdt, torch, case, dev, stream, per_iter_s, target=1e-4, ref_iters=30000, chunk=50,
+                     max_iters=20000, u_init=None, v_init=None):
+    """Iterations (and time at the measured per-iteration rate) for the plain start u0 = A^H f -- or a given
+    (u, v) warm start -- to reach rel-L2 <= target against the converged solution at fixed alpha
+    (reduction = 1). The converged solution is the engine's own fixed point after ref_iters iterations;
+    its stationarity (relative change over the last 1000 iterations) is reported. Errors are FP64 GPU
+    reductions outside the timed iterations."""
+    def make():
+        op = pdt.mri.MriCartesianRemoveROOSOperator()
+        op.setCoilSens(dev["sens"])
+        op.setMask(dev["mask"])
+        opt = pdt.mri.TgvMriOptimizer_2c3c()
+        prm = opt.getParameters()
+        prm.reduction, prm.alpha1 = 1.0, case["alpha1"]
+        prm.alpha0 = 2 * prm.alpha1
+        opt.setOperator(op)
+        opt.setNoisyData(dev["rawdata"], stream=stream)
+        return op, opt, prm
+
+    op, ref, prm = make()
+    prm.max_iter = ref_iters - 1001
+    ref.solve(stream=stream)
+    u_prev = torch.empty((H // 2, W), dtype=torch.complex64, device="cuda")
+    ref.getResult(out=u_prev, stream=stream)
+    prm.max_iter = 1000
+    ref.solve(stream=stream)
+    u_star = torch.empty_like(u_prev)
+    ref.getResult(out=u_star, stream=stream)
+    torch.cuda.synchronize()
+    n_star = pdt.dist2(u_star) ** 0.5
+    stationarity = pdt.dist2(u_star, u_prev) ** 0.5 / n_star
+
+    op2, opt, prm2 = make()
+    if u_init is not None:
+        opt.setInput0UV(u_init, v_init, stream=stream)
+    prm2.max_iter = chunk - 1
+    u = torch.empty_like(u_star)
+    it, err = 0, None
+    while it < max_iters:
+        opt.solve(stream=stream)
+        it += chunk
+        opt.getResult(out=u, stream=stream)
+        torch.cuda.synchronize()
+        err = pdt.dist2(u, u_star) ** 0.5 / n_star
+        if err <= target:
+            break
+    reached = err is not None and err <= target
+    return {"target_rel_l2": target, "iterations": it if reached else None, "reached": reached,
+            "final_rel_l2": err, "ms": round(it * per_iter_s * 1e3, 3) if reached else None,
+            "reference_iterations": ref_iters, "reference_stationarity": stationarity,
+            "alpha": "fixed (reduction 1)", "check_every": chunk}
 
 
 def _coil_groups(ns):
@@ -351,6 +420,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--accuracy", type=int, default=1, help="measure iterations/time to rel-L2 1e-4 (1) or skip (0)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -124,6 +124,9 @@ PDT_API pdt_status pdt_op_adjoint(pdt_op* op, const void* src, int src_ndim, con
                           int dst_ndim, const int64_t* dst_size, int is_device, void* stream);
 /* OperatorBase::print (operatorbase.h:343-351), e.g. "MriCartesianOperator: Added constants: (2/2)". */
 PDT_API pdt_status pdt_op_describe(pdt_op* op, char* buf, size_t len);
+/* No reference counterpart: the kernel configuration the operator's autotuner picked (launch shapes timed
+ * with CUDA events at set-up and cached per problem shape), as text. */
+PDT_API pdt_status pdt_op_tuning(pdt_op* op, char* buf, size_t len);
 /* adjointnessCheck (mricartesianoperator.cu:267-282 and siblings): random u, p (seeded), returns
  * <Au, p> and <u, A^H p> accumulated in double. */
 PDT_API pdt_status pdt_op_adjointness(pdt_op* op, uint64_t seed, double out[4]);
@@ -155,6 +158,40 @@ PDT_API pdt_status pdt_opt_get_result(pdt_opt* opt, void* dst, int is_device, vo
  * The iterations advance the optimizer state exactly like solve(). */
 PDT_API pdt_status pdt_opt_profile(pdt_opt* opt, int iters, void* stream, int max_phases, int* nphases, char* names,
                                    size_t names_len, double* ms);
+
+/* ---- FP64 metrics and state access (no counterpart in the reference, which reports no energies) ----- */
+/* setInput0 with the second TGV primal as well: u = u-bar = u0; v = v-bar = v0 (two planes vx then vy,
+ * each the size of u0; v0 may be NULL); p = q = 0. */
+PDT_API pdt_status pdt_opt_set_input0_uv(pdt_opt* opt, const void* u0, const void* v0, int ndim, const int64_t* size,
+                                         int is_device, void* stream);
+/* Copies one state plane: 0 u, 1 u-bar, 2 vx, 3 vy, 4 v-bar x, 5 v-bar y, 6 px, 7 py, 8 qxx, 9 qyy, 10 qxy. */
+PDT_API pdt_status pdt_opt_get_field(pdt_opt* opt, int field, void* dst, int is_device, void* stream);
+/* Energy of the current state accumulated in FP64: out = {total, data, first-order, second-order} --
+ * 1/2 ||K u - f||^2 + alpha1 sum |grad u - v| + alpha0 sum |eps(v)| (TGV-MRI at its final alpha), or the
+ * TV / denoising forms. */
+PDT_API pdt_status pdt_opt_energy(pdt_opt* opt, void* stream, double out[4]);
+/* Operator norm ||K|| by `iters` power iterations on K^H K (FP64 norms). */
+PDT_API pdt_status pdt_op_norm(pdt_op* op, int iters, uint64_t seed, double* out);
+/* sum |a - b|^2 of two device arrays (b may be NULL) accumulated in FP64. */
+PDT_API pdt_status pdt_dist2(pdt_dtype dtype, const void* a, const void* b, size_t n, void* stream, double* out);
+
+/* ---- learned warm start (no counterpart in the reference) --------------------------------------- */
+/* A residual CNN (8 convolutions, 32 channels, 3 x 3, BF16 weights and activations, FP32 accumulation)
+ * mapping the zero-filled image u0 = A^H f to an initial (u, v) for the TGV^2 solvers. All image
+ * pointers are device pointers: u0, u [B][H][W] complex64; v [B][2][H][W] complex64 (vx then vy).
+ * Training minimises the mean squared error to target solutions (ut, vt), scaled per image by max|u0|. */
+typedef struct pdt_cnn pdt_cnn;
+PDT_API pdt_status pdt_cnn_create(uint64_t seed, pdt_cnn** out);
+PDT_API pdt_status pdt_cnn_destroy(pdt_cnn* c);
+PDT_API pdt_status pdt_cnn_num_params(pdt_cnn* c, size_t* n);
+PDT_API pdt_status pdt_cnn_get_params(pdt_cnn* c, float* dst, size_t n);  /* host FP32 */
+PDT_API pdt_status pdt_cnn_set_params(pdt_cnn* c, const float* src, size_t n);
+PDT_API pdt_status pdt_cnn_get_grads(pdt_cnn* c, float* dst, size_t n);   /* gradients of the last step */
+/* One forward + backward pass; with lr > 0 also one Adam step. *loss = mean over pixels of the summed
+ * squared error of the six output channels. */
+PDT_API pdt_status pdt_cnn_train_step(pdt_cnn* c, const void* u0, const void* ut, const void* vt, int B, int H,
+                                      int W, float lr, void* stream, double* loss);
+PDT_API pdt_status pdt_cnn_predict(pdt_cnn* c, const void* u0, int B, int H, int W, void* u, void* v, void* stream);
 
 /* ---- batched solves ------------------------------------------------------------------------------ */
 /* No counterpart in the reference (which solves one reconstruction per call): a batch advances many

@@ -51,7 +51,7 @@ def lib():
         L.orc_tv_solve.argtypes = [i, i, i, i, vp, vp, vp, d, u]
         L.orc_tgv_solve.argtypes = [i, i, i, i, vp, vp, vp, d, d, d, u]
         L.orc_op_apply.argtypes = [i, i, i, i, i, i, vp, vp, vp, vp]
-        L.orc_op_solve.argtypes = [i, i, i, i, i, vp, vp, vp, vp, vp, i, d, d, d, d, u, vp]
+        L.orc_op_solve.argtypes = [i, i, i, i, i, vp, vp, vp, vp, vp, i, d, d, d, d, u, vp, vp]
         L.orc_alpha_schedule_f32.argtypes = [ctypes.c_float, ctypes.c_float, ctypes.c_float, u, u,
                                              ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]
         L.orc_radial_apply.argtypes = [i, i, i, d, i, i, i, vp, vp, vp, vp, vp]
@@ -62,6 +62,10 @@ def lib():
         L.orc_kb_beta.restype = d
         L.orc_kb_deapod.argtypes = [i, i, i, d]
         L.orc_kb_deapod.restype = d
+        L.orc_cnn_grad_exact.restype = d
+        L.orc_cnn_grad_exact.argtypes = [i, i, i, vp, vp, vp, vp, vp]
+        L.orc_cnn_grad.restype = d
+        L.orc_cnn_grad.argtypes = [i, i, i, vp, vp, vp, vp, vp, vp]
         L.orc_tgv_energy_f64.restype = d
         L.orc_tgv_energy_f64.argtypes = [i, i, i, i, vp, vp, vp, vp, vp, vp, d, d]
         _lib = L
@@ -115,8 +119,10 @@ def op_apply(kind, sens, mask, src, adjoint=False, prec=64):
 
 
 def op_solve(kind, sens, mask, f, variant="tgv_mri", alpha0=1.0, alpha1=1.0, reduction=1.0, lam=1.0,
-             max_iter=1, u0=None, prec=32, return_state=False):
-    """TgvMriOptimizer / TgvOptimizerWithOp / TvOptimizerWithOp with a Cartesian-family operator."""
+             max_iter=1, u0=None, prec=32, return_state=False, state=None):
+    """TgvMriOptimizer / TgvOptimizerWithOp / TvOptimizerWithOp with a Cartesian-family operator.
+    `state` (a dict as returned with return_state=True) continues a previous solve from all of its
+    primal and dual variables, as a second solve() call on the same optimizer does."""
     k = KIND[kind]
     mask = np.ascontiguousarray(mask, dtype=_re(prec))
     Hf, W = mask.shape
@@ -129,12 +135,17 @@ def op_solve(kind, sens, mask, f, variant="tgv_mri", alpha0=1.0, alpha1=1.0, red
     f = np.ascontiguousarray(f, dtype=_cx(prec))
     u0 = None if u0 is None else np.ascontiguousarray(u0, dtype=_cx(prec))
     u = np.zeros((Hi, W), dtype=_cx(prec))
+    names = ["u", "ubar", "vx", "vy", "vbx", "vby", "px", "py", "qxx", "qyy", "qxy"]
+    sin = None
+    if state is not None:
+        sin = np.concatenate([np.ravel(state[nm]) for nm in names] + [np.ravel(state["r"])]).astype(_cx(prec))
+        if sin.size != 11 * Hi * W + C * Hf * W:
+            raise ValueError("state does not match the problem size")
     state = np.zeros(11 * Hi * W + C * Hf * W, dtype=_cx(prec)) if return_state else None
     lib().orc_op_solve(prec, k, W, Hf, C, _ptr(s), _ptr(mask), _ptr(f), _ptr(u0), _ptr(u), VARIANT[variant],
-                       alpha0, alpha1, reduction, lam, int(max_iter), _ptr(state))
+                       alpha0, alpha1, reduction, lam, int(max_iter), _ptr(state), _ptr(sin))
     if return_state:
         n = Hi * W
-        names = ["u", "ubar", "vx", "vy", "vbx", "vby", "px", "py", "qxx", "qyy", "qxy"]
         st = {nm: state[i * n:(i + 1) * n].reshape(Hi, W) for i, nm in enumerate(names)}
         st["r"] = state[11 * n:].reshape((Hf, W) if k == 2 else (C, Hf, W))
         return u, st
@@ -214,3 +225,27 @@ def radial_solve(traj, dcf, sens, f, N, osf, kw, variant="tgv_mri", alpha0=1.0, 
 
 def radial_grid_size(N, osf):
     return lib().orc_radial_grid_size(N, osf)
+
+
+def cnn_grad(params, u0, ut, vt):
+    """Loss, flat gradient (FP64) and output (B, H, W, 8) of the warm-start network for a batch.
+    u0, ut: (B, H, W) complex64; vt: (B, 2, H, W) complex64; params: flat float32."""
+    params = np.ascontiguousarray(params, dtype=np.float32)
+    u0 = np.ascontiguousarray(u0, dtype=np.complex64)
+    ut = np.ascontiguousarray(ut, dtype=np.complex64)
+    vt = np.ascontiguousarray(vt, dtype=np.complex64)
+    B, H, W = u0.shape
+    g = np.zeros(params.size, dtype=np.float64)
+    out = np.zeros((B, H, W, 8), dtype=np.float64)
+    loss = lib().orc_cnn_grad(B, H, W, _ptr(params), _ptr(u0), _ptr(ut), _ptr(vt), _ptr(g), _ptr(out))
+    return loss, g, out
+
+
+def cnn_grad_exact(params, u0, ut, vt):
+    """Loss and gradient of the network in FP64 without BF16 rounding (finite-difference checkable)."""
+    params = np.ascontiguousarray(params, dtype=np.float32)
+    u0, ut, vt = (np.ascontiguousarray(a, dtype=np.complex64) for a in (u0, ut, vt))
+    B, H, W = u0.shape
+    g = np.zeros(params.size, dtype=np.float64)
+    loss = lib().orc_cnn_grad_exact(B, H, W, _ptr(params), _ptr(u0), _ptr(ut), _ptr(vt), _ptr(g))
+    return loss, g

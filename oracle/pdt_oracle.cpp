@@ -676,18 +676,27 @@ inline void alpha_schedule(R a0, R a1, R reduction, unsigned max_iter, unsigned 
 // (tgvoptimizerwithop.cu:89-179), 2 = TvOptimizerWithOp (tvoptimizerwithop.cu:86-164).
 template <class R, class Op>
 void op_solve(const Op& op, const cx<R>* f, const cx<R>* u0, cx<R>* uout, int variant, R alpha0, R alpha1,
-              R reduction, R lambda, unsigned max_iter, cx<R>* state_out) {
+              R reduction, R lambda, unsigned max_iter, cx<R>* state_out, const cx<R>* state_in = nullptr) {
   typedef cx<R> P;
   const int W = op.img_w(), H = op.img_h();
   ImgState<P> s(W, H);
   const size_t nk = op.ksp_n(), ni = op.img_n();
   std::vector<P> r(nk, pzero<P>()), tmp(nk);
-  if (u0) {
-    std::copy(u0, u0 + ni, s.u.begin());
+  if (state_in) {  // a later solve() continues from every primal and dual variable (tgvmrioptimizer.cu:62-91)
+    const P* o = state_in;
+    for (auto* v : {&s.u, &s.ubar, &s.vx, &s.vy, &s.vbx, &s.vby, &s.px, &s.py, &s.qxx, &s.qyy, &s.qxy}) {
+      std::copy(o, o + ni, v->begin());
+      o += ni;
+    }
+    std::copy(o, o + nk, r.begin());
   } else {
-    op.adjoint(f, s.u.data());  // "Initialization with A^T(f)"
+    if (u0) {
+      std::copy(u0, u0 + ni, s.u.begin());
+    } else {
+      op.adjoint(f, s.u.data());  // "Initialization with A^T(f)"
+    }
+    std::copy(s.u.begin(), s.u.end(), s.ubar.begin());
   }
-  std::copy(s.u.begin(), s.u.end(), s.ubar.begin());
   const R tau = (variant == 0) ? (R)(1.0 / 16.0) : (R)(1.0 / 8.0);
   const R sigma = (R)(1.0 / 8.0);
   const R lam = (variant == 0) ? R(1) : lambda;
@@ -749,6 +758,188 @@ double tgv_energy(const CartOp<R>& op, const cx<R>* f, const cx<R>* u, const cx<
     }
   return 0.5 * data + (double)alpha1 * t1 + (double)alpha0 * t0;
 }
+
+
+// ------------------------------------------------------------------------------------------------
+// The learned warm-start network (the engine's pdt_cnn.cu), restated for gradient checks: FP64
+// arithmetic with BF16 round-to-nearest-even applied exactly where the GPU stores BF16 (weights of the
+// 32-channel convolutions, activations, pre-activations, output and hidden gradients).
+// Parameter layout (flat): per layer weights [9][COUT][CIN] then bias [COUT]; layers conv_in (2 -> 32),
+// six hidden (32 -> 32), conv_out (32 -> 8, channels 6 and 7 unused).
+// ------------------------------------------------------------------------------------------------
+static bool g_cnn_round = true;  // BF16 rounding emulation (off: exact FP64, for finite-difference checks)
+inline float bf16r(float f) {
+  if (!g_cnn_round) return f;
+  uint32_t u;
+  std::memcpy(&u, &f, 4);
+  if ((u & 0x7f800000u) == 0x7f800000u) return f;
+  u += 0x7fffu + ((u >> 16) & 1u);
+  u &= 0xffff0000u;
+  std::memcpy(&f, &u, 4);
+  return f;
+}
+
+struct CnnOracle {
+  int B, H, W;
+  size_t np;
+  static const int L = 8;
+  int cin[L], cout[L];
+  std::vector<double> w[L], b[L];  // FP32 master values (as double)
+  std::vector<double> gw[L], gb[L];
+  CnnOracle(int B_, int H_, int W_, const float* params) : B(B_), H(H_), W(W_), np((size_t)B_ * H_ * W_) {
+    size_t o = 0;
+    for (int l = 0; l < L; ++l) {
+      cin[l] = l == 0 ? 2 : 32;
+      cout[l] = l == 7 ? 8 : 32;
+      const size_t nw = (size_t)9 * cout[l] * cin[l];
+      w[l].assign(params + o, params + o + nw);
+      o += nw;
+      b[l].assign(params + o, params + o + cout[l]);
+      o += cout[l];
+      if (l >= 1)
+        for (auto& v : w[l]) v = bf16r((float)v);  // tensor-core layers use BF16 weights
+    }
+  }
+  // y[p][co] = sum_{tap, ci} x[p + d(tap)][ci] w[tap][co][ci] + bias (zero padding)
+  void conv(const std::vector<double>& x, int ci_n, const std::vector<double>& wt, const double* bias, int co_n,
+            std::vector<double>& y) const {
+    y.assign(np * co_n, 0.0);
+#pragma omp parallel for schedule(static)
+    for (long long p = 0; p < (long long)np; ++p) {
+      const int xx = (int)(p % W), yy = (int)((p / W) % H), bb = (int)(p / ((size_t)W * H));
+      for (int co = 0; co < co_n; ++co) {
+        double s = bias ? bias[co] : 0.0;
+        for (int tap = 0; tap < 9; ++tap) {
+          const int gy = yy + tap / 3 - 1, gx = xx + tap % 3 - 1;
+          if (gy < 0 || gy >= H || gx < 0 || gx >= W) continue;
+          const size_t q = ((size_t)bb * H + gy) * W + gx;
+          for (int ci = 0; ci < ci_n; ++ci) s += x[q * ci_n + ci] * wt[((size_t)tap * co_n + co) * ci_n + ci];
+        }
+        y[p * co_n + co] = s;
+      }
+    }
+  }
+  // transposed convolution (data gradient): dx[q][ci] = sum_{tap, co} dy[q - d(tap)][co] w[tap][co][ci]
+  void conv_t(const std::vector<double>& dy, int co_n, const std::vector<double>& wt, int ci_n,
+              std::vector<double>& dx) const {
+    dx.assign(np * ci_n, 0.0);
+#pragma omp parallel for schedule(static)
+    for (long long q = 0; q < (long long)np; ++q) {
+      const int xx = (int)(q % W), yy = (int)((q / W) % H), bb = (int)(q / ((size_t)W * H));
+      for (int ci = 0; ci < ci_n; ++ci) {
+        double s = 0;
+        for (int tap = 0; tap < 9; ++tap) {
+          const int py = yy - (tap / 3 - 1), px = xx - (tap % 3 - 1);
+          if (py < 0 || py >= H || px < 0 || px >= W) continue;
+          const size_t p = ((size_t)bb * H + py) * W + px;
+          for (int co = 0; co < co_n; ++co) s += dy[p * co_n + co] * wt[((size_t)tap * co_n + co) * ci_n + ci];
+        }
+        dx[q * ci_n + ci] = s;
+      }
+    }
+  }
+  void wgrad(const std::vector<double>& x, int ci_n, const std::vector<double>& dy, int co_n, std::vector<double>& gw_,
+             std::vector<double>& gb_) const {
+    gw_.assign((size_t)9 * co_n * ci_n, 0.0);
+    gb_.assign(co_n, 0.0);
+#pragma omp parallel for schedule(static)
+    for (int idx = 0; idx < 9 * co_n; ++idx) {
+      const int tap = idx / co_n, co = idx % co_n;
+      for (int ci = 0; ci < ci_n; ++ci) {
+        double s = 0;
+        for (size_t p = 0; p < np; ++p) {
+          const int xx = (int)(p % W), yy = (int)((p / W) % H), bb = (int)(p / ((size_t)W * H));
+          const int gy = yy + tap / 3 - 1, gx = xx + tap % 3 - 1;
+          if (gy < 0 || gy >= H || gx < 0 || gx >= W) continue;
+          s += x[(((size_t)bb * H + gy) * W + gx) * ci_n + ci] * dy[p * co_n + co];
+        }
+        gw_[((size_t)tap * co_n + co) * ci_n + ci] = s;
+      }
+    }
+    for (int co = 0; co < co_n; ++co) {
+      double s = 0;
+      for (size_t p = 0; p < np; ++p) s += dy[p * co_n + co];
+      gb_[co] = s;
+    }
+  }
+  static void round_bf16(std::vector<double>& v) {
+    if (!g_cnn_round) return;
+    for (auto& x : v) x = bf16r((float)x);
+  }
+  // loss and gradients; u0, ut complex [B][H][W]; vt [B][2][H][W]
+  double run(const float* u0, const float* ut, const float* vt, double* out6 /* nullable: [np][8] */) {
+    std::vector<double> s(B);
+    for (int bb = 0; bb < B; ++bb) {
+      float m = 0.f;
+      for (size_t i = 0; i < (size_t)H * W; ++i) {
+        const size_t k = (size_t)bb * H * W + i;
+        m = std::max(m, std::sqrt(u0[2 * k] * u0[2 * k] + u0[2 * k + 1] * u0[2 * k + 1]));
+      }
+      s[bb] = m > 0.f ? m : 1.f;
+    }
+    std::vector<double> x(np * 2), t(np * 6);
+    const size_t hw = (size_t)H * W;
+    for (size_t p = 0; p < np; ++p) {
+      const size_t bb = p / hw, i = p % hw;
+      const float inv = 1.f / (float)s[bb];
+      x[2 * p] = u0[2 * p] * inv;
+      x[2 * p + 1] = u0[2 * p + 1] * inv;
+      t[6 * p + 0] = (ut[2 * p] - u0[2 * p]) * inv;
+      t[6 * p + 1] = (ut[2 * p + 1] - u0[2 * p + 1]) * inv;
+      for (int c = 0; c < 2; ++c) {
+        const size_t vi = ((2 * bb + c) * hw + i) * 2;
+        t[6 * p + 2 + 2 * c] = vt[vi] * inv;
+        t[6 * p + 3 + 2 * c] = vt[vi + 1] * inv;
+      }
+    }
+    // forward
+    std::vector<double> z[7], h[7], o;
+    conv(x, 2, w[0], b[0].data(), 32, z[0]);
+    h[0] = z[0];
+    for (auto& v : h[0]) v = bf16r((float)std::max(v, 0.0));
+    round_bf16(z[0]);
+    for (int l = 1; l <= 6; ++l) {
+      conv(h[l - 1], 32, w[l], b[l].data(), 32, z[l]);
+      h[l].resize(np * 32);
+      for (size_t i = 0; i < np * 32; ++i) h[l][i] = bf16r((float)(h[l - 1][i] + std::max(z[l][i], 0.0)));
+      round_bf16(z[l]);
+    }
+    conv(h[6], 32, w[7], b[7].data(), 8, o);
+    if (g_cnn_round)
+      for (auto& v : o) v = (float)v;
+    if (out6) std::copy(o.begin(), o.end(), out6);
+    // loss
+    double loss = 0;
+    std::vector<double> go(np * 8, 0.0);
+    for (size_t p = 0; p < np; ++p)
+      for (int c = 0; c < 6; ++c) {
+        const double d = o[p * 8 + c] - t[p * 6 + c];
+        loss += d * d;
+        go[p * 8 + c] = bf16r((float)(2.0 * d / (double)np));
+      }
+    // backward
+    wgrad(h[6], 32, go, 8, gw[7], gb[7]);
+    std::vector<double> g, tmp;
+    conv_t(go, 8, w[7], 32, tmp);
+    round_bf16(tmp);
+    g = tmp;
+    for (int l = 6; l >= 1; --l) {
+      std::vector<double> gz(np * 32);
+      for (size_t i = 0; i < np * 32; ++i) {
+        const double gi = bf16r((float)g[i]);
+        gz[i] = z[l][i] > 0 ? gi : 0.0;
+      }
+      wgrad(h[l - 1], 32, gz, 32, gw[l], gb[l]);
+      conv_t(gz, 32, w[l], 32, tmp);
+      round_bf16(tmp);
+      for (size_t i = 0; i < np * 32; ++i) g[i] += tmp[i];
+    }
+    std::vector<double> gz(np * 32);
+    for (size_t i = 0; i < np * 32; ++i) gz[i] = z[0][i] > 0 ? bf16r((float)g[i]) : 0.0;
+    wgrad(x, 2, gz, 32, gw[0], gb[0]);
+    return loss / (double)np;
+  }
+};
 
 }  // namespace
 
@@ -837,15 +1028,16 @@ void orc_op_apply(int prec, int kind, int adjoint, int W, int Hf, int C, const v
 // TgvMriOptimizer / TgvOptimizerWithOp / TvOptimizerWithOp with a Cartesian-family operator.
 void orc_op_solve(int prec, int kind, int W, int Hf, int C, const void* sens, const void* mask, const void* f,
                   const void* u0, void* uout, int variant, double alpha0, double alpha1, double reduction,
-                  double lambda, unsigned max_iter, void* state_out) {
+                  double lambda, unsigned max_iter, void* state_out, const void* state_in) {
   if (prec == 32) {
     CartOp<float> op(kind, W, Hf, C, (const cx<float>*)sens, (const float*)mask);
     op_solve<float, CartOp<float>>(op, (const cx<float>*)f, (const cx<float>*)u0, (cx<float>*)uout, variant, (float)alpha0,
-                    (float)alpha1, (float)reduction, (float)lambda, max_iter, (cx<float>*)state_out);
+                    (float)alpha1, (float)reduction, (float)lambda, max_iter, (cx<float>*)state_out,
+                    (const cx<float>*)state_in);
   } else {
     CartOp<double> op(kind, W, Hf, C, (const cx<double>*)sens, (const double*)mask);
     op_solve<double, CartOp<double>>(op, (const cx<double>*)f, (const cx<double>*)u0, (cx<double>*)uout, variant, alpha0, alpha1,
-                     reduction, lambda, max_iter, (cx<double>*)state_out);
+                     reduction, lambda, max_iter, (cx<double>*)state_out, (const cx<double>*)state_in);
   }
 }
 
@@ -896,5 +1088,34 @@ void orc_radial_solve(int prec, int N, double osf, int kw, int C, int Ns, const 
 int orc_radial_grid_size(int N, double osf) { return radial_grid_size(N, osf); }
 double orc_kb_beta(int kw, double osf) { return kb_beta(kw, osf); }
 double orc_kb_deapod(int m, int G, int kw, double beta) { return kb_deapod(m, G, kw, beta); }
+
+// The same network without any BF16 rounding (every value FP64 except the FP32 inputs and parameters).
+double orc_cnn_grad_exact(int B, int H, int W, const float* params, const float* u0, const float* ut,
+                          const float* vt, double* grads) {
+  g_cnn_round = false;
+  CnnOracle net(B, H, W, params);
+  const double loss = net.run(u0, ut, vt, nullptr);
+  g_cnn_round = true;
+  size_t o = 0;
+  for (int l = 0; l < CnnOracle::L; ++l) {
+    for (double v : net.gw[l]) grads[o++] = v;
+    for (double v : net.gb[l]) grads[o++] = v;
+  }
+  return loss;
+}
+
+// Loss and gradients of the warm-start network (flat layout as pdt_cnn_get_grads); returns the loss.
+double orc_cnn_grad(int B, int H, int W, const float* params, const float* u0, const float* ut, const float* vt,
+                    double* grads, double* out8) {
+  g_cnn_round = true;
+  CnnOracle net(B, H, W, params);
+  const double loss = net.run(u0, ut, vt, out8);
+  size_t o = 0;
+  for (int l = 0; l < CnnOracle::L; ++l) {
+    for (double v : net.gw[l]) grads[o++] = v;
+    for (double v : net.gb[l]) grads[o++] = v;
+  }
+  return loss;
+}
 
 }  // extern "C"

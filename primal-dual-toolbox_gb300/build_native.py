@@ -16,7 +16,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libpdt.so")
-SOURCES = ["pdt_capi.cu", "pdt_image.cu", "pdt_cartesian.cu", "pdt_radial.cu", "pdt_noalloc.cu"]
+SOURCES = ["pdt_capi.cu", "pdt_image.cu", "pdt_cartesian.cu", "pdt_radial.cu", "pdt_metrics.cu", "pdt_cnn.cu", "pdt_noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -63,7 +63,13 @@ void OpImpl::add_constant(pdt_dtype dtype, const Dims& size, const void* data, b
     }
   }
   constants_.push_back(std::move(c));
+  gen_ = next_generation();
   invalidate();
+}
+
+uint64_t OpImpl::next_generation() {
+  static std::atomic<uint64_t> g_gen{0};
+  return ++g_gen;
 }
 
 Constant& OpImpl::constant(unsigned idx, pdt_dtype dtype, int ndim) {
@@ -254,6 +260,62 @@ class OptImpl {
   void check_ready() const {
     if (with_op() && !op_) throw Error(PDT_ERR_STATE, "No operator is set!");
     if (!has_f_) throw Error(PDT_ERR_STATE, "No noisy data is set!");
+  }
+
+  // setInput0 extended with the second TGV primal: u = ubar = u0, v = vbar = v0 (two planes vx, vy),
+  // p = q = 0.
+  void set_input0_uv(const void* u0, const void* v0, const Dims& size, bool is_device, cudaStream_t st) {
+    set_input0(u0, size, is_device, st);
+    if (v0) {
+      const size_t plane = plane_bytes();
+      copy_in(field(F_VX, 0), v0, plane, is_device, st);
+      copy_in(field(F_VY, 0), static_cast<const char*>(v0) + plane, plane, is_device, st);
+      PDT_CUDA_CHECK(cudaMemcpyAsync(field(F_VBX, 0), field(F_VX, 0), plane, cudaMemcpyDeviceToDevice, st));
+      PDT_CUDA_CHECK(cudaMemcpyAsync(field(F_VBY, 0), field(F_VY, 0), plane, cudaMemcpyDeviceToDevice, st));
+    }
+  }
+
+  void get_field(int f, void* dst, bool is_device, cudaStream_t st) {
+    if (!has_state_) throw Error(PDT_ERR_STATE, "There is no result yet!");
+    if (f < 0 || f >= F_COUNT) throw Error(PDT_ERR_INVALID_ARGUMENT, "unknown field");
+    PDT_CUDA_CHECK(cudaMemcpyAsync(dst, field(f, parity_), plane_bytes(),
+                                   is_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, st));
+    if (!is_device) PDT_CUDA_CHECK(cudaStreamSynchronize(st));
+  }
+
+  // Energy of the current primal state in FP64: out = {total, data term, first-order term, second-order term}.
+  // TGV-MRI uses the final alpha of its continuation (alpha * reduction).
+  void energy(cudaStream_t st, double out[4]) {
+    check_ready();
+    if (!has_state_) throw Error(PDT_ERR_STATE, "There is no result yet!");
+    double a0 = params_.alpha0, a1 = params_.alpha1;
+    if (kind_ == PDT_OPT_TGV_MRI) {
+      a0 *= params_.reduction;
+      a1 *= params_.reduction;
+    }
+    const bool has_v = tgv();
+    double reg[2];
+    reduce_regularizer(cplx_, field(F_U, parity_), has_v ? field(F_VX, parity_) : nullptr,
+                       has_v ? field(F_VY, parity_) : nullptr, W_, H_, reg, st);
+    double data;
+    if (with_op()) {
+      DevBuf ku;
+      ku.ensure(std::max<size_t>(numel_of(fsize_) * sizeof(float2), 1));
+      op_->forward(static_cast<const float2*>(field(F_U, parity_)), usize_, ku.as<float2>(), fsize_, st);
+      data = 0.5 * reduce_dist2(true, ku.p, f_.p, numel_of(fsize_), st);
+      if (kind_ == PDT_OPT_TV_OP) data *= params_.lambda;
+    } else {
+      data = 0.5 * params_.lambda * reduce_dist2(cplx_, field(F_U, parity_), f_.p, (size_t)W_ * H_, st);
+    }
+    out[1] = data;
+    if (has_v) {
+      out[2] = a1 * reg[0];
+      out[3] = a0 * reg[1];
+    } else {
+      out[2] = (kind_ == PDT_OPT_TV_OP || kind_ == PDT_OPT_TV) ? reg[0] : a1 * reg[0];
+      out[3] = 0;
+    }
+    out[0] = out[1] + out[2] + out[3];
   }
 
   // A solve split in three: plan() enqueues the set-up on `st` and returns the per-iteration body,
@@ -506,17 +568,23 @@ class OptImpl {
             std::cout << "iter=" << k << " lambda=" << lambda << std::endl;
         }
     }
-    alpha_.ensure(std::max<size_t>(tab.size() * sizeof(float), 16) + 64);
-    int* iter = reinterpret_cast<int*>(alpha_.as<char>() + alpha_.bytes - 64);
+    // device layout: a 64-byte header {iteration counter, table length n} at a fixed offset, then the
+    // table. Graph kernels keep the header's address, so it must not move when n changes.
+    alpha_.ensure(kAlphaHeader + tab.size() * sizeof(float));
+    int* iter = alpha_.as<int>();
     if (alpha_host_ != tab) {
-      PDT_CUDA_CHECK(cudaMemcpyAsync(alpha_.p, tab.data(), tab.size() * sizeof(float), cudaMemcpyHostToDevice, st));
+      std::vector<char> img(alpha_.bytes, 0);
+      const int hdr[2] = {-1, n};
+      std::memcpy(img.data(), hdr, sizeof(hdr));
+      std::memcpy(img.data() + kAlphaHeader, tab.data(), tab.size() * sizeof(float));
+      PDT_CUDA_CHECK(cudaMemcpyAsync(alpha_.p, img.data(), img.size(), cudaMemcpyHostToDevice, st));
       PDT_CUDA_CHECK(cudaStreamSynchronize(st));
       alpha_host_ = tab;
     }
     PDT_CUDA_CHECK(cudaMemsetAsync(iter, 0xFF, sizeof(int), st));  // -1: the first round ticks it to 0
     const bool is_tgv = kind_ != PDT_OPT_TV_OP;
     const int p0 = parity_;
-    const float* atab = alpha_.as<float>();
+    const float* atab = reinterpret_cast<const float*>(alpha_.as<char>() + kAlphaHeader);
     float2* khr = khr_.as<float2>();
     Plan pl;
     pl.n = n;
@@ -530,12 +598,17 @@ class OptImpl {
       if (prof_) prof_->mark(is_tgv ? "mri_image_step_tgv" : "mri_image_step_tv", s);
     };
     pl.key = graph_key({(uintptr_t)img_.p, (uintptr_t)r_.p, (uintptr_t)fc_.p, (uintptr_t)khr_.p,
-                        (uintptr_t)alpha_.p, (uintptr_t)op_.get(), (uintptr_t)W_, (uintptr_t)H_, (uintptr_t)G,
-                        (uintptr_t)p0, (uintptr_t)is_tgv, fbits(lambda), fbits(tau), (uintptr_t)version_});
+                        (uintptr_t)alpha_.p, (uintptr_t)alpha_.bytes, (uintptr_t)op_.get(),
+                        (uintptr_t)op_->generation(), (uintptr_t)W_, (uintptr_t)H_, (uintptr_t)G, (uintptr_t)p0,
+                        (uintptr_t)is_tgv, fbits(lambda), fbits(tau), (uintptr_t)version_});
     return pl;
   }
 
   void ensure_fc(SolverHooks* hk, cudaStream_t st) {
+    if (op_gen_ != op_->generation()) {  // new constants: the compact layout may have changed
+      op_gen_ = op_->generation();
+      fc_valid_ = false;
+    }
     if (fc_valid_) return;
     const size_t nk = hk->compact_elems();
     fc_.ensure(std::max<size_t>(nk, 1) * sizeof(float2));
@@ -580,6 +653,7 @@ class OptImpl {
  private:
 
   static constexpr int kGraphIters = 20;
+  static constexpr size_t kAlphaHeader = 64;
 
   pdt_opt_kind kind_;
   bool cplx_;
@@ -594,6 +668,7 @@ class OptImpl {
   DevBuf img_, r_, fc_, khr_, alpha_;
   std::vector<float> alpha_host_;
   bool r_reset_ = true, fc_valid_ = false;
+  uint64_t op_gen_ = 0;
   uint64_t version_ = 1;
   IterGraph graph_;
   PhaseMarker* prof_ = nullptr;
@@ -892,6 +967,18 @@ pdt_status pdt_op_describe(pdt_op* op, char* buf, size_t len) {
   });
 }
 
+pdt_status pdt_op_tuning(pdt_op* op, char* buf, size_t len) {
+  return guarded([&] {
+    need(op, "operator");
+    need(buf, "buf");
+    const std::string s = op->impl->tuning();
+    if (len == 0) return;
+    const size_t n = std::min(len - 1, s.size());
+    std::memcpy(buf, s.data(), n);
+    buf[n] = 0;
+  });
+}
+
 pdt_status pdt_op_adjointness(pdt_op* op, uint64_t seed, double out[4]) {
   return guarded([&] {
     need(op, "operator");
@@ -1024,6 +1111,78 @@ pdt_status pdt_opt_get_result(pdt_opt* opt, void* dst, int is_device, void* stre
     cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : opt->impl->own_stream();
     opt->impl->get_result(dst, is_device != 0, st);
     if (!stream) PDT_CUDA_CHECK(cudaStreamSynchronize(st));
+  });
+}
+
+pdt_status pdt_opt_set_input0_uv(pdt_opt* opt, const void* u0, const void* v0, int ndim, const int64_t* size,
+                                 int is_device, void* stream) {
+  return guarded([&] {
+    need(opt, "optimizer");
+    const Dims d = dims_in(ndim, size);
+    if (numel_of(d)) need(u0, "input");
+    cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : opt->impl->own_stream();
+    opt->impl->set_input0_uv(u0, v0, d, is_device != 0, st);
+    if (!stream) PDT_CUDA_CHECK(cudaStreamSynchronize(st));
+  });
+}
+
+pdt_status pdt_opt_get_field(pdt_opt* opt, int field, void* dst, int is_device, void* stream) {
+  return guarded([&] {
+    need(opt, "optimizer");
+    need(dst, "dst");
+    opt->impl->result_size();
+    cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : opt->impl->own_stream();
+    opt->impl->get_field(field, dst, is_device != 0, st);
+    if (!stream) PDT_CUDA_CHECK(cudaStreamSynchronize(st));
+  });
+}
+
+pdt_status pdt_opt_energy(pdt_opt* opt, void* stream, double out[4]) {
+  return guarded([&] {
+    need(opt, "optimizer");
+    need(out, "out");
+    opt->impl->check_ready();
+    opt->impl->result_size();
+    cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : opt->impl->own_stream();
+    opt->impl->energy(st, out);
+  });
+}
+
+pdt_status pdt_op_norm(pdt_op* op, int iters, uint64_t seed, double* out) {
+  return guarded([&] {
+    need(op, "operator");
+    need(out, "out");
+    if (iters < 1) throw Error(PDT_ERR_INVALID_ARGUMENT, "iters must be >= 1");
+    OpImpl& o = *op->impl;
+    const Dims isz = o.natural_input_size();
+    const Dims osz = o.output_size(isz);
+    const size_t ni = numel_of(isz), no = numel_of(osz);
+    std::mt19937_64 gen(seed);
+    std::normal_distribution<float> dis(0.f, 1.f);
+    std::vector<float2> x0(ni);
+    for (auto& v : x0) v = make_float2(dis(gen), dis(gen));
+    DevBuf x, y;
+    cudaStream_t st = 0;
+    dev_copy_of(x0.data(), ni * 8, x, st);
+    y.ensure(std::max<size_t>(no * 8, 1));
+    double lam = 0;
+    double nx = std::sqrt(reduce_dist2(true, x.p, nullptr, ni, st));
+    for (int k = 0; k < iters; ++k) {
+      launch_scale(x.as<float2>(), (float)(1.0 / nx), ni, st);  // |x| = 1
+      o.forward(x.as<float2>(), isz, y.as<float2>(), osz, st);
+      o.adjoint(y.as<float2>(), osz, x.as<float2>(), isz, st);  // x <- K^H K x
+      nx = std::sqrt(reduce_dist2(true, x.p, nullptr, ni, st));
+      lam = nx;  // Rayleigh growth of a unit vector
+    }
+    *out = std::sqrt(lam);
+  });
+}
+
+pdt_status pdt_dist2(pdt_dtype dtype, const void* a, const void* b, size_t n, void* stream, double* out) {
+  return guarded([&] {
+    need(a, "a");
+    need(out, "out");
+    *out = reduce_dist2(dtype == PDT_C64, a, b, n, static_cast<cudaStream_t>(stream));
   });
 }
 

@@ -16,18 +16,18 @@ namespace cg = cooperative_groups;
 namespace pdt {
 namespace {
 
-constexpr int kFastWarps = 8;  // sequences (warps) per block
+constexpr int kMaxWarps = 8;  // largest warps-per-block instance (one sequence per warp)
 
 // Phase 1 (fast): rows of ubar . sens_c -> FFT along W -> sampled columns t1[c][s][yi].
-template <int A, int B>
-__global__ void __launch_bounds__(32 * kFastWarps) fr_rows_fwd(CartDev d, const float2* __restrict__ ubar,
+template <int A, int B, int WPB>
+__global__ void __launch_bounds__(32 * WPB) fr_rows_fwd(CartDev d, const float2* __restrict__ ubar,
                                                                float2* __restrict__ t1, int* __restrict__ tick) {
   using TL = TwoLevel<A, B>;
   extern __shared__ float2 sm[];
   float2* tw = sm;
   float2* ex = tw + TL::n;
-  float2* stage = ex + kFastWarps * TL::xch;
-  int* fs2s = reinterpret_cast<int*>(stage + (size_t)d.ns * kFastWarps);
+  float2* stage = ex + WPB * TL::xch;
+  int* fs2s = reinterpret_cast<int*>(stage + (size_t)d.ns * WPB);
   if (tick && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) atomicAdd(tick, 1);
   for (int i = threadIdx.x; i < TL::n; i += blockDim.x) {
     tw[i] = d.twW[i];
@@ -35,7 +35,7 @@ __global__ void __launch_bounds__(32 * kFastWarps) fr_rows_fwd(CartDev d, const 
   }
   __syncthreads();
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int yi0 = blockIdx.x * kFastWarps, yi = yi0 + w, c = blockIdx.y;
+  const int yi0 = blockIdx.x * WPB, yi = yi0 + w, c = blockIdx.y;
   float2* myex = ex + w * TL::xch;
   const bool ok = yi < d.Hi;
   if (ok && lane < A) {
@@ -59,20 +59,20 @@ __global__ void __launch_bounds__(32 * kFastWarps) fr_rows_fwd(CartDev d, const 
 #pragma unroll
     for (int ka = 0; ka < A; ++ka) {
       const int s = fs2s[lane + B * ka];
-      if (s >= 0) stage[s * kFastWarps + w] = u[ka];
+      if (s >= 0) stage[s * WPB + w] = u[ka];
     }
   }
   __syncthreads();
-  const int nr = min(kFastWarps, d.Hi - yi0);
+  const int nr = min(WPB, d.Hi - yi0);
   for (int i = threadIdx.x; i < d.ns * nr; i += blockDim.x) {
     const int s = i / nr, r = i - s * nr;
-    t1[((size_t)c * d.ns + s) * d.Hi + yi0 + r] = stage[s * kFastWarps + r];
+    t1[((size_t)c * d.ns + s) * d.Hi + yi0 + r] = stage[s * WPB + r];
   }
 }
 
 // Phase 2 (fast): per sampled column, FFT along H -> mask -> (prox) -> mask -> IFFT along H.
-template <int A, int B>
-__global__ void __launch_bounds__(32 * kFastWarps) fr_cols(CartDev d, int mode, const float2* t_in, float2* t_out,
+template <int A, int B, int WPB>
+__global__ void __launch_bounds__(32 * WPB) fr_cols(CartDev d, int mode, const float2* t_in, float2* t_out,
                                                            float2* __restrict__ r, const float2* __restrict__ fc,
                                                            const float2* __restrict__ kin, float2* __restrict__ kout,
                                                            float sigma, float lambda) {
@@ -83,7 +83,7 @@ __global__ void __launch_bounds__(32 * kFastWarps) fr_cols(CartDev d, int mode, 
   for (int i = threadIdx.x; i < TL::n; i += blockDim.x) tw[i] = d.twH[i];
   __syncthreads();
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int s = blockIdx.x * kFastWarps + w, c = blockIdx.y;
+  const int s = blockIdx.x * WPB + w, c = blockIdx.y;
   const bool ok = s < d.ns;
   float2* myex = ex + w * TL::xch;
   constexpr int Hf = TL::n;
@@ -172,28 +172,29 @@ __global__ void __launch_bounds__(32 * kFastWarps) fr_cols(CartDev d, int mode, 
 // the coil sum. A cluster of G blocks shares the row block, each block taking one coil group and
 // accumulating in its shared memory; the blocks then reduce the G partial rows through distributed
 // shared memory in rank order (deterministic) and write one K^H r plane. With G = 1 it is a plain launch.
-template <int A, int B>
-__global__ void __launch_bounds__(32 * kFastWarps) fr_rows_adj(CartDev d, const float2* __restrict__ t2,
-                                                               float2* __restrict__ out) {
+template <int A, int B, int WPB>
+__global__ void __launch_bounds__(32 * WPB) fr_rows_adj(CartDev d, const float2* __restrict__ t2,
+                                                        float2* __restrict__ out, int use_cluster, int G,
+                                                        long long gstride) {
   using TL = TwoLevel<A, B>;
   constexpr int W = TL::n;
   extern __shared__ float2 sm[];
   float2* tw = sm;
   float2* ex = tw + W;
-  float2* stage = ex + kFastWarps * TL::xch;
-  float2* red = stage + (size_t)d.ns * kFastWarps;  // kFastWarps rows x W: this block's coil-group sum
-  int* as2s = reinterpret_cast<int*>(red + (size_t)kFastWarps * W);
-  cg::cluster_group cluster = cg::this_cluster();
-  const int G = (int)cluster.num_blocks();
-  const int g = (int)cluster.block_rank();
+  float2* stage = ex + WPB * TL::xch;
+  float2* red = stage + (size_t)d.ns * WPB;  // WPB rows x W: this block's coil-group sum
+  int* as2s = reinterpret_cast<int*>(red + (size_t)WPB * W);
+  // with use_cluster, the G coil groups of a row block form a cluster (grid.y = G); otherwise each
+  // block writes its group's partial sum to out + g * gstride
+  const int g = blockIdx.y;
   for (int i = threadIdx.x; i < W; i += blockDim.x) {
     tw[i] = d.twW[i];
     as2s[i] = d.slot2s[i];
   }
-  for (int i = threadIdx.x; i < kFastWarps * W; i += blockDim.x) red[i] = c2(0.f, 0.f);
+  for (int i = threadIdx.x; i < WPB * W; i += blockDim.x) red[i] = c2(0.f, 0.f);
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int yi0 = blockIdx.x * kFastWarps, yi = yi0 + w;
-  const int nr = min(kFastWarps, d.Hi - yi0);
+  const int yi0 = blockIdx.x * WPB, yi = yi0 + w;
+  const int nr = min(WPB, d.Hi - yi0);
   const int c_begin = (int)((long long)g * d.C / G), c_end = (int)((long long)(g + 1) * d.C / G);
   float2* myex = ex + w * TL::xch;
   const bool ok = w < nr;
@@ -220,14 +221,14 @@ __global__ void __launch_bounds__(32 * kFastWarps) fr_rows_adj(CartDev d, const 
         const int i = threadIdx.x + q * (int)blockDim.x;
         if (i < d.ns * nr) {
           const int s = i / nr, rr = i - s * nr;
-          stage[s * kFastWarps + rr] = pf[q];
+          stage[s * WPB + rr] = pf[q];
         }
       }
       if (c + 1 < c_end) fetch(c + 1);
     } else {
       for (int i = threadIdx.x; i < d.ns * nr; i += blockDim.x) {
         const int s = i / nr, rr = i - s * nr;
-        stage[s * kFastWarps + rr] = t2[((size_t)c * d.ns + s) * d.Hi + yi0 + rr];
+        stage[s * WPB + rr] = t2[((size_t)c * d.ns + s) * d.Hi + yi0 + rr];
       }
     }
     __syncthreads();
@@ -236,7 +237,7 @@ __global__ void __launch_bounds__(32 * kFastWarps) fr_rows_adj(CartDev d, const 
 #pragma unroll
       for (int ka = 0; ka < A; ++ka) {
         const int s = as2s[lane + B * ka];
-        u[ka] = s >= 0 ? stage[s * kFastWarps + w] : c2(0.f, 0.f);
+        u[ka] = s >= 0 ? stage[s * WPB + w] : c2(0.f, 0.f);
       }
       TL::inv_step1(u, lane, myex, tw);
     }
@@ -255,37 +256,53 @@ __global__ void __launch_bounds__(32 * kFastWarps) fr_rows_adj(CartDev d, const 
     }
     __syncwarp();
   }
-  cluster.sync();  // every block's coil-group rows complete
-  const int total = nr * W;
-  const int beg = (int)((long long)g * total / G), end = (int)((long long)(g + 1) * total / G);
-  for (int i = beg + threadIdx.x; i < end; i += blockDim.x) {
-    float2 acc = c2(0.f, 0.f);
-    for (int q = 0; q < G; ++q) acc += cluster.map_shared_rank(red, q)[i];
-    out[(size_t)(yi0 + i / W) * W + i % W] = acc;
+  if (use_cluster) {
+    cg::cluster_group cluster = cg::this_cluster();
+    cluster.sync();  // every block's coil-group rows complete
+    const int total = nr * W;
+    const int beg = (int)((long long)g * total / G), end = (int)((long long)(g + 1) * total / G);
+    for (int i = beg + threadIdx.x; i < end; i += blockDim.x) {
+      float2 acc = c2(0.f, 0.f);
+      for (int q = 0; q < G; ++q) acc += cluster.map_shared_rank(red, q)[i];  // rank order: deterministic
+      out[(size_t)(yi0 + i / W) * W + i % W] = acc;
+    }
+    cluster.sync();  // keep this block's shared memory alive until the other blocks have read it
+  } else {
+    __syncthreads();
+    float2* og = out + (size_t)g * gstride;
+    for (int i = threadIdx.x; i < nr * W; i += blockDim.x) og[(size_t)(yi0 + i / W) * W + i % W] = red[i];
   }
-  cluster.sync();  // keep this block's shared memory alive until the other blocks have read it
 }
 
 typedef void (*FrRowsFwdFn)(CartDev, const float2*, float2*, int*);
 typedef void (*FrColsFn)(CartDev, int, const float2*, float2*, float2*, const float2*, const float2*, float2*, float,
                          float);
-typedef void (*FrRowsAdjFn)(CartDev, const float2*, float2*);
+typedef void (*FrRowsAdjFn)(CartDev, const float2*, float2*, int, int, long long);
 
+constexpr int kWpbChoices[3] = {2, 4, 8};
+
+// Kernels of one compiled length, one instance per warps-per-block choice.
 struct FastRowKernels {
-  FrRowsFwdFn fwd = nullptr;
-  FrRowsAdjFn adj = nullptr;
+  FrRowsFwdFn fwd[3] = {nullptr, nullptr, nullptr};
+  FrRowsAdjFn adj[3] = {nullptr, nullptr, nullptr};
   int A = 0, B = 0;
+  bool ok() const { return fwd[0] != nullptr; }
 };
 struct FastColKernels {
-  FrColsFn cols = nullptr;
+  FrColsFn cols[3] = {nullptr, nullptr, nullptr};
   int A = 0, B = 0;
+  bool ok() const { return cols[0] != nullptr; }
 };
 
 template <int A, int B>
 FastRowKernels row_kernels() {
   FastRowKernels k;
-  k.fwd = fr_rows_fwd<A, B>;
-  k.adj = fr_rows_adj<A, B>;
+  k.fwd[0] = fr_rows_fwd<A, B, 2>;
+  k.fwd[1] = fr_rows_fwd<A, B, 4>;
+  k.fwd[2] = fr_rows_fwd<A, B, 8>;
+  k.adj[0] = fr_rows_adj<A, B, 2>;
+  k.adj[1] = fr_rows_adj<A, B, 4>;
+  k.adj[2] = fr_rows_adj<A, B, 8>;
   k.A = A;
   k.B = B;
   return k;
@@ -293,7 +310,9 @@ FastRowKernels row_kernels() {
 template <int A, int B>
 FastColKernels col_kernels() {
   FastColKernels k;
-  k.cols = fr_cols<A, B>;
+  k.cols[0] = fr_cols<A, B, 2>;
+  k.cols[1] = fr_cols<A, B, 4>;
+  k.cols[2] = fr_cols<A, B, 8>;
   k.A = A;
   k.B = B;
   return k;
@@ -318,16 +337,16 @@ FastColKernels find_col_kernels(int n) {
   return FastColKernels();
 }
 
-size_t fast_rows_smem(const CartDev& d, int A, int B) {
+size_t fast_rows_smem(const CartDev& d, int A, int B, int wpb) {
   const size_t n = (size_t)A * B, xch = (size_t)B * (A + 1);
-  return sizeof(float2) * (n + kFastWarps * xch + (size_t)d.ns * kFastWarps) + sizeof(int) * n;
+  return sizeof(float2) * (n + wpb * xch + (size_t)d.ns * wpb) + sizeof(int) * n;
 }
-size_t fast_rows_adj_smem(const CartDev& d, int A, int B) {
-  return fast_rows_smem(d, A, B) + sizeof(float2) * (size_t)kFastWarps * A * B;
+size_t fast_rows_adj_smem(const CartDev& d, int A, int B, int wpb) {
+  return fast_rows_smem(d, A, B, wpb) + sizeof(float2) * (size_t)wpb * A * B;
 }
-size_t fast_cols_smem(int A, int B) {
+size_t fast_cols_smem(int A, int B, int wpb) {
   const size_t n = (size_t)A * B, xch = (size_t)B * (A + 1);
-  return sizeof(float2) * (n + kFastWarps * xch);
+  return sizeof(float2) * (n + wpb * xch);
 }
 
 }  // namespace

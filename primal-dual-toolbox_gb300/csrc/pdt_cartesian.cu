@@ -18,8 +18,12 @@
 // The k-space dual r and the data f live in the compact layout [c][s][Hf] (sampled columns only);
 // the entries of unsampled columns never reach u in the reference either (the mask zeroes them).
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstring>
+#include <functional>
+#include <map>
+#include <mutex>
 #include <sstream>
 
 #include "pdt_device.cuh"
@@ -258,6 +262,22 @@ class CartesianOp : public OpImpl, public SolverHooks {
     return constant(0, PDT_C64, 3).size;
   }
   SolverHooks* hooks() override { return this; }
+  std::string tuning() override {
+    prepare();
+    std::ostringstream os;
+    os << "W=" << dev_.W << " H=" << dev_.Hf << " C=" << dev_.C << " sampled_columns=" << dev_.ns;
+    if (frow_.ok())
+      os << " rows_fwd=register_fft(" << frow_.A << "x" << frow_.B << ",warps=" << kWpbChoices[tune_.wf] << ")"
+         << " rows_adj=register_fft(warps=" << kWpbChoices[tune_.wa] << ",coil_groups=" << G_
+         << (tune_.cluster ? ",cluster" : ",partials") << ")";
+    else
+      os << " rows=stockham(coil_groups=" << G_ << ")";
+    if (fcol_.ok())
+      os << " cols=register_fft(" << fcol_.A << "x" << fcol_.B << ",warps=" << kWpbChoices[tune_.wc] << ")";
+    else
+      os << " cols=stockham";
+    return os.str();
+  }
   Dims natural_input_size() override {
     if (kind_ == PDT_OP_SAMPLING) return constant(0, PDT_F32, 2).size;
     const Dims& m = constant(1, PDT_F32, 2).size;
@@ -280,7 +300,7 @@ class CartesianOp : public OpImpl, public SolverHooks {
   }
   int groups() override {
     prepare();
-    return frow_.adj ? 1 : G_;  // the register-FFT path reduces the coil groups inside a cluster
+    return (frow_.ok() && tune_.cluster) ? 1 : G_;  // a cluster reduces its coil groups on chip
   }
   long long group_stride() override { return (long long)dev_.Hi * dev_.W; }
   void round(const float2* ubar, float2* r, const float2* fc, float sigma, float lambda, float2* khr, int* tick,
@@ -296,7 +316,7 @@ class CartesianOp : public OpImpl, public SolverHooks {
     if (mk) mk->mark("cart_rows_fwd", st);
     launch_cols(COL_SOLVE, t, t, r, fc, nullptr, nullptr, sigma, lambda, st);
     if (mk) mk->mark("cart_cols_prox", st);
-    launch_rows_adj(t, khr, frow_.adj ? G_ : G_, st);
+    launch_rows_adj(t, khr, G_, st);
     if (mk) mk->mark("cart_rows_adj", st);
   }
   void adjoint_compact(const float2* fc, float2* img, cudaStream_t st) override {
@@ -351,13 +371,17 @@ class CartesianOp : public OpImpl, public SolverHooks {
   void invalidate() override { prepared_ = false; }
 
  private:
-  // coil groups per row block on the register-FFT path: a portable cluster of at most 8 blocks
-  static int fast_cluster(int G) { return std::max(1, std::min(G, 8)); }
+  // Launch configuration of the register-FFT kernels, chosen by the autotuner in prepare().
+  struct Tune {
+    int wf = 2, wc = 2, wa = 2;  // warps-per-block index (kWpbChoices) of rows_fwd, cols, rows_adj
+    bool cluster = false;        // coil groups of a row block reduced in a cluster (else partial images)
+  };
 
   void launch_rows_fwd(const float2* ubar, float2* t1, int* tick, cudaStream_t st) {
-    if (frow_.fwd) {
-      dim3 grid((dev_.Hi + kFastWarps - 1) / kFastWarps, dev_.C);
-      frow_.fwd<<<grid, 32 * kFastWarps, fast_rows_smem(dev_, frow_.A, frow_.B), st>>>(dev_, ubar, t1, tick);
+    if (frow_.ok()) {
+      const int wpb = kWpbChoices[tune_.wf];
+      dim3 grid((dev_.Hi + wpb - 1) / wpb, dev_.C);
+      frow_.fwd[tune_.wf]<<<grid, 32 * wpb, fast_rows_smem(dev_, frow_.A, frow_.B, wpb), st>>>(dev_, ubar, t1, tick);
       PDT_LAUNCH_CHECK();
       count_launch();
       return;
@@ -369,10 +393,11 @@ class CartesianOp : public OpImpl, public SolverHooks {
   }
   void launch_cols(int mode, const float2* tin, float2* tout, float2* r, const float2* fc, const float2* kin,
                    float2* kout, float sigma, float lambda, cudaStream_t st) {
-    if (fcol_.cols) {
-      dim3 grid((dev_.ns + kFastWarps - 1) / kFastWarps, dev_.C);
-      fcol_.cols<<<grid, 32 * kFastWarps, fast_cols_smem(fcol_.A, fcol_.B), st>>>(dev_, mode, tin, tout, r, fc, kin,
-                                                                                  kout, sigma, lambda);
+    if (fcol_.ok()) {
+      const int wpb = kWpbChoices[tune_.wc];
+      dim3 grid((dev_.ns + wpb - 1) / wpb, dev_.C);
+      fcol_.cols[tune_.wc]<<<grid, 32 * wpb, fast_cols_smem(fcol_.A, fcol_.B, wpb), st>>>(dev_, mode, tin, tout, r, fc,
+                                                                                        kin, kout, sigma, lambda);
       PDT_LAUNCH_CHECK();
       count_launch();
       return;
@@ -382,23 +407,25 @@ class CartesianOp : public OpImpl, public SolverHooks {
     PDT_LAUNCH_CHECK();
     count_launch();
   }
+  // K^H: G coil-group partial images (or, with a cluster, one reduced image) into out.
   void launch_rows_adj(const float2* t2, float2* out, int G, cudaStream_t st) {
-    if (frow_.adj) {
-      // the coil groups of one row block form a thread-block cluster and reduce in shared memory
-      const int cl = fast_cluster(G);
+    if (frow_.ok()) {
+      const int wpb = kWpbChoices[tune_.wa];
+      const bool cl = tune_.cluster && G > 1;
       cudaLaunchConfig_t cfg = {};
-      cfg.gridDim = dim3((dev_.Hi + kFastWarps - 1) / kFastWarps, cl);
-      cfg.blockDim = dim3(32 * kFastWarps);
-      cfg.dynamicSmemBytes = fast_rows_adj_smem(dev_, frow_.A, frow_.B);
+      cfg.gridDim = dim3((dev_.Hi + wpb - 1) / wpb, G);
+      cfg.blockDim = dim3(32 * wpb);
+      cfg.dynamicSmemBytes = fast_rows_adj_smem(dev_, frow_.A, frow_.B, wpb);
       cfg.stream = st;
       cudaLaunchAttribute attr[1];
       attr[0].id = cudaLaunchAttributeClusterDimension;
       attr[0].val.clusterDim.x = 1;
-      attr[0].val.clusterDim.y = cl;
+      attr[0].val.clusterDim.y = cl ? G : 1;
       attr[0].val.clusterDim.z = 1;
       cfg.attrs = attr;
       cfg.numAttrs = 1;
-      PDT_CUDA_CHECK(cudaLaunchKernelEx(&cfg, frow_.adj, dev_, t2, out));
+      PDT_CUDA_CHECK(cudaLaunchKernelEx(&cfg, frow_.adj[tune_.wa], dev_, t2, out, cl ? 1 : 0, G,
+                                        (long long)dev_.Hi * dev_.W));
       count_launch();
       return;
     }
@@ -502,24 +529,118 @@ class CartesianOp : public OpImpl, public SolverHooks {
     // register-FFT kernels where the length has a compiled split
     frow_ = find_row_kernels(W);
     fcol_ = find_col_kernels(Hf);
-    if (frow_.fwd && fast_rows_smem(d, frow_.A, frow_.B) > (size_t)g_max_smem) frow_ = FastRowKernels();
-    if (fcol_.cols && fast_cols_smem(fcol_.A, fcol_.B) > (size_t)g_max_smem) fcol_ = FastColKernels();
-    if (frow_.fwd && fast_rows_adj_smem(d, frow_.A, frow_.B) > (size_t)g_max_smem) frow_ = FastRowKernels();
-    if (frow_.fwd) {
-      PDT_CUDA_CHECK(cudaFuncSetAttribute(frow_.fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, g_max_smem));
-      PDT_CUDA_CHECK(cudaFuncSetAttribute(frow_.adj, cudaFuncAttributeMaxDynamicSharedMemorySize, g_max_smem));
-      PDT_CUDA_CHECK(cudaFuncSetAttribute(frow_.adj, cudaFuncAttributeNonPortableClusterSizeAllowed, 0));
+    if (frow_.ok() && fast_rows_adj_smem(d, frow_.A, frow_.B, 8) > (size_t)g_max_smem) frow_ = FastRowKernels();
+    if (fcol_.ok() && fast_cols_smem(fcol_.A, fcol_.B, 8) > (size_t)g_max_smem) fcol_ = FastColKernels();
+    for (int w = 0; w < 3; ++w) {
+      if (frow_.ok()) {
+        PDT_CUDA_CHECK(cudaFuncSetAttribute(frow_.fwd[w], cudaFuncAttributeMaxDynamicSharedMemorySize, g_max_smem));
+        PDT_CUDA_CHECK(cudaFuncSetAttribute(frow_.adj[w], cudaFuncAttributeMaxDynamicSharedMemorySize, g_max_smem));
+      }
+      if (fcol_.ok())
+        PDT_CUDA_CHECK(cudaFuncSetAttribute(fcol_.cols[w], cudaFuncAttributeMaxDynamicSharedMemorySize, g_max_smem));
     }
-    if (fcol_.cols)
-      PDT_CUDA_CHECK(cudaFuncSetAttribute(fcol_.cols, cudaFuncAttributeMaxDynamicSharedMemorySize, g_max_smem));
-    // coil groups for the adjoint row phase: enough blocks for two waves
-    const int row_blocks = frow_.fwd ? (d.Hi + kFastWarps - 1) / kFastWarps : (d.Hi + d.RB - 1) / d.RB;
+    const int row_blocks = (d.Hi + d.RB - 1) / d.RB;
     G_ = std::max(1, std::min(C, (2 * g_num_sms + row_blocks - 1) / row_blocks));
+    dev_ = d;
+    autotune();
     dev_ = d;
     prepared_ = true;
   }
 
+  // Times the candidate launch shapes of the register-FFT kernels on scratch buffers (CUDA events, a
+  // few launches each) and keeps the fastest: warps per block of each kernel, and for the adjoint rows
+  // the number of coil groups and cluster reduction versus partial images. Results are cached per
+  // (W, H, coils, sampled columns).
+  void autotune() {
+    if (!frow_.ok() && !fcol_.ok()) return;
+    static std::mutex g_tune_mu;
+    static std::map<std::array<int, 6>, std::pair<Tune, int>> g_tune_cache;
+    const std::array<int, 6> key = {dev_.W, dev_.Hf, dev_.Hi, dev_.C, dev_.ns, dev_.sens ? 1 : 0};
+    {
+      std::lock_guard<std::mutex> lock(g_tune_mu);
+      auto it = g_tune_cache.find(key);
+      if (it != g_tune_cache.end()) {
+        tune_ = it->second.first;
+        G_ = it->second.second;
+        return;
+      }
+    }
+    if (dev_.ns == 0) return;
+    const size_t nimg = (size_t)dev_.Hi * dev_.W, nk = (size_t)dev_.C * dev_.ns * dev_.Hf;
+    DevBuf ub, rr, ff, kh;
+    ub.ensure(nimg * sizeof(float2));
+    rr.ensure(nk * sizeof(float2));
+    ff.ensure(nk * sizeof(float2));
+    kh.ensure((size_t)dev_.C * nimg * sizeof(float2));
+    PDT_CUDA_CHECK(cudaMemset(ub.p, 0, ub.bytes));
+    PDT_CUDA_CHECK(cudaMemset(rr.p, 0, rr.bytes));
+    PDT_CUDA_CHECK(cudaMemset(ff.p, 0, ff.bytes));
+    float2* t = scratch_.as<float2>();
+    cudaStream_t st = 0;
+    cudaEvent_t e0, e1;
+    PDT_CUDA_CHECK(cudaEventCreate(&e0));
+    PDT_CUDA_CHECK(cudaEventCreate(&e1));
+    // a candidate whose launch is rejected (e.g. a cluster shape the device cannot schedule) is skipped
+    auto time = [&](const std::function<void()>& fn) {
+      try {
+        fn();  // warm-up
+        PDT_CUDA_CHECK(cudaEventRecord(e0, st));
+        for (int i = 0; i < 5; ++i) fn();
+        PDT_CUDA_CHECK(cudaEventRecord(e1, st));
+        PDT_CUDA_CHECK(cudaEventSynchronize(e1));
+        float ms = 0;
+        PDT_CUDA_CHECK(cudaEventElapsedTime(&ms, e0, e1));
+        return ms;
+      } catch (const Error&) {
+        cudaGetLastError();
+        PDT_CUDA_CHECK(cudaDeviceSynchronize());  // a sticky error surfaces here and fails the operator
+        return 1e30f;
+      }
+    };
+    const uint64_t launches0 = g_launches.load();
+    Tune best = tune_;
+    if (frow_.ok()) {
+      float bt = 1e30f;
+      for (int w = 0; w < 3; ++w) {
+        tune_.wf = w;
+        const float ms = time([&] { launch_rows_fwd(ub.as<float2>(), t, nullptr, st); });
+        if (ms < bt) bt = ms, best.wf = w;
+      }
+      tune_.wf = best.wf;
+      float ba = 1e30f;
+      int bestG = G_;
+      const int gmax = std::min(dev_.C, 16);
+      for (int w = 0; w < 3; ++w)
+        for (int cl = 0; cl < 2; ++cl)
+          for (int g : {1, 2, 3, 4, 5, 6, 8, 10, 12, 16}) {
+            if (g > gmax || (cl && (g < 2 || g > 8))) continue;
+            tune_.wa = w;
+            tune_.cluster = cl != 0;
+            const float ms = time([&] { launch_rows_adj(t, kh.as<float2>(), g, st); });
+            if (ms < ba) ba = ms, best.wa = w, best.cluster = cl != 0, bestG = g;
+          }
+      G_ = bestG;
+    }
+    if (fcol_.ok()) {
+      float bc = 1e30f;
+      for (int w = 0; w < 3; ++w) {
+        tune_.wc = w;
+        const float ms = time([&] {
+          launch_cols(COL_SOLVE, t, t, rr.as<float2>(), ff.as<float2>(), nullptr, nullptr, 0.125f, 1.f, st);
+        });
+        if (ms < bc) bc = ms, best.wc = w;
+      }
+    }
+    g_launches.fetch_sub(g_launches.load() - launches0);  // tuning launches are not solver work
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    tune_ = best;
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    g_tune_cache[key] = {tune_, G_};
+  }
+
   bool prepared_ = false;
+  Tune tune_;
   CartDev dev_{};
   FastRowKernels frow_;
   FastColKernels fcol_;

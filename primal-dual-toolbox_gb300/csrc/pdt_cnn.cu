@@ -1,0 +1,822 @@
+// pdt_cnn.cu -- the learned warm start: a small residual CNN with BF16 weights and activations and FP32
+// accumulation, trained and run by the engine's own kernels.
+//
+// Network (fully convolutional, 3 x 3 convolutions, zero padding, channel-last BF16 activations):
+//   x  = [Re u0, Im u0] / s                       (u0 = A^H f, s = max |u0|)
+//   h1 = relu(conv_in(x))                          2 -> 32
+//   h_{l+1} = h_l + relu(conv_l(h_l)), l = 1..6    32 -> 32
+//   o  = conv_out(h7)                              32 -> 8 (6 used)
+//   u  = u0 + s (o0 + i o1),  v = s (o2 + i o3, o4 + i o5)
+// Eight convolutions in all. The 32-channel convolutions run as implicit GEMMs on the tensor cores
+// (mma.sync m16n8k16, BF16 in, FP32 accumulate): pixels are the M dimension, output channels N, and
+// (tap, input channel) K. The data gradient is the same kernel with flipped taps and transposed channels;
+// the weight gradient is a second implicit GEMM with pixels as K, reduced over blocks in block order.
+#include <cuda_bf16.h>
+
+#include <cmath>
+#include <cstring>
+#include <random>
+#include <memory>
+#include <vector>
+
+#include "pdt_device.cuh"
+#include "pdt_internal.h"
+
+namespace pdt {
+namespace {
+
+typedef __nv_bfloat16 bf16;
+
+constexpr int CH = 32;    // hidden channels
+constexpr int TW = 16;    // pixel tile width (one mma M tile)
+constexpr int TH = 8;     // pixel tile height (one row per warp)
+constexpr int NTAP = 9;
+
+__device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
+  __nv_bfloat162 v = __floats2bfloat162_rn(a, b);
+  return *reinterpret_cast<uint32_t*>(&v);
+}
+
+__device__ __forceinline__ void mma16816(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};\n"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+enum Epi {
+  EPI_LINEAR = 0,    // out = z (BF16)
+  EPI_RELU = 1,      // zsave = z, out = relu(z)
+  EPI_RELU_RES = 2,  // zsave = z, out = in + relu(z)   (CIN == COUT)
+  EPI_F32 = 3        // out32 = z (FP32)
+};
+
+// 3 x 3 convolution as an implicit GEMM. in: [B][H][W][CIN] BF16; w: [9][COUT][CIN] BF16; bias: [COUT] FP32
+// (may be null). Each block computes a 16 x 8 pixel tile; warp w owns tile row w (16 pixels = one M tile).
+template <int CIN, int COUT, int EPI>
+__global__ void __launch_bounds__(32 * TH) conv3x3_mma(const bf16* __restrict__ in, const bf16* __restrict__ w,
+                                                       const float* __restrict__ bias, int H, int W,
+                                                       bf16* __restrict__ out, bf16* __restrict__ zsave,
+                                                       float* __restrict__ out32) {
+  static_assert(CIN % 16 == 0 && COUT % 8 == 0, "channel counts");
+  constexpr int PS = CIN + 4;       // smem pixel stride (bf16): spreads the fragment loads over all banks
+  constexpr int WS = CIN + 8;       // smem weight row stride (bf16)
+  __shared__ __align__(16) bf16 s_in[(TH + 2) * (TW + 2) * PS];
+  __shared__ __align__(16) bf16 s_w[NTAP * COUT * WS];
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int gid = lane >> 2, tig = lane & 3;
+  const int x0 = blockIdx.x * TW, y0 = blockIdx.y * TH, b = blockIdx.z;
+  const bf16* inb = in + (size_t)b * H * W * CIN;
+  // stage weights and the input tile with a one-pixel halo (zero outside the image), 4-byte granules
+  for (int i = tid; i < NTAP * COUT * (CIN / 2); i += blockDim.x) {
+    const int row = i / (CIN / 2), c2 = i - row * (CIN / 2);
+    reinterpret_cast<uint32_t*>(s_w + row * WS)[c2] = reinterpret_cast<const uint32_t*>(w + (size_t)row * CIN)[c2];
+  }
+  for (int i = tid; i < (TH + 2) * (TW + 2) * (CIN / 2); i += blockDim.x) {
+    const int pix = i / (CIN / 2), c2 = i - pix * (CIN / 2);
+    const int ty = pix / (TW + 2), tx = pix - ty * (TW + 2);
+    const int gy = y0 - 1 + ty, gx = x0 - 1 + tx;
+    uint32_t v = 0;
+    if (gy >= 0 && gy < H && gx >= 0 && gx < W)
+      v = reinterpret_cast<const uint32_t*>(inb + ((size_t)gy * W + gx) * CIN)[c2];
+    reinterpret_cast<uint32_t*>(s_in + pix * PS)[c2] = v;
+  }
+  __syncthreads();
+  float acc[COUT / 8][4];
+#pragma unroll
+  for (int n = 0; n < COUT / 8; ++n) acc[n][0] = acc[n][1] = acc[n][2] = acc[n][3] = 0.f;
+#pragma unroll
+  for (int tap = 0; tap < NTAP; ++tap) {
+    const int ky = tap / 3, kx = tap % 3;
+    const bf16* arow0 = s_in + ((warp + ky) * (TW + 2) + gid + kx) * PS;  // pixel gid of this warp's row
+    const bf16* arow1 = arow0 + 8 * PS;                                    // pixel gid + 8
+#pragma unroll
+    for (int kk = 0; kk < CIN / 16; ++kk) {
+      uint32_t a[4];
+      const int c = kk * 16 + tig * 2;
+      a[0] = *reinterpret_cast<const uint32_t*>(arow0 + c);
+      a[1] = *reinterpret_cast<const uint32_t*>(arow1 + c);
+      a[2] = *reinterpret_cast<const uint32_t*>(arow0 + c + 8);
+      a[3] = *reinterpret_cast<const uint32_t*>(arow1 + c + 8);
+#pragma unroll
+      for (int n = 0; n < COUT / 8; ++n) {
+        const bf16* brow = s_w + (tap * COUT + n * 8 + gid) * WS + c;
+        mma16816(acc[n], a, *reinterpret_cast<const uint32_t*>(brow), *reinterpret_cast<const uint32_t*>(brow + 8));
+      }
+    }
+  }
+  // epilogue: rows gid and gid + 8 of the M tile are pixels x0 + gid (+ 8) of image row y0 + warp
+  const int gy = y0 + warp;
+  if (gy >= H) return;
+#pragma unroll
+  for (int half = 0; half < 2; ++half) {
+    const int gx = x0 + gid + 8 * half;
+    if (gx >= W) continue;
+    const size_t pix = ((size_t)b * H + gy) * W + gx;
+#pragma unroll
+    for (int n = 0; n < COUT / 8; ++n) {
+      const int co = n * 8 + tig * 2;
+      float z0 = acc[n][2 * half], z1 = acc[n][2 * half + 1];
+      if (bias) {
+        z0 += bias[co];
+        z1 += bias[co + 1];
+      }
+      if constexpr (EPI == EPI_F32) {
+        out32[pix * COUT + co] = z0;
+        out32[pix * COUT + co + 1] = z1;
+      } else if constexpr (EPI == EPI_LINEAR) {
+        reinterpret_cast<uint32_t*>(out + pix * COUT)[co / 2] = pack_bf16(z0, z1);
+      } else {
+        reinterpret_cast<uint32_t*>(zsave + pix * COUT)[co / 2] = pack_bf16(z0, z1);
+        float r0 = fmaxf(z0, 0.f), r1 = fmaxf(z1, 0.f);
+        if constexpr (EPI == EPI_RELU_RES) {
+          const __nv_bfloat162 h = reinterpret_cast<const __nv_bfloat162*>(in + pix * CIN)[co / 2];
+          r0 += __bfloat162float(h.x);
+          r1 += __bfloat162float(h.y);
+        }
+        reinterpret_cast<uint32_t*>(out + pix * COUT)[co / 2] = pack_bf16(r0, r1);
+      }
+    }
+  }
+}
+
+// Weight gradient dW[tap][co][ci] = sum_p x[p + d(tap)][ci] dy[p][co] for CIN = 32 and COUT = 32 or 8:
+// a persistent grid, each block walking 16 x 8 tiles and warp `tap` accumulating that tap's 32 x 32 (or
+// 8 x 32) block in registers; partial[block] is summed by wgrad_reduce in block order.
+template <int COUT>
+__global__ void __launch_bounds__(32 * NTAP) wgrad_mma(const bf16* __restrict__ x, const bf16* __restrict__ dy, int B,
+                                                       int H, int W, float* __restrict__ partial) {
+  constexpr int CIN = CH;
+  constexpr int XS = TW + 2 + 2;  // smem row stride of the transposed input tile (pixels)
+  constexpr int DS = TW + 8;      // smem row stride of the transposed output-gradient tile
+  __shared__ __align__(16) bf16 s_x[CIN * (TH + 2) * XS];  // [ci][ty][tx]
+  __shared__ __align__(16) bf16 s_dy[COUT * TH * DS];       // [co][ty][tx]
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int gid = lane >> 2, tig = lane & 3;
+  const int tap = warp, ky = tap / 3, kx = tap % 3;
+  constexpr int MT = COUT >= 16 ? COUT / 16 : 1;  // M tiles over co (COUT 8: one padded tile)
+  float acc[MT][CIN / 8][4];
+#pragma unroll
+  for (int m = 0; m < MT; ++m)
+#pragma unroll
+    for (int n = 0; n < CIN / 8; ++n) acc[m][n][0] = acc[m][n][1] = acc[m][n][2] = acc[m][n][3] = 0.f;
+  const int tiles_x = (W + TW - 1) / TW, tiles_y = (H + TH - 1) / TH;
+  const int ntiles = B * tiles_x * tiles_y;
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const int b = t / (tiles_x * tiles_y), r = t - b * tiles_x * tiles_y;
+    const int y0 = (r / tiles_x) * TH, x0 = (r % tiles_x) * TW;
+    __syncthreads();
+    for (int i = tid; i < (TH + 2) * (TW + 2) * CIN; i += blockDim.x) {
+      const int pix = i / CIN, ci = i - pix * CIN;
+      const int ty = pix / (TW + 2), tx = pix - ty * (TW + 2);
+      const int gy = y0 - 1 + ty, gx = x0 - 1 + tx;
+      bf16 v = __float2bfloat16(0.f);
+      if (gy >= 0 && gy < H && gx >= 0 && gx < W) v = x[(((size_t)b * H + gy) * W + gx) * CIN + ci];
+      s_x[(ci * (TH + 2) + ty) * XS + tx] = v;
+    }
+    for (int i = tid; i < TH * TW * COUT; i += blockDim.x) {
+      const int pix = i / COUT, co = i - pix * COUT;
+      const int ty = pix / TW, tx = pix - ty * TW;
+      const int gy = y0 + ty, gx = x0 + tx;
+      bf16 v = __float2bfloat16(0.f);
+      if (gy < H && gx < W) v = dy[(((size_t)b * H + gy) * W + gx) * COUT + co];
+      s_dy[(co * TH + ty) * DS + tx] = v;
+    }
+    __syncthreads();
+    // K = pixels: one k-step per tile row (16 pixels)
+    for (int ty = 0; ty < TH; ++ty) {
+#pragma unroll
+      for (int m = 0; m < MT; ++m) {
+        uint32_t a[4];
+        const int co0 = m * 16 + gid, co1 = co0 + 8;
+        const bf16* d0 = s_dy + (co0 * TH + ty) * DS + tig * 2;
+        a[0] = *reinterpret_cast<const uint32_t*>(d0);
+        a[2] = *reinterpret_cast<const uint32_t*>(d0 + 8);
+        if (COUT >= 16) {
+          const bf16* d1 = s_dy + (co1 * TH + ty) * DS + tig * 2;
+          a[1] = *reinterpret_cast<const uint32_t*>(d1);
+          a[3] = *reinterpret_cast<const uint32_t*>(d1 + 8);
+        } else {
+          a[1] = a[3] = 0u;  // rows 8..15 of the padded 8-channel tile
+        }
+#pragma unroll
+        for (int n = 0; n < CIN / 8; ++n) {
+          const bf16* xr = s_x + ((n * 8 + gid) * (TH + 2) + ty + ky) * XS + kx + tig * 2;
+          const uint32_t b0 = (uint32_t)__bfloat16_as_ushort(xr[0]) | ((uint32_t)__bfloat16_as_ushort(xr[1]) << 16);
+          const uint32_t b1 = (uint32_t)__bfloat16_as_ushort(xr[8]) | ((uint32_t)__bfloat16_as_ushort(xr[9]) << 16);
+          mma16816(acc[m][n], a, b0, b1);
+        }
+      }
+    }
+  }
+  // partial[block][tap][co][ci]
+  float* pb = partial + ((size_t)blockIdx.x * NTAP + tap) * COUT * CIN;
+#pragma unroll
+  for (int m = 0; m < MT; ++m)
+#pragma unroll
+    for (int n = 0; n < CIN / 8; ++n)
+#pragma unroll
+      for (int hh = 0; hh < 2; ++hh) {
+        const int co = m * 16 + gid + 8 * hh;
+        if (co >= COUT) continue;
+        const int ci = n * 8 + tig * 2;
+        pb[co * CIN + ci] = acc[m][n][2 * hh];
+        pb[co * CIN + ci + 1] = acc[m][n][2 * hh + 1];
+      }
+}
+
+// grad[i] = sum_b partial[b][i] (block order)
+__global__ void wgrad_reduce(const float* __restrict__ partial, int nblocks, int n, float* __restrict__ grad) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    float s = 0.f;
+    for (int b = 0; b < nblocks; ++b) s += partial[(size_t)b * n + i];
+    grad[i] = s;
+  }
+}
+
+// db[co] = sum over pixels of dy[p][co]: one block per channel, fixed-order tree.
+__global__ void bias_grad(const bf16* __restrict__ dy, size_t npix, int C, float* __restrict__ db) {
+  __shared__ float sh[256];
+  const int co = blockIdx.x;
+  float s = 0.f;
+  for (size_t p = threadIdx.x; p < npix; p += blockDim.x) s += __bfloat162float(dy[p * C + co]);
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) db[co] = sh[0];
+}
+
+// w'[tap'][ci][co] = w[8 - tap'][co][ci] (padded to COP output / CIP input channels) for the data gradient.
+__global__ void flip_transpose(const bf16* __restrict__ w, int cout, int cin, int cop, int cip, bf16* __restrict__ wt) {
+  const int n = NTAP * cip * cop;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int tap = i / (cip * cop), r = i - tap * cip * cop;
+    const int ci = r / cop, co = r - ci * cop;  // wt[tap][ci (as out)][co (as in)]
+    bf16 v = __float2bfloat16(0.f);
+    if (ci < cin && co < cout) v = w[((size_t)(8 - tap) * cout + co) * cin + ci];
+    wt[i] = v;
+  }
+}
+
+// First layer, 2 -> 32 channels (too narrow for the tensor cores): SIMT, relu, saves z.
+__global__ void conv_in_fwd(const float* __restrict__ x, const float* __restrict__ w, const float* __restrict__ bias,
+                            int B, int H, int W, bf16* __restrict__ out, bf16* __restrict__ zsave) {
+  const size_t n = (size_t)B * H * W;
+  for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < n; p += (size_t)gridDim.x * blockDim.x) {
+    const int xx = (int)(p % W), yy = (int)((p / W) % H), b = (int)(p / ((size_t)W * H));
+    float in[NTAP][2];
+    for (int tap = 0; tap < NTAP; ++tap) {
+      const int gy = yy + tap / 3 - 1, gx = xx + tap % 3 - 1;
+      const bool ok = gy >= 0 && gy < H && gx >= 0 && gx < W;
+      const size_t q = ((size_t)b * H + gy) * W + gx;
+      in[tap][0] = ok ? x[q * 2] : 0.f;
+      in[tap][1] = ok ? x[q * 2 + 1] : 0.f;
+    }
+    for (int co = 0; co < CH; co += 2) {
+      float z[2];
+      for (int j = 0; j < 2; ++j) {
+        float s = bias[co + j];
+        for (int tap = 0; tap < NTAP; ++tap)
+          s += w[(tap * CH + co + j) * 2] * in[tap][0] + w[(tap * CH + co + j) * 2 + 1] * in[tap][1];
+        z[j] = s;
+      }
+      reinterpret_cast<uint32_t*>(zsave + p * CH)[co / 2] = pack_bf16(z[0], z[1]);
+      reinterpret_cast<uint32_t*>(out + p * CH)[co / 2] = pack_bf16(fmaxf(z[0], 0.f), fmaxf(z[1], 0.f));
+    }
+  }
+}
+
+// First-layer weight gradient: dW[tap][co][cj] = sum_p x[p + d][cj] g[p][co]; block per (tap, co).
+__global__ void conv_in_wgrad(const float* __restrict__ x, const bf16* __restrict__ g, int B, int H, int W,
+                              float* __restrict__ dw, float* __restrict__ db) {
+  __shared__ float sh[3][256];
+  const int tap = blockIdx.x / CH, co = blockIdx.x % CH;
+  const int ky = tap / 3 - 1, kx = tap % 3 - 1;
+  const size_t n = (size_t)B * H * W;
+  float s0 = 0.f, s1 = 0.f, sb = 0.f;
+  for (size_t p = threadIdx.x; p < n; p += blockDim.x) {
+    const int xx = (int)(p % W), yy = (int)((p / W) % H), b = (int)(p / ((size_t)W * H));
+    const float gv = __bfloat162float(g[p * CH + co]);
+    const int gy = yy + ky, gx = xx + kx;
+    if (gy >= 0 && gy < H && gx >= 0 && gx < W) {
+      const size_t q = ((size_t)b * H + gy) * W + gx;
+      s0 += x[q * 2] * gv;
+      s1 += x[q * 2 + 1] * gv;
+    }
+    sb += gv;
+  }
+  sh[0][threadIdx.x] = s0;
+  sh[1][threadIdx.x] = s1;
+  sh[2][threadIdx.x] = sb;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o)
+      for (int j = 0; j < 3; ++j) sh[j][threadIdx.x] += sh[j][threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    dw[(tap * CH + co) * 2] = sh[0][0];
+    dw[(tap * CH + co) * 2 + 1] = sh[1][0];
+    if (tap == 0) db[co] = sh[2][0];
+  }
+}
+
+// g = gin * relu'(z)   (BF16 in and out)
+__global__ void relu_bwd(const bf16* __restrict__ gin, const bf16* __restrict__ z, size_t n, bf16* __restrict__ gout) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    gout[i] = __bfloat162float(z[i]) > 0.f ? gin[i] : __float2bfloat16(0.f);
+}
+
+// acc = acc + g  (FP32 accumulator of a residual stream's gradient, BF16 addend)
+__global__ void add_into(float* __restrict__ acc, const bf16* __restrict__ g, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    acc[i] += __bfloat162float(g[i]);
+}
+
+__global__ void to_bf16(const float* __restrict__ a, size_t n, bf16* __restrict__ out) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    out[i] = __float2bfloat16(a[i]);
+}
+
+// Mean squared error over the 6 used output channels and its gradient (padded to 8 channels, BF16).
+__global__ void mse_loss(const float* __restrict__ y, const float* __restrict__ t, size_t npix, float scale,
+                         bf16* __restrict__ g, double* __restrict__ partial) {
+  __shared__ double sh[256];
+  double s = 0;
+  for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < npix; p += (size_t)gridDim.x * blockDim.x) {
+    for (int c = 0; c < 8; ++c) {
+      float d = 0.f;
+      if (c < 6) {
+        d = y[p * 8 + c] - t[p * 6 + c];
+        s += (double)d * d;
+      }
+      g[p * 8 + c] = __float2bfloat16(2.f * d * scale);
+    }
+  }
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) partial[blockIdx.x] = sh[0];
+}
+
+// Adam on FP32 master weights, BF16 copy refreshed.
+__global__ void adam_step(float* __restrict__ w, const float* __restrict__ g, float* __restrict__ m,
+                          float* __restrict__ v, int n, float lr, float b1, float b2, float eps, float c1, float c2,
+                          bf16* __restrict__ wb) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const float gi = g[i];
+    const float mi = b1 * m[i] + (1.f - b1) * gi;
+    const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    const float wi = w[i] - lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+    w[i] = wi;
+    if (wb) wb[i] = __float2bfloat16(wi);
+  }
+}
+
+// x = [Re, Im] of the complex input / s per image (s = max |u0| of that image, given).
+__global__ void prep_input(const float2* __restrict__ u0, const float* __restrict__ inv_s, int B, size_t npix,
+                           float* __restrict__ x) {
+  const size_t n = (size_t)B * npix;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const float s = inv_s[i / npix];
+    x[2 * i] = u0[i].x * s;
+    x[2 * i + 1] = u0[i].y * s;
+  }
+}
+
+// u = u0 + s (o0 + i o1), vx = s (o2 + i o3), vy = s (o4 + i o5)
+__global__ void assemble_output(const float2* __restrict__ u0, const float* __restrict__ o, const float* __restrict__ s,
+                                int B, size_t npix, float2* __restrict__ u, float2* __restrict__ v) {
+  const size_t n = (size_t)B * npix;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const size_t b = i / npix, p = i - b * npix;
+    const float sc = s[b];
+    u[i] = u0[i] + sc * c2(o[i * 8], o[i * 8 + 1]);
+    v[(2 * b) * npix + p] = sc * c2(o[i * 8 + 2], o[i * 8 + 3]);
+    v[(2 * b + 1) * npix + p] = sc * c2(o[i * 8 + 4], o[i * 8 + 5]);
+  }
+}
+
+// training target: t = [(u* - u0)/s, v*/s] in 6 channels
+__global__ void prep_target(const float2* __restrict__ u0, const float2* __restrict__ ut, const float2* __restrict__ vt,
+                            const float* __restrict__ inv_s, int B, size_t npix, float* __restrict__ t) {
+  const size_t n = (size_t)B * npix;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const size_t b = i / npix, p = i - b * npix;
+    const float s = inv_s[b];
+    const float2 du = (ut[i] - u0[i]) * s;
+    const float2 vx = vt[(2 * b) * npix + p] * s, vy = vt[(2 * b + 1) * npix + p] * s;
+    t[i * 6 + 0] = du.x;
+    t[i * 6 + 1] = du.y;
+    t[i * 6 + 2] = vx.x;
+    t[i * 6 + 3] = vx.y;
+    t[i * 6 + 4] = vy.x;
+    t[i * 6 + 5] = vy.y;
+  }
+}
+
+// s[b] = max |u0| over image b; inv_s[b] = 1 / s[b] (1 for an all-zero image). Block per image.
+__global__ void image_scale(const float2* __restrict__ u0, size_t npix, float* __restrict__ s,
+                            float* __restrict__ inv_s) {
+  __shared__ float sh[256];
+  const float2* img = u0 + (size_t)blockIdx.x * npix;
+  float m = 0.f;
+  for (size_t i = threadIdx.x; i < npix; i += blockDim.x) m = fmaxf(m, sqrtf(abs2(img[i])));
+  sh[threadIdx.x] = m;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) sh[threadIdx.x] = fmaxf(sh[threadIdx.x], sh[threadIdx.x + o]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    const float v = sh[0] > 0.f ? sh[0] : 1.f;
+    s[blockIdx.x] = v;
+    inv_s[blockIdx.x] = 1.f / v;
+  }
+}
+
+inline int grid_for(size_t n) { return (int)std::min<size_t>((n + 255) / 256, 4096); }
+
+}  // namespace
+
+// ------------------------------------------------------------------------------------------------
+// Host side: parameters, activations for a batch, forward / backward / Adam.
+// ------------------------------------------------------------------------------------------------
+struct CnnParam {
+  int n = 0;          // elements
+  DevBuf w, g, m, v;  // FP32 master, gradient, Adam moments
+  DevBuf wb;          // BF16 copy used by the tensor-core kernels (null for the SIMT first layer)
+};
+
+class WarmStartCnn {
+ public:
+  static constexpr int kLayers = 8;  // conv_in, 6 hidden, conv_out
+  explicit WarmStartCnn(uint64_t seed) {
+    std::mt19937_64 gen(seed);
+    // conv_in: [9][32][2] + bias 32; hidden: [9][32][32] + 32; conv_out: [9][8][32] + 8
+    const int sizes[kLayers] = {NTAP * CH * 2, NTAP * CH * CH, NTAP * CH * CH, NTAP * CH * CH, NTAP * CH * CH,
+                                NTAP * CH * CH, NTAP * CH * CH, NTAP * 8 * CH};
+    const int fan_in[kLayers] = {NTAP * 2, NTAP * CH, NTAP * CH, NTAP * CH, NTAP * CH, NTAP * CH, NTAP * CH, NTAP * CH};
+    const int nb[kLayers] = {CH, CH, CH, CH, CH, CH, CH, 8};
+    for (int l = 0; l < kLayers; ++l) {
+      std::vector<float> w(sizes[l]);
+      // He initialisation; the hidden residual branches start small so the net begins near identity
+      const float sd = std::sqrt(2.0f / fan_in[l]) * ((l >= 1 && l <= 6) ? 0.25f : (l == 7 ? 0.1f : 1.0f));
+      std::normal_distribution<float> dis(0.f, sd);
+      for (auto& x : w) x = dis(gen);
+      if (l == 7)  // output channels 6, 7 are padding
+        for (int tap = 0; tap < NTAP; ++tap)
+          for (int co = 6; co < 8; ++co)
+            for (int ci = 0; ci < CH; ++ci) w[((size_t)tap * 8 + co) * CH + ci] = 0.f;
+      init_param(W_[l], w, l >= 1);
+      init_param(B_[l], std::vector<float>(nb[l], 0.f), false);
+    }
+  }
+
+  // Parameters as one flat FP32 vector (weights then biases per layer) for saving / loading.
+  std::vector<float> get_params() const {
+    std::vector<float> out;
+    for (int l = 0; l < kLayers; ++l)
+      for (const CnnParam* p : {&W_[l], &B_[l]}) {
+        const size_t o = out.size();
+        out.resize(o + p->n);
+        PDT_CUDA_CHECK(cudaMemcpy(out.data() + o, p->w.p, p->n * sizeof(float), cudaMemcpyDeviceToHost));
+      }
+    return out;
+  }
+  void set_params(const float* src, size_t n) {
+    size_t o = 0;
+    for (int l = 0; l < kLayers; ++l)
+      for (CnnParam* p : {&W_[l], &B_[l]}) {
+        if (o + p->n > n) throw Error(PDT_ERR_SIZE, "parameter vector too short");
+        PDT_CUDA_CHECK(cudaMemcpy(p->w.p, src + o, p->n * sizeof(float), cudaMemcpyHostToDevice));
+        if (p->wb.p) refresh_bf16(*p, 0);
+        o += p->n;
+      }
+    if (o != n) throw Error(PDT_ERR_SIZE, "parameter vector length mismatch");
+    PDT_CUDA_CHECK(cudaDeviceSynchronize());
+  }
+  size_t num_params() const {
+    size_t n = 0;
+    for (int l = 0; l < kLayers; ++l) n += W_[l].n + B_[l].n;
+    return n;
+  }
+
+  // Forward pass for B images of H x W; u0 complex [B][H][W], s = per-image scale. Writes o (FP32, 8 ch).
+  void forward(const float2* u0, const float* inv_s, int B, int H, int W, cudaStream_t st) {
+    alloc(B, H, W);
+    const size_t npix = (size_t)B * H * W;
+    prep_input<<<grid_for(npix), 256, 0, st>>>(u0, inv_s, B, (size_t)H * W, x_.as<float>());
+    PDT_LAUNCH_CHECK();
+    conv_in_fwd<<<grid_for(npix), 256, 0, st>>>(x_.as<float>(), W_[0].w.as<float>(), B_[0].w.as<float>(), B, H, W,
+                                               h_[0].as<bf16>(), z_[0].as<bf16>());
+    PDT_LAUNCH_CHECK();
+    count_launch(2);
+    const dim3 grid((W + TW - 1) / TW, (H + TH - 1) / TH, B);
+    for (int l = 1; l <= 6; ++l) {
+      conv3x3_mma<CH, CH, EPI_RELU_RES><<<grid, 32 * TH, 0, st>>>(h_[l - 1].as<bf16>(), W_[l].wb.as<bf16>(),
+                                                                  B_[l].w.as<float>(), H, W, h_[l].as<bf16>(),
+                                                                  z_[l].as<bf16>(), nullptr);
+      PDT_LAUNCH_CHECK();
+      count_launch();
+    }
+    conv3x3_mma<CH, 8, EPI_F32><<<grid, 32 * TH, 0, st>>>(h_[6].as<bf16>(), W_[7].wb.as<bf16>(), B_[7].w.as<float>(),
+                                                          H, W, nullptr, nullptr, o_.as<float>());
+    PDT_LAUNCH_CHECK();
+    count_launch();
+  }
+
+  // Backward pass after forward(): loss = mean over pixels of sum_c (o_c - t_c)^2 (t: 6 channels FP32).
+  double backward(const float* target, int B, int H, int W, cudaStream_t st) {
+    const size_t npix = (size_t)B * H * W;
+    const float scale = 1.0f / (float)npix;
+    const int lb = grid_for(npix);
+    part_.ensure(sizeof(double) * lb);
+    mse_loss<<<lb, 256, 0, st>>>(o_.as<float>(), target, npix, scale, go_.as<bf16>(), part_.as<double>());
+    PDT_LAUNCH_CHECK();
+    count_launch();
+    const dim3 grid((W + TW - 1) / TW, (H + TH - 1) / TH, B);
+    // conv_out: dW, db, and dh6 = conv(go, W7') (8 -> 32 channels, padded to 16 input channels)
+    wgrad(8, h_[6].as<bf16>(), go_.as<bf16>(), B, H, W, W_[7].g.as<float>(), st);
+    bias_grad<<<8, 256, 0, st>>>(go_.as<bf16>(), npix, 8, B_[7].g.as<float>());
+    PDT_LAUNCH_CHECK();
+    // go is [npix][8]; the data-gradient kernel needs 16 input channels: pad into go16_
+    pad8to16(go_.as<bf16>(), npix, st);
+    flip_transpose<<<64, 256, 0, st>>>(W_[7].wb.as<bf16>(), 8, CH, 16, CH, wt_.as<bf16>());
+    PDT_LAUNCH_CHECK();
+    conv3x3_mma<16, CH, EPI_LINEAR><<<grid, 32 * TH, 0, st>>>(go16_.as<bf16>(), wt_.as<bf16>(), nullptr, H, W,
+                                                              gtmp_.as<bf16>(), nullptr, nullptr);
+    PDT_LAUNCH_CHECK();
+    count_launch(4);
+    // residual stream gradient G (FP32): G = dh6
+    zero_acc(npix * CH, st);
+    add_into<<<grid_for(npix * CH), 256, 0, st>>>(gacc_.as<float>(), gtmp_.as<bf16>(), npix * CH);
+    PDT_LAUNCH_CHECK();
+    for (int l = 6; l >= 1; --l) {
+      // h_l = h_{l-1} + relu(z_l), z_l = conv_l(h_{l-1}):  dz = G * relu'(z_l); dh_{l-1} = G + conv_l^T(dz)
+      to_bf16<<<grid_for(npix * CH), 256, 0, st>>>(gacc_.as<float>(), npix * CH, gbf_.as<bf16>());
+      relu_bwd<<<grid_for(npix * CH), 256, 0, st>>>(gbf_.as<bf16>(), z_[l].as<bf16>(), npix * CH, gz_.as<bf16>());
+      PDT_LAUNCH_CHECK();
+      wgrad(CH, h_[l - 1].as<bf16>(), gz_.as<bf16>(), B, H, W, W_[l].g.as<float>(), st);
+      bias_grad<<<CH, 256, 0, st>>>(gz_.as<bf16>(), npix, CH, B_[l].g.as<float>());
+      flip_transpose<<<64, 256, 0, st>>>(W_[l].wb.as<bf16>(), CH, CH, CH, CH, wt_.as<bf16>());
+      conv3x3_mma<CH, CH, EPI_LINEAR><<<grid, 32 * TH, 0, st>>>(gz_.as<bf16>(), wt_.as<bf16>(), nullptr, H, W,
+                                                                gtmp_.as<bf16>(), nullptr, nullptr);
+      add_into<<<grid_for(npix * CH), 256, 0, st>>>(gacc_.as<float>(), gtmp_.as<bf16>(), npix * CH);
+      PDT_LAUNCH_CHECK();
+      count_launch(6);
+    }
+    // conv_in: h1 = relu(z_0): dz0 = G * relu'(z0)
+    to_bf16<<<grid_for(npix * CH), 256, 0, st>>>(gacc_.as<float>(), npix * CH, gbf_.as<bf16>());
+    relu_bwd<<<grid_for(npix * CH), 256, 0, st>>>(gbf_.as<bf16>(), z_[0].as<bf16>(), npix * CH, gz_.as<bf16>());
+    conv_in_wgrad<<<NTAP * CH, 256, 0, st>>>(x_.as<float>(), gz_.as<bf16>(), B, H, W, W_[0].g.as<float>(),
+                                             B_[0].g.as<float>());
+    PDT_LAUNCH_CHECK();
+    count_launch(3);
+    std::vector<double> h(lb);
+    PDT_CUDA_CHECK(cudaMemcpyAsync(h.data(), part_.p, sizeof(double) * lb, cudaMemcpyDeviceToHost, st));
+    PDT_CUDA_CHECK(cudaStreamSynchronize(st));
+    double loss = 0;
+    for (double v : h) loss += v;
+    return loss / (double)npix;
+  }
+
+  void adam(float lr, cudaStream_t st) {
+    ++step_;
+    const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+    const float c1 = 1.f - std::pow(b1, (float)step_), c2 = 1.f - std::pow(b2, (float)step_);
+    for (int l = 0; l < kLayers; ++l)
+      for (CnnParam* p : {&W_[l], &B_[l]}) {
+        adam_step<<<grid_for(p->n), 256, 0, st>>>(p->w.as<float>(), p->g.as<float>(), p->m.as<float>(),
+                                                  p->v.as<float>(), p->n, lr, b1, b2, eps, c1, c2,
+                                                  p->wb.p ? p->wb.as<bf16>() : nullptr);
+        PDT_LAUNCH_CHECK();
+        count_launch();
+      }
+  }
+
+  const float* output() const { return o_.as<float>(); }
+  // per-image scales of u0 (device): s, 1/s
+  void scales(const float2* u0, int B, size_t npix_img, cudaStream_t st) {
+    sc_.ensure(2 * sizeof(float) * std::max(B, 1));
+    image_scale<<<B, 256, 0, st>>>(u0, npix_img, sc_.as<float>(), sc_.as<float>() + B);
+    PDT_LAUNCH_CHECK();
+    count_launch();
+  }
+  const float* scale_ptr() const { return sc_.as<float>(); }
+  const float* inv_scale_ptr(int B) const { return sc_.as<float>() + B; }
+  std::vector<float> get_grads() const {
+    std::vector<float> out;
+    for (int l = 0; l < kLayers; ++l)
+      for (const CnnParam* p : {&W_[l], &B_[l]}) {
+        const size_t o = out.size();
+        out.resize(o + p->n);
+        PDT_CUDA_CHECK(cudaMemcpy(out.data() + o, p->g.p, p->n * sizeof(float), cudaMemcpyDeviceToHost));
+      }
+    return out;
+  }
+  float* target_buf(size_t npix) {
+    t_.ensure(npix * 6 * sizeof(float));
+    return t_.as<float>();
+  }
+
+  void make_target(const float2* u0, const float2* ut, const float2* vt, const float* inv_s, int B, size_t npix_img,
+                   cudaStream_t st) {
+    float* t = target_buf((size_t)B * npix_img);
+    prep_target<<<grid_for((size_t)B * npix_img), 256, 0, st>>>(u0, ut, vt, inv_s, B, npix_img, t);
+    PDT_LAUNCH_CHECK();
+    count_launch();
+  }
+  void assemble(const float2* u0, const float* s, int B, size_t npix_img, float2* u, float2* v, cudaStream_t st) {
+    assemble_output<<<grid_for((size_t)B * npix_img), 256, 0, st>>>(u0, o_.as<float>(), s, B, npix_img, u, v);
+    PDT_LAUNCH_CHECK();
+    count_launch();
+  }
+
+ private:
+  void init_param(CnnParam& p, const std::vector<float>& w, bool bf) {
+    p.n = (int)w.size();
+    p.w.ensure(w.size() * sizeof(float));
+    p.g.ensure(w.size() * sizeof(float));
+    p.m.ensure(w.size() * sizeof(float));
+    p.v.ensure(w.size() * sizeof(float));
+    PDT_CUDA_CHECK(cudaMemcpy(p.w.p, w.data(), w.size() * sizeof(float), cudaMemcpyHostToDevice));
+    PDT_CUDA_CHECK(cudaMemset(p.g.p, 0, p.g.bytes));
+    PDT_CUDA_CHECK(cudaMemset(p.m.p, 0, p.m.bytes));
+    PDT_CUDA_CHECK(cudaMemset(p.v.p, 0, p.v.bytes));
+    if (bf) {
+      p.wb.ensure(w.size() * sizeof(bf16));
+      refresh_bf16(p, 0);
+    }
+  }
+  void refresh_bf16(CnnParam& p, cudaStream_t st) {
+    to_bf16<<<grid_for(p.n), 256, 0, st>>>(p.w.as<float>(), p.n, p.wb.as<bf16>());
+    PDT_LAUNCH_CHECK();
+  }
+  void alloc(int B, int H, int W) {
+    if (B == B_n_ && H == H_n_ && W == W_n_) return;
+    const size_t npix = (size_t)B * H * W;
+    x_.ensure(npix * 2 * sizeof(float));
+    for (int l = 0; l < 7; ++l) {
+      h_[l].ensure(npix * CH * sizeof(bf16));
+      z_[l].ensure(npix * CH * sizeof(bf16));
+    }
+    o_.ensure(npix * 8 * sizeof(float));
+    go_.ensure(npix * 8 * sizeof(bf16));
+    go16_.ensure(npix * 16 * sizeof(bf16));
+    gtmp_.ensure(npix * CH * sizeof(bf16));
+    gbf_.ensure(npix * CH * sizeof(bf16));
+    gz_.ensure(npix * CH * sizeof(bf16));
+    gacc_.ensure(npix * CH * sizeof(float));
+    wt_.ensure(NTAP * CH * CH * sizeof(bf16));
+    B_n_ = B;
+    H_n_ = H;
+    W_n_ = W;
+  }
+  void zero_acc(size_t n, cudaStream_t st) { PDT_CUDA_CHECK(cudaMemsetAsync(gacc_.p, 0, n * sizeof(float), st)); }
+  void pad8to16(const bf16* g8, size_t npix, cudaStream_t st) {
+    PDT_CUDA_CHECK(cudaMemsetAsync(go16_.p, 0, npix * 16 * sizeof(bf16), st));
+    PDT_CUDA_CHECK(cudaMemcpy2DAsync(go16_.p, 16 * sizeof(bf16), g8, 8 * sizeof(bf16), 8 * sizeof(bf16), npix,
+                                     cudaMemcpyDeviceToDevice, st));
+  }
+  void wgrad(int cout, const bf16* x, const bf16* dy, int B, int H, int W, float* grad, cudaStream_t st) {
+    int sms = 0, dev = 0;
+    PDT_CUDA_CHECK(cudaGetDevice(&dev));
+    PDT_CUDA_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const int tiles = B * ((W + TW - 1) / TW) * ((H + TH - 1) / TH);
+    const int nb = std::max(1, std::min(sms * 2, tiles));
+    const int n = NTAP * cout * CH;
+    wpart_.ensure((size_t)nb * NTAP * CH * CH * sizeof(float));
+    if (cout == CH)
+      wgrad_mma<CH><<<nb, 32 * NTAP, 0, st>>>(x, dy, B, H, W, wpart_.as<float>());
+    else
+      wgrad_mma<8><<<nb, 32 * NTAP, 0, st>>>(x, dy, B, H, W, wpart_.as<float>());
+    PDT_LAUNCH_CHECK();
+    wgrad_reduce<<<grid_for(n), 256, 0, st>>>(wpart_.as<float>(), nb, n, grad);
+    PDT_LAUNCH_CHECK();
+    count_launch(2);
+  }
+
+  CnnParam W_[kLayers], B_[kLayers];
+  DevBuf x_, h_[7], z_[7], o_, go_, go16_, gtmp_, gbf_, gz_, gacc_, wt_, wpart_, part_, t_, sc_;
+  int B_n_ = 0, H_n_ = 0, W_n_ = 0;
+  long step_ = 0;
+};
+
+}  // namespace pdt
+
+// ==================================================================================================
+// C ABI of the warm-start network
+// ==================================================================================================
+struct pdt_cnn {
+  std::unique_ptr<pdt::WarmStartCnn> impl;
+};
+
+namespace {
+template <class F>
+pdt_status cnn_guard(F&& fn) {
+  try {
+    fn();
+    return PDT_OK;
+  } catch (const pdt::Error& e) {
+    pdt::set_last_error(e.what());
+    return e.code;
+  } catch (const std::exception& e) {
+    pdt::set_last_error(e.what());
+    return PDT_ERR_INVALID_ARGUMENT;
+  }
+}
+void cnn_check(pdt_cnn* c, int B, int H, int W) {
+  if (!c) throw pdt::Error(PDT_ERR_INVALID_ARGUMENT, "null network");
+  if (B < 1 || H < 1 || W < 1) throw pdt::Error(PDT_ERR_INVALID_ARGUMENT, "B, H and W must be positive");
+}
+}  // namespace
+
+extern "C" {
+
+pdt_status pdt_cnn_create(uint64_t seed, pdt_cnn** out) {
+  return cnn_guard([&] {
+    if (!out) throw pdt::Error(PDT_ERR_INVALID_ARGUMENT, "null out");
+    auto h = std::make_unique<pdt_cnn>();
+    h->impl = std::make_unique<pdt::WarmStartCnn>(seed);
+    *out = h.release();
+  });
+}
+
+pdt_status pdt_cnn_destroy(pdt_cnn* c) {
+  return cnn_guard([&] { delete c; });
+}
+
+pdt_status pdt_cnn_num_params(pdt_cnn* c, size_t* n) {
+  return cnn_guard([&] {
+    cnn_check(c, 1, 1, 1);
+    *n = c->impl->num_params();
+  });
+}
+
+pdt_status pdt_cnn_get_params(pdt_cnn* c, float* dst, size_t n) {
+  return cnn_guard([&] {
+    cnn_check(c, 1, 1, 1);
+    auto v = c->impl->get_params();
+    if (n != v.size()) throw pdt::Error(PDT_ERR_SIZE, "parameter count mismatch");
+    std::memcpy(dst, v.data(), n * sizeof(float));
+  });
+}
+
+pdt_status pdt_cnn_set_params(pdt_cnn* c, const float* src, size_t n) {
+  return cnn_guard([&] {
+    cnn_check(c, 1, 1, 1);
+    c->impl->set_params(src, n);
+  });
+}
+
+pdt_status pdt_cnn_get_grads(pdt_cnn* c, float* dst, size_t n) {
+  return cnn_guard([&] {
+    cnn_check(c, 1, 1, 1);
+    auto v = c->impl->get_grads();
+    if (n != v.size()) throw pdt::Error(PDT_ERR_SIZE, "parameter count mismatch");
+    std::memcpy(dst, v.data(), n * sizeof(float));
+  });
+}
+
+pdt_status pdt_cnn_train_step(pdt_cnn* c, const void* u0, const void* ut, const void* vt, int B, int H, int W,
+                              float lr, void* stream, double* loss) {
+  return cnn_guard([&] {
+    cnn_check(c, B, H, W);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    auto& n = *c->impl;
+    const size_t np = (size_t)H * W;
+    n.scales(static_cast<const float2*>(u0), B, np, st);
+    n.make_target(static_cast<const float2*>(u0), static_cast<const float2*>(ut), static_cast<const float2*>(vt),
+                  n.inv_scale_ptr(B), B, np, st);
+    n.forward(static_cast<const float2*>(u0), n.inv_scale_ptr(B), B, H, W, st);
+    const double l = n.backward(n.target_buf((size_t)B * np), B, H, W, st);
+    if (lr > 0.f) n.adam(lr, st);
+    if (loss) *loss = l;
+  });
+}
+
+pdt_status pdt_cnn_predict(pdt_cnn* c, const void* u0, int B, int H, int W, void* u, void* v, void* stream) {
+  return cnn_guard([&] {
+    cnn_check(c, B, H, W);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    auto& n = *c->impl;
+    const size_t np = (size_t)H * W;
+    n.scales(static_cast<const float2*>(u0), B, np, st);
+    n.forward(static_cast<const float2*>(u0), n.inv_scale_ptr(B), B, H, W, st);
+    n.assemble(static_cast<const float2*>(u0), n.scale_ptr(), B, np, static_cast<float2*>(u), static_cast<float2*>(v),
+               st);
+    if (!stream) PDT_CUDA_CHECK(cudaStreamSynchronize(st));
+  });
+}
+
+}  // extern "C"

@@ -265,7 +265,8 @@ __global__ void __launch_bounds__(NT) mri_image_step_kernel(int W, int H, ImgPtr
   }
   float alpha0 = 1.f, alpha1 = 1.f;
   if constexpr (TGV) {
-    const int k = *iter;
+    // iter[0] = this round's index, iter[1] = table length
+    const int k = min(max(iter[0], 0), iter[1] - 1);
     alpha0 = alpha_tab[2 * k];
     alpha1 = alpha_tab[2 * k + 1];
   }

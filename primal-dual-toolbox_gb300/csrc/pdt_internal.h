@@ -98,6 +98,11 @@ struct PhaseMarker {
 
 // Element-wise helpers.
 void launch_fill_zero(void* p, size_t bytes, cudaStream_t st);
+// FP64 reductions (pdt_metrics.cu); they synchronise the stream.
+double reduce_dist2(bool complex_, const void* a, const void* b, size_t n, cudaStream_t st);
+void reduce_regularizer(bool complex_, const void* u, const void* vx, const void* vy, int W, int H, double out[2],
+                        cudaStream_t st);
+void launch_scale(float2* x, float s, size_t n, cudaStream_t st);
 // *tick += 1 (one thread).
 void launch_tick(int* tick, cudaStream_t st);
 

@@ -48,8 +48,12 @@ struct SolverHooks {
 class OpImpl {
  public:
   OpImpl(pdt_op_kind kind, std::string name, unsigned nreq, std::map<std::string, std::string> cfg)
-      : kind_(kind), name_(std::move(name)), nreq_(nreq), cfg_(std::move(cfg)) {}
+      : kind_(kind), name_(std::move(name)), nreq_(nreq), cfg_(std::move(cfg)), gen_(next_generation()) {}
   virtual ~OpImpl() = default;
+
+  // Process-wide unique identity of this operator and its current constants: changes whenever a constant
+  // is added, so solvers re-gather their data and re-capture graphs that baked in the operator's tables.
+  uint64_t generation() const { return gen_; }
 
   pdt_op_kind kind() const { return kind_; }
   const std::string& name() const { return name_; }
@@ -68,6 +72,9 @@ class OpImpl {
   virtual Dims output_size(const Dims& in) = 0;
   virtual SolverHooks* hooks() = 0;
 
+  // Launch configuration chosen by the operator's autotuner ("" when it has none).
+  virtual std::string tuning() { return ""; }
+
   // Checks for solvers: constants complete, sizes consistent.
   void operator_check(const Dims& in, const Dims& out);
 
@@ -85,6 +92,9 @@ class OpImpl {
   unsigned nreq_;
   std::map<std::string, std::string> cfg_;
   std::vector<std::unique_ptr<Constant>> constants_;
+  uint64_t gen_;
+
+  static uint64_t next_generation();
 };
 
 std::shared_ptr<OpImpl> make_operator(pdt_op_kind kind, const std::map<std::string, std::string>& cfg);

@@ -162,11 +162,23 @@ class _Operator:
         """Apply the adjoint operator (k-space -> image)."""
         return self._apply(True, y, out, stream)
 
+    def norm(self, iters=30, seed=0):
+        """Operator norm ||K|| by power iteration on K^H K with FP64 norms (the TGV step sizes assume <= 1)."""
+        out = ctypes.c_double()
+        check(lib.pdt_op_norm(self._h, int(iters), int(seed), ctypes.byref(out)))
+        return out.value
+
     def adjointnessCheck(self, seed=42):
         """Random u, p: returns (<Au, p>, <u, A^H p>) as complex numbers (adjointnessCheck of the reference)."""
         out = (ctypes.c_double * 4)()
         check(lib.pdt_op_adjointness(self._h, int(seed), out))
         return complex(out[0], out[1]), complex(out[2], out[3])
+
+    def tuning(self):
+        """The kernel configuration the autotuner picked for this operator (text)."""
+        buf = ctypes.create_string_buffer(1024)
+        check(lib.pdt_op_tuning(self._h, buf, 1024))
+        return buf.value.decode()
 
     def __str__(self):
         buf = ctypes.create_string_buffer(512)
@@ -214,6 +226,38 @@ class _Optimizer:
             raise TypeError(f"setOperator expects one of: {names}")
         check(lib.pdt_opt_set_operator(self._h, op._h))
         self._op = op
+
+    FIELDS = {"u": 0, "ubar": 1, "vx": 2, "vy": 3, "vbarx": 4, "vbary": 5, "px": 6, "py": 7, "qxx": 8, "qyy": 9,
+              "qxy": 10}
+
+    def setInput0UV(self, u0, v0=None, stream=None):
+        """Warm start of both TGV primals: u = u0, v = v0 (shape (2, H, W): vx, vy); duals reset to 0."""
+        b = Buffer(u0, self._dtype)
+        vb = None if v0 is None else Buffer(v0, self._dtype)
+        if vb is not None and vb.is_device != b.is_device:
+            raise ValueError("u0 and v0 must both be host or both be device arrays")
+        check(lib.pdt_opt_set_input0_uv(self._h, b.ptr, vb.ptr if vb else None, len(b.shape), _lib.iu_size(b.shape),
+                                        b.is_device, _lib.stream_handle(stream)))
+
+    def getField(self, name, out=None, stream=None):
+        """One plane of the solver state ('u', 'ubar', 'vx', 'vy', 'px', 'py', 'qxx', 'qyy', 'qxy', ...)."""
+        nd = ctypes.c_int()
+        size = (ctypes.c_int64 * 4)()
+        check(lib.pdt_opt_result_size(self._h, ctypes.byref(nd), size))
+        shape = _lib.np_shape(nd.value, size)
+        if out is None:
+            out = np.empty(shape, dtype=self._dtype)
+        b = Buffer(out, self._dtype)
+        if b.shape != shape:
+            raise ValueError(f"out has shape {b.shape}, expected {shape}")
+        check(lib.pdt_opt_get_field(self._h, self.FIELDS[name], b.ptr, b.is_device, _lib.stream_handle(stream)))
+        return out
+
+    def energy(self, stream=None):
+        """FP64 energy of the current state: {'total', 'data', 'first_order', 'second_order'}."""
+        out = (ctypes.c_double * 4)()
+        check(lib.pdt_opt_energy(self._h, _lib.stream_handle(stream), out))
+        return {"total": out[0], "data": out[1], "first_order": out[2], "second_order": out[3]}
 
     def solve(self, verbose=False, stream=None):
         """Run max_iter + 1 primal-dual iterations (asynchronous when a stream is given)."""

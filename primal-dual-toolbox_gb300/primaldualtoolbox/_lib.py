@@ -28,10 +28,14 @@ OPT_TV, OPT_TGV, OPT_TV_OP, OPT_TGV_OP, OPT_TGV_MRI = range(5)
 EXPORTED = ["pdt_last_error", "pdt_version", "pdt_launch_count", "pdt_host_alloc", "pdt_host_free",
             "pdt_stream_synchronize", "pdt_op_create", "pdt_op_destroy", "pdt_op_add_constant", "pdt_op_input_size",
             "pdt_op_output_size", "pdt_op_forward", "pdt_op_adjoint", "pdt_op_describe", "pdt_op_adjointness",
+            "pdt_op_tuning",
             "pdt_opt_create", "pdt_opt_destroy", "pdt_opt_get_params", "pdt_opt_set_params", "pdt_opt_set_operator",
             "pdt_opt_set_noisy_data", "pdt_opt_set_input0", "pdt_opt_solve", "pdt_opt_result_size",
-            "pdt_opt_get_result", "pdt_opt_profile", "pdt_batch_create", "pdt_batch_destroy", "pdt_batch_add",
-            "pdt_batch_solve", "pdt_cartesian_forward_noalloc"]
+            "pdt_opt_get_result", "pdt_opt_profile", "pdt_opt_set_input0_uv", "pdt_opt_get_field", "pdt_opt_energy",
+            "pdt_op_norm", "pdt_dist2", "pdt_batch_create", "pdt_batch_destroy", "pdt_batch_add",
+            "pdt_batch_solve", "pdt_cnn_create", "pdt_cnn_destroy", "pdt_cnn_num_params", "pdt_cnn_get_params",
+            "pdt_cnn_set_params", "pdt_cnn_get_grads", "pdt_cnn_train_step", "pdt_cnn_predict",
+            "pdt_cartesian_forward_noalloc"]
 
 
 class PdtError(RuntimeError):
@@ -71,6 +75,7 @@ def _load():
     L.pdt_op_forward.argtypes = [vp, vp, i, i64p, vp, i, i64p, i, vp]
     L.pdt_op_adjoint.argtypes = [vp, vp, i, i64p, vp, i, i64p, i, vp]
     L.pdt_op_describe.argtypes = [vp, ctypes.c_char_p, ctypes.c_size_t]
+    L.pdt_op_tuning.argtypes = [vp, ctypes.c_char_p, ctypes.c_size_t]
     L.pdt_op_adjointness.argtypes = [vp, ctypes.c_uint64, ctypes.POINTER(ctypes.c_double)]
     L.pdt_opt_create.argtypes = [i, i, ctypes.POINTER(vp)]
     L.pdt_opt_destroy.argtypes = [vp]
@@ -84,6 +89,11 @@ def _load():
     L.pdt_opt_get_result.argtypes = [vp, vp, i, vp]
     L.pdt_opt_profile.argtypes = [vp, i, vp, i, ctypes.POINTER(i), ctypes.c_char_p, ctypes.c_size_t,
                                   ctypes.POINTER(ctypes.c_double)]
+    L.pdt_opt_set_input0_uv.argtypes = [vp, vp, vp, i, i64p, i, vp]
+    L.pdt_opt_get_field.argtypes = [vp, i, vp, i, vp]
+    L.pdt_opt_energy.argtypes = [vp, vp, ctypes.POINTER(ctypes.c_double)]
+    L.pdt_op_norm.argtypes = [vp, i, ctypes.c_uint64, ctypes.POINTER(ctypes.c_double)]
+    L.pdt_dist2.argtypes = [i, vp, vp, ctypes.c_size_t, vp, ctypes.POINTER(ctypes.c_double)]
     L.pdt_batch_create.argtypes = [ctypes.POINTER(vp)]
     L.pdt_batch_destroy.argtypes = [vp]
     L.pdt_batch_add.argtypes = [vp, vp]

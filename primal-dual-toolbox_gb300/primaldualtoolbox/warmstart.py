@@ -1,0 +1,220 @@
+"""primaldualtoolbox.warmstart -- the learned warm start for TGV^2 MRI reconstruction.
+
+A small residual CNN (8 convolutions, 32 channels, 3 x 3, BF16 weights / activations, FP32 accumulation;
+libpdt.so's own tensor-core kernels for inference and training) maps the zero-filled image
+u0 = A^H f to an initial (u, v). ``warm_start`` applies it to an optimizer and keeps the plain start
+(u0, v = 0) whenever the network's start has the higher TGV energy -- the primal-dual iteration that
+follows still decides the result.
+
+Training data are made by the engine itself: TGV^2 solutions at fixed alpha of synthetic Cartesian
+problems (``make_training_set``), solved many at a time with ``primaldualtoolbox.batch``.
+
+    python -m primaldualtoolbox.warmstart --cases 256 --iters 3000 --out weights.npz
+
+There is no counterpart in the reference.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import time
+
+import numpy as np
+
+from . import _lib
+from ._lib import Buffer, check, lib
+
+DEFAULT_WEIGHTS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data", "warmstart_15c_640x368.npz")
+
+
+def _bind():
+    vp, i = ctypes.c_void_p, ctypes.c_int
+    lib.pdt_cnn_create.argtypes = [ctypes.c_uint64, ctypes.POINTER(vp)]
+    lib.pdt_cnn_destroy.argtypes = [vp]
+    lib.pdt_cnn_num_params.argtypes = [vp, ctypes.POINTER(ctypes.c_size_t)]
+    lib.pdt_cnn_get_params.argtypes = [vp, vp, ctypes.c_size_t]
+    lib.pdt_cnn_set_params.argtypes = [vp, vp, ctypes.c_size_t]
+    lib.pdt_cnn_get_grads.argtypes = [vp, vp, ctypes.c_size_t]
+    lib.pdt_cnn_train_step.argtypes = [vp, vp, vp, vp, i, i, i, ctypes.c_float, vp, ctypes.POINTER(ctypes.c_double)]
+    lib.pdt_cnn_predict.argtypes = [vp, vp, i, i, i, vp, vp, vp]
+    for n in ("pdt_cnn_create", "pdt_cnn_destroy", "pdt_cnn_num_params", "pdt_cnn_get_params", "pdt_cnn_set_params",
+              "pdt_cnn_get_grads", "pdt_cnn_train_step", "pdt_cnn_predict"):
+        getattr(lib, n).restype = ctypes.c_int
+
+
+_bind()
+
+
+def _dev(a, dtype):
+    b = Buffer(a, dtype)
+    if not b.is_device:
+        raise TypeError("the network takes device arrays (e.g. torch CUDA tensors)")
+    return b
+
+
+class WarmStartNet:
+    """The warm-start network. Images are device arrays: u0 (B, H, W) complex64, v (B, 2, H, W)."""
+
+    def __init__(self, seed=0, weights=None):
+        h = ctypes.c_void_p()
+        check(lib.pdt_cnn_create(int(seed), ctypes.byref(h)))
+        self._h = h
+        if weights is not None:
+            self.load(weights)
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            lib.pdt_cnn_destroy(h)
+            self._h = None
+
+    @property
+    def num_params(self):
+        n = ctypes.c_size_t()
+        check(lib.pdt_cnn_num_params(self._h, ctypes.byref(n)))
+        return n.value
+
+    def get_params(self):
+        out = np.empty(self.num_params, dtype=np.float32)
+        check(lib.pdt_cnn_get_params(self._h, out.ctypes.data, out.size))
+        return out
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        check(lib.pdt_cnn_set_params(self._h, p.ctypes.data, p.size))
+
+    def grads(self):
+        out = np.empty(self.num_params, dtype=np.float32)
+        check(lib.pdt_cnn_get_grads(self._h, out.ctypes.data, out.size))
+        return out
+
+    def save(self, path, **meta):
+        os.makedirs(os.path.dirname(os.path.abspath(path)), exist_ok=True)
+        np.savez(path, params=self.get_params(), meta=json.dumps(meta))
+
+    def load(self, path):
+        with np.load(path) as z:
+            self.set_params(z["params"])
+
+    def train_step(self, u0, ut, vt, lr=1e-3, stream=None):
+        """Forward, backward and (lr > 0) one Adam step; returns the loss (mean squared error per pixel)."""
+        a, b, c = _dev(u0, np.complex64), _dev(ut, np.complex64), _dev(vt, np.complex64)
+        B, H, W = a.shape
+        loss = ctypes.c_double()
+        check(lib.pdt_cnn_train_step(self._h, a.ptr, b.ptr, c.ptr, B, H, W, float(lr), _lib.stream_handle(stream),
+                                     ctypes.byref(loss)))
+        return loss.value
+
+    def predict(self, u0, u_out, v_out, stream=None):
+        a = _dev(u0, np.complex64)
+        B, H, W = a.shape
+        check(lib.pdt_cnn_predict(self._h, a.ptr, B, H, W, _dev(u_out, np.complex64).ptr,
+                                  _dev(v_out, np.complex64).ptr, _lib.stream_handle(stream)))
+
+
+def warm_start(optimizer, net, u0, torch, stream=None):
+    """Starts `optimizer` (a TGV-MRI optimizer with operator and data set) from the network's (u, v) when
+    that start has the lower FP64 TGV energy, else from the plain start (u0 = A^H f, v = 0). u0 is the
+    device image A^H f, shape (H, W). Returns {'used': 'network' | 'plain', 'energy_network', 'energy_plain'}."""
+    H, W = u0.shape
+    u = torch.empty((1, H, W), dtype=torch.complex64, device=u0.device)
+    v = torch.empty((1, 2, H, W), dtype=torch.complex64, device=u0.device)
+    net.predict(u0.reshape(1, H, W), u, v, stream=stream)
+    optimizer.setInput0(u0, stream=stream)
+    e_plain = optimizer.energy(stream=stream)["total"]
+    optimizer.setInput0UV(u[0], v[0], stream=stream)
+    e_net = optimizer.energy(stream=stream)["total"]
+    if e_net <= e_plain:
+        return {"used": "network", "energy_network": e_net, "energy_plain": e_plain}
+    optimizer.setInput0(u0, stream=stream)
+    return {"used": "plain", "energy_network": e_net, "energy_plain": e_plain}
+
+
+def make_training_set(pdt, torch, n_cases, iters, seed0=1000, C=15, H=640, W=368, roos=True, accel=4,
+                      batch=16, log=print):
+    """(u0, u*, v*) device tensors of n_cases synthetic problems; u* = TGV solution at fixed alpha after
+    `iters` iterations from u0 = A^H f, computed `batch` problems at a time."""
+    from . import synthetic
+
+    Hi = H // 2 if roos else H
+    U0 = torch.empty((n_cases, Hi, W), dtype=torch.complex64, device="cuda")
+    UT = torch.empty_like(U0)
+    VT = torch.empty((n_cases, 2, Hi, W), dtype=torch.complex64, device="cuda")
+    t0 = time.time()
+    for start in range(0, n_cases, batch):
+        opts, keep = [], []
+        for i in range(start, min(n_cases, start + batch)):
+            case = synthetic.cartesian_case(C=C, H=H, W=W, roos=roos, accel=accel, seed=seed0 + i,
+                                            mask_kind="random" if i % 2 == 0 else "regular")
+            op = (pdt.mri.MriCartesianRemoveROOSOperator if roos else pdt.mri.MriCartesianOperator)()
+            op.setCoilSens(case["sens"])
+            op.setMask(case["mask"])
+            opt = pdt.mri.TgvMriOptimizer_2c3c()
+            prm = opt.getParameters()
+            prm.max_iter, prm.reduction, prm.alpha1 = iters - 1, 1.0, case["alpha1"]
+            prm.alpha0 = 2 * prm.alpha1
+            opt.setOperator(op)
+            f = torch.from_numpy(case["rawdata"]).cuda()
+            opt.setNoisyData(f)
+            op.adjoint(f, out=U0[i])
+            opt.setInput0(U0[i])
+            opts.append((i, opt))
+            keep.append((op, f))
+        pdt.batch.BatchSolver([o for _, o in opts]).solve()
+        for i, opt in opts:
+            opt.getResult(out=UT[i])
+            opt.getField("vx", out=VT[i, 0])
+            opt.getField("vy", out=VT[i, 1])
+        torch.cuda.synchronize()
+        log(f"targets {min(n_cases, start + batch)}/{n_cases}  {time.time() - t0:.1f}s")
+    return U0, UT, VT
+
+
+def train(net, U0, UT, VT, epochs=10, batch=8, lr=1e-3, seed=0, log=print):
+    """Adam on mini-batches (shuffled per epoch); returns the per-epoch mean losses."""
+    rng = np.random.default_rng(seed)
+    n = U0.shape[0]
+    losses = []
+    for ep in range(epochs):
+        order = rng.permutation(n)
+        tot, cnt = 0.0, 0
+        lr_ep = lr * (0.5 ** (ep // max(1, epochs // 3)))
+        for s in range(0, n - batch + 1, batch):
+            idx = order[s:s + batch].tolist()
+            tot += net.train_step(U0[idx].contiguous(), UT[idx].contiguous(), VT[idx].contiguous(), lr=lr_ep)
+            cnt += 1
+        losses.append(tot / max(cnt, 1))
+        log(f"epoch {ep}: loss {losses[-1]:.3e}")
+    return losses
+
+
+def main():
+    import torch
+
+    import primaldualtoolbox as pdt
+
+    ap = argparse.ArgumentParser(description="train the warm-start network on engine-generated TGV solutions")
+    ap.add_argument("--cases", type=int, default=256)
+    ap.add_argument("--iters", type=int, default=3000)
+    ap.add_argument("--epochs", type=int, default=12)
+    ap.add_argument("--batch", type=int, default=8)
+    ap.add_argument("--lr", type=float, default=1e-3)
+    ap.add_argument("--out", default=DEFAULT_WEIGHTS)
+    args = ap.parse_args()
+    t0 = time.time()
+    U0, UT, VT = make_training_set(pdt, torch, args.cases, args.iters)
+    t_data = time.time() - t0
+    net = WarmStartNet(seed=0)
+    t1 = time.time()
+    losses = train(net, U0, UT, VT, epochs=args.epochs, batch=args.batch, lr=args.lr)
+    torch.cuda.synchronize()
+    t_train = time.time() - t1
+    net.save(args.out, cases=args.cases, target_iters=args.iters, epochs=args.epochs, batch=args.batch, lr=args.lr,
+             losses=losses, data_seconds=t_data, train_seconds=t_train, shape=[15, 640, 368], accel=4)
+    print(json.dumps({"out": args.out, "losses": losses, "data_s": round(t_data, 1), "train_s": round(t_train, 1)}))
+
+
+if __name__ == "__main__":
+    main()

@@ -253,3 +253,27 @@ def test_solve_is_deterministic_and_resumable(pdt):
     assert np.array_equal(a, b)  # bitwise reproducible
     c = run([25, 35])  # state persists across solve() calls (alpha constant at reduction 1)
     assert rel_l2(c, a) <= 1e-6
+
+
+def test_consecutive_solves_with_changing_max_iter(pdt, oracle):
+    """Three solve() calls on one optimizer with a growing then shrinking alpha schedule (each call restarts
+    the continuation over its own max_iter and continues every primal and dual variable), against the FP32
+    oracle run the same way. Every call runs at least one captured 20-iteration graph."""
+    case = _cart_case(C=4, H=64, W=48, roos=True, seed=6)
+    op = pdt.mri.MriCartesianRemoveROOSOperator()
+    op.setCoilSens(case["sens"])
+    op.setMask(case["mask"])
+    opt = pdt.mri.TgvMriOptimizer_2c3c()
+    prm = opt.getParameters()
+    prm.alpha1, prm.alpha0, prm.reduction = case["alpha1"], case["alpha0"], 0.3
+    opt.setOperator(op)
+    opt.setNoisyData(case["rawdata"])
+    state = None
+    for max_iter in (29, 71, 23):
+        prm.max_iter = max_iter
+        opt.solve()
+        ref, state = oracle.op_solve("cartesian_roos", case["sens"], case["mask"], case["rawdata"], "tgv_mri",
+                                     alpha0=float(np.float32(case["alpha0"])),
+                                     alpha1=float(np.float32(case["alpha1"])), reduction=float(np.float32(0.3)),
+                                     max_iter=max_iter, prec=32, return_state=True, state=state)
+        assert rel_l2(opt.getResult(), ref) <= SOLVE_TOL, max_iter

@@ -144,3 +144,18 @@ def test_reference_masks_are_line_masks(oracle):
     Au = oracle.op_apply("sampling", None, m, u)
     Atp = oracle.op_apply("sampling", None, m, p, adjoint=True)
     assert abs(np.vdot(p, Au) - np.vdot(Atp, u)) / (np.linalg.norm(Au) * np.linalg.norm(p)) < 1e-12
+
+
+def test_op_solve_continues_from_state(oracle):
+    # at reduction 1 two solves of 10 and 20 iterations are the 30-iteration solve (up to the rounding of
+    # exp(log alpha) in the schedule, which depends on max_iter)
+    from primaldualtoolbox import synthetic
+
+    case = synthetic.cartesian_case(C=2, H=32, W=24, roos=True, seed=7)
+    args = ("cartesian_roos", case["sens"], case["mask"], case["rawdata"], "tgv_mri")
+    kw = dict(alpha0=case["alpha0"], alpha1=case["alpha1"], reduction=1.0, prec=64)
+    _, st = oracle.op_solve(*args, max_iter=9, return_state=True, **kw)
+    u2 = oracle.op_solve(*args, max_iter=19, state=st, **kw)
+    u = oracle.op_solve(*args, max_iter=29, **kw)
+    assert rel_l2(u2, u) < 1e-12
+    assert rel_l2(oracle.op_solve(*args, max_iter=19, **kw), u) > 1e-3  # the state did carry over
