@@ -16,6 +16,15 @@ constexpr int kRedBlocks = 592;  // 4 x 148-152 SMs
 
 __device__ __forceinline__ double dabs2(float2 a) { return (double)a.x * a.x + (double)a.y * a.y; }
 __device__ __forceinline__ double dabs2(float a) { return (double)a * a; }
+// |a - b|^2 with the difference taken in double (exact for FP32 inputs)
+__device__ __forceinline__ double ddist2(float2 a, float2 b) {
+  const double dx = (double)a.x - (double)b.x, dy = (double)a.y - (double)b.y;
+  return dx * dx + dy * dy;
+}
+__device__ __forceinline__ double ddist2(float a, float b) {
+  const double d = (double)a - (double)b;
+  return d * d;
+}
 
 __device__ double block_sum(double v) {
   __shared__ double sh[kRedThreads / 32];
@@ -36,9 +45,7 @@ __global__ void __launch_bounds__(kRedThreads) dist2_kernel(const P* __restrict_
                                                             size_t n, double* __restrict__ partial) {
   double s = 0;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-    P d = a[i];
-    if (b) d = d - b[i];
-    s += dabs2(d);
+    s += b ? ddist2(a[i], b[i]) : dabs2(a[i]);
   }
   s = block_sum(s);
   if (threadIdx.x == 0) partial[blockIdx.x] = s;
