@@ -20,6 +20,8 @@
 #include <algorithm>
 #include <array>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <functional>
 #include <map>
@@ -553,6 +555,7 @@ class CartesianOp : public OpImpl, public SolverHooks {
   // (W, H, coils, sampled columns).
   void autotune() {
     if (!frow_.ok() && !fcol_.ok()) return;
+    if (pinned_tune()) return;
     static std::mutex g_tune_mu;
     static std::map<std::array<int, 6>, std::pair<Tune, int>> g_tune_cache;
     const std::array<int, 6> key = {dev_.W, dev_.Hf, dev_.Hi, dev_.C, dev_.ns, dev_.sens ? 1 : 0};
@@ -581,16 +584,21 @@ class CartesianOp : public OpImpl, public SolverHooks {
     PDT_CUDA_CHECK(cudaEventCreate(&e0));
     PDT_CUDA_CHECK(cudaEventCreate(&e1));
     // a candidate whose launch is rejected (e.g. a cluster shape the device cannot schedule) is skipped
+    // the best of three batches of ten launches (after one warm-up launch)
     auto time = [&](const std::function<void()>& fn) {
       try {
-        fn();  // warm-up
-        PDT_CUDA_CHECK(cudaEventRecord(e0, st));
-        for (int i = 0; i < 5; ++i) fn();
-        PDT_CUDA_CHECK(cudaEventRecord(e1, st));
-        PDT_CUDA_CHECK(cudaEventSynchronize(e1));
-        float ms = 0;
-        PDT_CUDA_CHECK(cudaEventElapsedTime(&ms, e0, e1));
-        return ms;
+        fn();
+        float best = 1e30f;
+        for (int rep = 0; rep < 3; ++rep) {
+          PDT_CUDA_CHECK(cudaEventRecord(e0, st));
+          for (int i = 0; i < 10; ++i) fn();
+          PDT_CUDA_CHECK(cudaEventRecord(e1, st));
+          PDT_CUDA_CHECK(cudaEventSynchronize(e1));
+          float ms = 0;
+          PDT_CUDA_CHECK(cudaEventElapsedTime(&ms, e0, e1));
+          best = std::min(best, ms);
+        }
+        return best;
       } catch (const Error&) {
         cudaGetLastError();
         PDT_CUDA_CHECK(cudaDeviceSynchronize());  // a sticky error surfaces here and fails the operator
@@ -637,6 +645,29 @@ class CartesianOp : public OpImpl, public SolverHooks {
     tune_ = best;
     std::lock_guard<std::mutex> lock(g_tune_mu);
     g_tune_cache[key] = {tune_, G_};
+  }
+
+  // PDT_CARTESIAN_TUNE="wf,wc,wa,groups,cluster" (warps per block of rows_fwd, cols, rows_adj; coil
+  // groups; 1 = cluster reduction) replaces the autotuner, e.g. to profile one fixed configuration.
+  bool pinned_tune() {
+    const char* env = std::getenv("PDT_CARTESIAN_TUNE");
+    if (!env || !*env) return false;
+    int v[5];
+    if (std::sscanf(env, "%d,%d,%d,%d,%d", &v[0], &v[1], &v[2], &v[3], &v[4]) != 5)
+      throw Error(PDT_ERR_INVALID_ARGUMENT, "PDT_CARTESIAN_TUNE: expected wf,wc,wa,groups,cluster");
+    auto idx = [&](int w) {
+      for (int i = 0; i < 3; ++i)
+        if (kWpbChoices[i] == w) return i;
+      throw Error(PDT_ERR_INVALID_ARGUMENT, "PDT_CARTESIAN_TUNE: warps per block must be 2, 4 or 8");
+    };
+    tune_.wf = idx(v[0]);
+    tune_.wc = idx(v[1]);
+    tune_.wa = idx(v[2]);
+    tune_.cluster = v[4] != 0;
+    if (v[3] < 1 || v[3] > std::min(dev_.C, 16) || (tune_.cluster && (v[3] < 2 || v[3] > 8)))
+      throw Error(PDT_ERR_INVALID_ARGUMENT, "PDT_CARTESIAN_TUNE: coil groups out of range for this operator");
+    G_ = v[3];
+    return true;
   }
 
   bool prepared_ = false;

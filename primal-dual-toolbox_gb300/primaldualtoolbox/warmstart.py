@@ -132,22 +132,43 @@ def warm_start(optimizer, net, u0, torch, stream=None):
     return {"used": "plain", "energy_network": e_net, "energy_plain": e_plain}
 
 
-def make_training_set(pdt, torch, n_cases, iters, seed0=1000, C=15, H=640, W=368, roos=True, accel=4,
-                      batch=16, log=print):
-    """(u0, u*, v*) device tensors of n_cases synthetic problems; u* = TGV solution at fixed alpha after
-    `iters` iterations from u0 = A^H f, computed `batch` problems at a time."""
+def _case(kw):
     from . import synthetic
+
+    return synthetic.cartesian_case(**kw)
+
+
+def make_training_set(pdt, torch, n_cases, iters, seed0=1000, C=15, H=640, W=368, roos=True, accel=4,
+                      batch=16, workers=None, log=print):
+    """(u0, u*, v*) device tensors of n_cases synthetic problems; u* = TGV solution at fixed alpha after
+    `iters` iterations from u0 = A^H f, computed `batch` problems at a time. The synthetic cases are
+    generated by a pool of `workers` host processes (spawned, so no process inherits a CUDA context)
+    while the GPU solves the previous batch."""
+    import concurrent.futures
+    import multiprocessing
 
     Hi = H // 2 if roos else H
     U0 = torch.empty((n_cases, Hi, W), dtype=torch.complex64, device="cuda")
     UT = torch.empty_like(U0)
     VT = torch.empty((n_cases, 2, Hi, W), dtype=torch.complex64, device="cuda")
+    kws = [dict(C=C, H=H, W=W, roos=roos, accel=accel, seed=seed0 + i,
+                mask_kind="random" if i % 2 == 0 else "regular") for i in range(n_cases)]
+    workers = workers or max(1, min(16, (os.cpu_count() or 2) - 1))
+    pool = concurrent.futures.ProcessPoolExecutor(workers, mp_context=multiprocessing.get_context("spawn"))
+    cases = pool.map(_case, kws, chunksize=1)
     t0 = time.time()
+    try:
+        _solve_batches(pdt, torch, cases, n_cases, iters, roos, batch, U0, UT, VT, t0, log)
+    finally:
+        pool.shutdown(cancel_futures=True)
+    return U0, UT, VT
+
+
+def _solve_batches(pdt, torch, cases, n_cases, iters, roos, batch, U0, UT, VT, t0, log):
     for start in range(0, n_cases, batch):
         opts, keep = [], []
         for i in range(start, min(n_cases, start + batch)):
-            case = synthetic.cartesian_case(C=C, H=H, W=W, roos=roos, accel=accel, seed=seed0 + i,
-                                            mask_kind="random" if i % 2 == 0 else "regular")
+            case = next(cases)
             op = (pdt.mri.MriCartesianRemoveROOSOperator if roos else pdt.mri.MriCartesianOperator)()
             op.setCoilSens(case["sens"])
             op.setMask(case["mask"])
@@ -169,7 +190,6 @@ def make_training_set(pdt, torch, n_cases, iters, seed0=1000, C=15, H=640, W=368
             opt.getField("vy", out=VT[i, 1])
         torch.cuda.synchronize()
         log(f"targets {min(n_cases, start + batch)}/{n_cases}  {time.time() - t0:.1f}s")
-    return U0, UT, VT
 
 
 def train(net, U0, UT, VT, epochs=10, batch=8, lr=1e-3, seed=0, log=print):
@@ -201,19 +221,39 @@ def main():
     ap.add_argument("--epochs", type=int, default=12)
     ap.add_argument("--batch", type=int, default=8)
     ap.add_argument("--lr", type=float, default=1e-3)
+    ap.add_argument("--held-out", type=int, default=16)
     ap.add_argument("--out", default=DEFAULT_WEIGHTS)
     args = ap.parse_args()
     t0 = time.time()
     U0, UT, VT = make_training_set(pdt, torch, args.cases, args.iters)
     t_data = time.time() - t0
+    # held-out problems (other seeds) for the report
+    H0, HT, HV = make_training_set(pdt, torch, args.held_out, args.iters, seed0=500000)
     net = WarmStartNet(seed=0)
     t1 = time.time()
     losses = train(net, U0, UT, VT, epochs=args.epochs, batch=args.batch, lr=args.lr)
     torch.cuda.synchronize()
     t_train = time.time() - t1
+    held = evaluate(net, torch, H0, HT)
     net.save(args.out, cases=args.cases, target_iters=args.iters, epochs=args.epochs, batch=args.batch, lr=args.lr,
-             losses=losses, data_seconds=t_data, train_seconds=t_train, shape=[15, 640, 368], accel=4)
-    print(json.dumps({"out": args.out, "losses": losses, "data_s": round(t_data, 1), "train_s": round(t_train, 1)}))
+             losses=losses, data_seconds=t_data, train_seconds=t_train, shape=[15, 640, 368], accel=4,
+             held_out=held)
+    print(json.dumps({"out": args.out, "losses": losses, "data_s": round(t_data, 1), "train_s": round(t_train, 1),
+                      "held_out": held}))
+
+
+def evaluate(net, torch, U0, UT):
+    """Mean rel-L2 distance to the targets of the network's u and of the plain start u0."""
+    n, H, W = U0.shape
+    u = torch.empty((1, H, W), dtype=torch.complex64, device=U0.device)
+    v = torch.empty((1, 2, H, W), dtype=torch.complex64, device=U0.device)
+    e_net, e_plain = [], []
+    for i in range(n):
+        net.predict(U0[i:i + 1].contiguous(), u, v)
+        t = UT[i]
+        e_net.append(float(torch.linalg.vector_norm(u[0] - t) / torch.linalg.vector_norm(t)))
+        e_plain.append(float(torch.linalg.vector_norm(U0[i] - t) / torch.linalg.vector_norm(t)))
+    return {"cases": n, "rel_l2_network": float(np.mean(e_net)), "rel_l2_plain": float(np.mean(e_plain))}
 
 
 if __name__ == "__main__":
