@@ -1,10 +1,22 @@
-// pdt_cart_fast.cuh -- register-FFT kernels of the Cartesian operator for even W and H with a
-// compile-time two-level split (W = A * B, A, B <= 32). One warp owns one sequence (an image row or a
-// k-space column): lanes < A run the first-level B-point FFTs in registers, lanes < B the second-level
-// A-point FFTs, exchanging once through the warp's own shared-memory tile. The column kernel runs
-// forward FFT, mask, k-space dual prox and inverse FFT with two exchanges, because the inverse starts
-// from the registers the forward leaves (the shifts cancel for even H: slot k of the forward output is
-// slot k of the inverse input). Included by pdt_cartesian.cu after CartDev.
+// pdt_cart_fast.cuh -- lane-distributed FFT kernels of the Cartesian operator for the lengths with a
+// compiled split n = M * L (L = 8, 16 or 32 lanes per sequence, M values per lane). Included by
+// pdt_cartesian.cu after CartDev.
+//
+// LaneFft<M, L>: lane t of a group of L lanes holds x[t + L j] (j < M) in registers. The forward
+// transform is an M-point register FFT per lane, a twiddle w_n^(t k1), and an L-point FFT across the
+// lanes (radix-2 decimation in frequency, one __shfl_xor_sync butterfly per stage and value):
+//   X[k1 + M k2] = sum_t w_L^(t k2) w_n^(t k1) sum_j w_M^(j k1) x[t + L j]
+// leaving X[k1 + M brev_L(t)] in register k1 of lane t. The inverse runs the same network backwards
+// (decimation in time) with conjugate twiddles, from that order back to natural order. Every lane
+// works in every stage and no shared-memory exchange is needed.
+//
+// Kernels (one sequence per lane group; 32 / L sequences per warp):
+//   fl_rows_fwd   rows of ubar . sens_c -> FFT along W -> sampled columns t1[c][s][yi]
+//   fl_cols       per sampled column: FFT along Hf -> mask -> k-space dual prox -> mask -> IFFT along Hf
+//   fl_rows_adj   per row block and coil group: IFFT along W -> conj(sens_c) . -> coil sum
+// The k-space arrays of the column phase (dual r, data f, mask) are stored per sampled column in the
+// order the transform leaves them: position P = k1 * L + t holds spectrum index k1 + M brev_L(t), so
+// that lanes read and write consecutive addresses. CartDev::kperm maps P to the output row.
 #pragma once
 
 #include <cooperative_groups.h>
@@ -16,189 +28,240 @@ namespace cg = cooperative_groups;
 namespace pdt {
 namespace {
 
-constexpr int kMaxWarps = 8;  // largest warps-per-block instance (one sequence per warp)
+constexpr int ct_log2(int n) { return n <= 1 ? 0 : 1 + ct_log2(n / 2); }
 
-// Phase 1 (fast): rows of ubar . sens_c -> FFT along W -> sampled columns t1[c][s][yi].
-template <int A, int B, int WPB>
-__global__ void __launch_bounds__(32 * WPB) fr_rows_fwd(CartDev d, const float2* __restrict__ ubar,
-                                                               float2* __restrict__ t1, int* __restrict__ tick) {
-  using TL = TwoLevel<A, B>;
+__device__ __forceinline__ float2 shfl_xor2(float2 v, int m) {
+  return c2(__shfl_xor_sync(0xffffffffu, v.x, m), __shfl_xor_sync(0xffffffffu, v.y, m));
+}
+
+// bit reversal of t over log2(L) bits
+template <int L>
+__device__ __forceinline__ int lane_brev(int t) {
+  return (int)(__brev((unsigned)t) >> (32 - ct_log2(L)));
+}
+
+template <int M, int L>
+struct LaneFft {
+  static_assert(L == 8 || L == 16 || L == 32, "lanes per sequence");
+  static constexpr int n = M * L;
+
+  // Forward: v[j] = x[t + L j] on entry; v[k1] = X[k1 + M brev_L(t)] on exit. tw[i] = exp(-2 pi i i / n).
+  static __device__ __forceinline__ void fwd(float2 (&v)[M], int t, const float2* __restrict__ tw) {
+    reg_fft<M, L>(v, tw, -1.f);
+#pragma unroll
+    for (int k1 = 1; k1 < M; ++k1) v[k1] = cmul(v[k1], tw[t * k1]);  // t k1 < n
+#pragma unroll
+    for (int h = L / 2; h >= 1; h >>= 1) {
+      const bool up = (t & h) != 0;
+      const float2 w = tw[(t & (h - 1)) * (n / (2 * h))];  // w_2h^(t mod h)
+#pragma unroll
+      for (int k1 = 0; k1 < M; ++k1) {
+        const float2 p = shfl_xor2(v[k1], h);
+        v[k1] = up ? cmul(p - v[k1], w) : v[k1] + p;
+      }
+    }
+  }
+
+  // Unnormalised inverse: v[k1] = Z[k1 + M brev_L(t)] on entry; v[j] = n z[t + L j] on exit.
+  static __device__ __forceinline__ void inv(float2 (&v)[M], int t, const float2* __restrict__ tw) {
+#pragma unroll
+    for (int h = 1; h < L; h <<= 1) {
+      const bool up = (t & h) != 0;
+      const float2 w = conjf2(tw[(t & (h - 1)) * (n / (2 * h))]);
+#pragma unroll
+      for (int k1 = 0; k1 < M; ++k1) {
+        const float2 m = up ? cmul(v[k1], w) : v[k1];
+        const float2 p = shfl_xor2(m, h);
+        v[k1] = up ? p - m : m + p;
+      }
+    }
+#pragma unroll
+    for (int k1 = 1; k1 < M; ++k1) v[k1] = cmul(v[k1], conjf2(tw[t * k1]));
+    reg_fft<M, L>(v, tw, 1.f);
+  }
+};
+
+// Phase 1: rows of ubar . sens_c -> FFT along W -> sampled columns t1[c][s][yi]. A block takes
+// R = WPB * 32 / L consecutive rows of one coil and writes each sampled column's R rows as one run.
+template <int M, int L, int WPB>
+__global__ void __launch_bounds__(32 * WPB) fl_rows_fwd(CartDev d, const float2* __restrict__ ubar,
+                                                        float2* __restrict__ t1, int* __restrict__ tick) {
+  using F = LaneFft<M, L>;
+  constexpr int W = F::n, R = WPB * (32 / L);
   extern __shared__ float2 sm[];
   float2* tw = sm;
-  float2* ex = tw + TL::n;
-  float2* stage = ex + WPB * TL::xch;
-  int* fs2s = reinterpret_cast<int*>(stage + (size_t)d.ns * WPB);
+  float2* stage = tw + W;  // [ns][R]
+  int* fs2s = reinterpret_cast<int*>(stage + (size_t)d.ns * R);
   if (tick && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) atomicAdd(tick, 1);
-  for (int i = threadIdx.x; i < TL::n; i += blockDim.x) {
+  for (int i = threadIdx.x; i < W; i += blockDim.x) {
     tw[i] = d.twW[i];
     fs2s[i] = d.fslot2s[i];
   }
   __syncthreads();
-  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int yi0 = blockIdx.x * WPB, yi = yi0 + w, c = blockIdx.y;
-  float2* myex = ex + w * TL::xch;
-  const bool ok = yi < d.Hi;
-  if (ok && lane < A) {
-    float2 v[B];
-    const float2* urow = ubar + (size_t)yi * TL::n;
-    const float2* srow = d.sens ? d.sens + ((size_t)c * d.Hf + yi + d.y0) * TL::n : nullptr;
+  const int lane = threadIdx.x & 31, t = lane & (L - 1);
+  const int r = (threadIdx.x >> 5) * (32 / L) + lane / L;
+  const int yi0 = blockIdx.x * R, c = blockIdx.y;
+  const int nr = min(R, d.Hi - yi0);
+  const bool ok = r < nr;
+  const int yi = yi0 + (ok ? r : 0);  // a group past the last row transforms row yi0 and discards it
+  const float2* urow = ubar + (size_t)yi * W;
+  const float2* srow = d.sens ? d.sens + ((size_t)c * d.Hf + yi + d.y0) * W : nullptr;
+  float2 v[M];
 #pragma unroll
-    for (int b = 0; b < B; ++b) {
-      int x = lane + A * b - d.mxW;  // FFT slot j holds image column (j - mid) mod W
-      if (x < 0) x += TL::n;
-      float2 val = urow[x];
-      if (srow) val = cmul(val, srow[x]);
-      v[b] = val;
-    }
-    TL::fwd_step1(v, lane, myex, tw);
+  for (int j = 0; j < M; ++j) {
+    int x = t + L * j - d.mxW;  // FFT slot t + L j holds image column (slot - mid) mod W
+    if (x < 0) x += W;
+    float2 val = urow[x];
+    if (srow) val = cmul(val, srow[x]);
+    v[j] = val;
   }
-  __syncwarp();
-  if (ok && lane < B) {
-    float2 u[A];
-    TL::fwd_step2(u, lane, myex, tw);
+  F::fwd(v, t, tw);
+  if (ok) {
+    const int kb = M * lane_brev<L>(t);
 #pragma unroll
-    for (int ka = 0; ka < A; ++ka) {
-      const int s = fs2s[lane + B * ka];
-      if (s >= 0) stage[s * WPB + w] = u[ka];
+    for (int k1 = 0; k1 < M; ++k1) {
+      const int s = fs2s[k1 + kb];
+      if (s >= 0) stage[s * R + r] = v[k1];
     }
   }
   __syncthreads();
-  const int nr = min(WPB, d.Hi - yi0);
   for (int i = threadIdx.x; i < d.ns * nr; i += blockDim.x) {
-    const int s = i / nr, r = i - s * nr;
-    t1[((size_t)c * d.ns + s) * d.Hi + yi0 + r] = stage[s * WPB + r];
+    const int s = i / nr, rr = i - s * nr;
+    t1[((size_t)c * d.ns + s) * d.Hi + yi0 + rr] = stage[s * R + rr];
   }
 }
 
-// Phase 2 (fast): per sampled column, FFT along H -> mask -> (prox) -> mask -> IFFT along H.
-template <int A, int B, int WPB>
-__global__ void __launch_bounds__(32 * WPB) fr_cols(CartDev d, int mode, const float2* t_in, float2* t_out,
-                                                           float2* __restrict__ r, const float2* __restrict__ fc,
-                                                           const float2* __restrict__ kin, float2* __restrict__ kout,
-                                                           float sigma, float lambda) {
-  using TL = TwoLevel<A, B>;
+// Phase 2: per sampled column, FFT along Hf -> mask -> (k-space dual prox) -> mask -> IFFT along Hf.
+// r, fc and the mask are in the transform order (position k1 * L + t of the column).
+template <int M, int L, int WPB>
+__global__ void __launch_bounds__(32 * WPB) fl_cols(CartDev d, int mode, const float2* t_in, float2* t_out,
+                                                    float2* __restrict__ r, const float2* __restrict__ fc,
+                                                    const float2* __restrict__ kin, float2* __restrict__ kout,
+                                                    float sigma, float lambda) {
+  using F = LaneFft<M, L>;
+  constexpr int Hf = F::n;
   extern __shared__ float2 sm[];
   float2* tw = sm;
-  float2* ex = tw + TL::n;
-  for (int i = threadIdx.x; i < TL::n; i += blockDim.x) tw[i] = d.twH[i];
+  for (int i = threadIdx.x; i < Hf; i += blockDim.x) tw[i] = d.twH[i];
   __syncthreads();
-  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int s = blockIdx.x * WPB + w, c = blockIdx.y;
-  const bool ok = s < d.ns;
-  float2* myex = ex + w * TL::xch;
-  constexpr int Hf = TL::n;
-  const size_t colc = ((size_t)c * d.ns + s);
-  float2 u[A];
+  const int lane = threadIdx.x & 31, t = lane & (L - 1);
+  const int s0 = (blockIdx.x * WPB + (threadIdx.x >> 5)) * (32 / L) + lane / L;
+  const int c = blockIdx.y;
+  const bool ok = s0 < d.ns;
+  const int s = ok ? s0 : d.ns - 1;  // a group past the last column reads column ns-1 and discards it
+  const size_t colc = (size_t)c * d.ns + s;
+  const int kb = M * lane_brev<L>(t);
+  const float* mrow = d.maskc + (size_t)s * Hf;
+  float2 v[M];
   if (mode == COL_SOLVE || mode == COL_FWD_DENSE) {
-    if (ok && lane < A) {
-      float2 v[B];
 #pragma unroll
-      for (int b = 0; b < B; ++b) {
-        int yf = lane + A * b - d.mxH;
-        if (yf < 0) yf += Hf;
-        const int yi = yf - d.y0;
-        v[b] = (yi >= 0 && yi < d.Hi) ? t_in[colc * d.Hi + yi] : c2(0.f, 0.f);
-      }
-      TL::fwd_step1(v, lane, myex, tw);
+    for (int j = 0; j < M; ++j) {
+      int yf = t + L * j - d.mxH;
+      if (yf < 0) yf += Hf;
+      const int yi = yf - d.y0;
+      v[j] = (yi >= 0 && yi < d.Hi) ? t_in[colc * d.Hi + yi] : c2(0.f, 0.f);
     }
-    __syncwarp();
-    if (ok && lane < B) {
-      TL::fwd_step2(u, lane, myex, tw);
-      const float* mrow = d.maskc + (size_t)s * Hf;
-      // chunks of loads -> math -> stores: r is read and written in place, so the compiler cannot hoist
-      // a later load above an earlier store; batching keeps CH loads in flight per lane
-      constexpr int CH = A < 8 ? A : 8;
+    F::fwd(v, t, tw);
+    if (mode == COL_FWD_DENSE) {
+      if (ok) {
 #pragma unroll
-      for (int k0 = 0; k0 < A; k0 += CH) {
-        int yp[CH];
-        float m[CH];
-        float2 fv[CH], rv[CH];
-#pragma unroll
-        for (int q = 0; q < CH; ++q) {
-          int ypos = lane + B * (k0 + q) + d.oyH;
+        for (int k1 = 0; k1 < M; ++k1) {
+          int ypos = k1 + kb + d.oyH;
           if (ypos >= Hf) ypos -= Hf;
-          yp[q] = ypos;
-          m[q] = mrow[ypos];
-        }
-        if (mode == COL_FWD_DENSE) {
-#pragma unroll
-          for (int q = 0; q < CH; ++q)
-            kout[((size_t)c * Hf + yp[q]) * d.W + d.col_x[s]] = u[k0 + q] * (d.scale * m[q]);
-        } else {
-#pragma unroll
-          for (int q = 0; q < CH; ++q) {
-            fv[q] = fc[colc * Hf + yp[q]];
-            rv[q] = r[colc * Hf + yp[q]];
-          }
-#pragma unroll
-          for (int q = 0; q < CH; ++q) {
-            const float2 kv = u[k0 + q] * (d.scale * m[q]);
-            rv[q] = (rv[q] + sigma * (kv - fv[q])) / (1.0f + sigma * lambda);
-            u[k0 + q] = rv[q] * m[q];
-          }
-#pragma unroll
-          for (int q = 0; q < CH; ++q) r[colc * Hf + yp[q]] = rv[q];
+          kout[((size_t)c * Hf + ypos) * d.W + d.col_x[s]] = v[k1] * (d.scale * mrow[k1 * L + t]);
         }
       }
+      return;
     }
-    if (mode == COL_FWD_DENSE) return;
-    __syncwarp();
-  } else if (ok && lane < B) {
-    const float* mrow = d.maskc + (size_t)s * Hf;
+    // chunks of loads -> math -> stores (r is read and written in place)
+    constexpr int CH = M < 8 ? M : 8;
+    const float2* fcol = fc + colc * Hf;
+    float2* rcol = r + colc * Hf;
 #pragma unroll
-    for (int ka = 0; ka < A; ++ka) {
-      int ypos = lane + B * ka + d.oyH;
-      if (ypos >= Hf) ypos -= Hf;
-      const float2 v = (mode == COL_ADJ_DENSE) ? kin[((size_t)c * Hf + ypos) * d.W + d.col_x[s]] : fc[colc * Hf + ypos];
-      u[ka] = v * mrow[ypos];
+    for (int k0 = 0; k0 < M; k0 += CH) {
+      float m[CH];
+      float2 fv[CH], rv[CH];
+#pragma unroll
+      for (int q = 0; q < CH; ++q) {
+        if (k0 + q < M) {
+          const int P = (k0 + q) * L + t;
+          m[q] = mrow[P];
+          fv[q] = fcol[P];
+          rv[q] = rcol[P];
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < CH; ++q) {
+        if (k0 + q < M) {
+          const float2 kv = v[k0 + q] * (d.scale * m[q]);
+          rv[q] = (rv[q] + sigma * (kv - fv[q])) / (1.0f + sigma * lambda);
+          v[k0 + q] = rv[q] * m[q];
+        }
+      }
+      if (ok) {
+#pragma unroll
+        for (int q = 0; q < CH; ++q)
+          if (k0 + q < M) rcol[(k0 + q) * L + t] = rv[q];
+      }
+    }
+  } else {
+#pragma unroll
+    for (int k1 = 0; k1 < M; ++k1) {
+      float2 val;
+      if (mode == COL_ADJ_DENSE) {
+        int ypos = k1 + kb + d.oyH;
+        if (ypos >= Hf) ypos -= Hf;
+        val = kin[((size_t)c * Hf + ypos) * d.W + d.col_x[s]];
+      } else {
+        val = fc[colc * Hf + k1 * L + t];
+      }
+      v[k1] = val * mrow[k1 * L + t];
     }
   }
-  if (ok && lane < B) TL::inv_step1(u, lane, myex, tw);
-  __syncwarp();
-  if (ok && lane < A) {
-    float2 v[B];
-    TL::inv_step2(v, lane, myex, tw);
+  F::inv(v, t, tw);
+  if (ok) {
 #pragma unroll
-    for (int b = 0; b < B; ++b) {
-      int yf = lane + A * b + d.oyH;
+    for (int j = 0; j < M; ++j) {
+      int yf = t + L * j + d.oyH;
       if (yf >= Hf) yf -= Hf;
       const int yi = yf - d.y0;
-      if (yi >= 0 && yi < d.Hi) t_out[colc * d.Hi + yi] = v[b] * d.scale;
+      if (yi >= 0 && yi < d.Hi) t_out[colc * d.Hi + yi] = v[j] * d.scale;
     }
   }
 }
 
-// Phase 3 (fast): per image row block, IFFT along W of the sampled columns, conj(sens_c) multiply and
-// the coil sum. A cluster of G blocks shares the row block, each block taking one coil group and
-// accumulating in its shared memory; the blocks then reduce the G partial rows through distributed
-// shared memory in rank order (deterministic) and write one K^H r plane. With G = 1 it is a plain launch.
-template <int A, int B, int WPB>
-__global__ void __launch_bounds__(32 * WPB) fr_rows_adj(CartDev d, const float2* __restrict__ t2,
+// Phase 3: per block of R image rows and coil group g, IFFT along W of the sampled columns, conj(sens_c)
+// multiply and the coil sum, accumulated in shared memory (each lane always owns the same pixels).
+// With use_cluster the G coil groups of a row block form a cluster (grid.y = G) and reduce their rows
+// through distributed shared memory in rank order (deterministic) into one K^H r plane; otherwise each
+// block writes its group's partial sum to out + g * gstride.
+template <int M, int L, int WPB>
+__global__ void __launch_bounds__(32 * WPB) fl_rows_adj(CartDev d, const float2* __restrict__ t2,
                                                         float2* __restrict__ out, int use_cluster, int G,
                                                         long long gstride) {
-  using TL = TwoLevel<A, B>;
-  constexpr int W = TL::n;
+  using F = LaneFft<M, L>;
+  constexpr int W = F::n, R = WPB * (32 / L);
   extern __shared__ float2 sm[];
   float2* tw = sm;
-  float2* ex = tw + W;
-  float2* stage = ex + WPB * TL::xch;
-  float2* red = stage + (size_t)d.ns * WPB;  // WPB rows x W: this block's coil-group sum
-  int* as2s = reinterpret_cast<int*>(red + (size_t)WPB * W);
-  // with use_cluster, the G coil groups of a row block form a cluster (grid.y = G); otherwise each
-  // block writes its group's partial sum to out + g * gstride
+  float2* stage = tw + W;                    // [ns][R]
+  float2* red = stage + (size_t)d.ns * R;    // [R][W]
+  int* as2s = reinterpret_cast<int*>(red + (size_t)R * W);
   const int g = blockIdx.y;
   for (int i = threadIdx.x; i < W; i += blockDim.x) {
     tw[i] = d.twW[i];
     as2s[i] = d.slot2s[i];
   }
-  for (int i = threadIdx.x; i < WPB * W; i += blockDim.x) red[i] = c2(0.f, 0.f);
-  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int yi0 = blockIdx.x * WPB, yi = yi0 + w;
-  const int nr = min(WPB, d.Hi - yi0);
+  for (int i = threadIdx.x; i < R * W; i += blockDim.x) red[i] = c2(0.f, 0.f);
+  const int lane = threadIdx.x & 31, t = lane & (L - 1);
+  const int r = (threadIdx.x >> 5) * (32 / L) + lane / L;
+  const int yi0 = blockIdx.x * R;
+  const int nr = min(R, d.Hi - yi0);
+  const bool ok = r < nr;
+  const int rc = ok ? r : 0;  // a group past the last row transforms row 0 of the block and discards it
+  const int yi = yi0 + rc;
   const int c_begin = (int)((long long)g * d.C / G), c_end = (int)((long long)(g + 1) * d.C / G);
-  float2* myex = ex + w * TL::xch;
-  const bool ok = w < nr;
-  // prefetch of the next coil's sampled columns (ns * nr values spread over the block)
+  const int kb = M * lane_brev<L>(t);
+  // register prefetch of the next coil's sampled columns (ns * nr values spread over the block)
   constexpr int PF = 8;
   float2 pf[PF];
   auto fetch = [&](int c) {
@@ -214,47 +277,41 @@ __global__ void __launch_bounds__(32 * WPB) fr_rows_adj(CartDev d, const float2*
   const bool pf_all = d.ns * nr <= PF * (int)blockDim.x;
   if (c_begin < c_end && pf_all) fetch(c_begin);
   for (int c = c_begin; c < c_end; ++c) {
-    __syncthreads();  // stage free (and, first time, tables and red ready)
+    __syncthreads();  // stage free (and, the first time, tables and red ready)
     if (pf_all) {
 #pragma unroll
       for (int q = 0; q < PF; ++q) {
         const int i = threadIdx.x + q * (int)blockDim.x;
         if (i < d.ns * nr) {
           const int s = i / nr, rr = i - s * nr;
-          stage[s * WPB + rr] = pf[q];
+          stage[s * R + rr] = pf[q];
         }
       }
       if (c + 1 < c_end) fetch(c + 1);
     } else {
       for (int i = threadIdx.x; i < d.ns * nr; i += blockDim.x) {
         const int s = i / nr, rr = i - s * nr;
-        stage[s * WPB + rr] = t2[((size_t)c * d.ns + s) * d.Hi + yi0 + rr];
+        stage[s * R + rr] = t2[((size_t)c * d.ns + s) * d.Hi + yi0 + rr];
       }
     }
     __syncthreads();
-    if (ok && lane < B) {
-      float2 u[A];
+    float2 v[M];
 #pragma unroll
-      for (int ka = 0; ka < A; ++ka) {
-        const int s = as2s[lane + B * ka];
-        u[ka] = s >= 0 ? stage[s * WPB + w] : c2(0.f, 0.f);
-      }
-      TL::inv_step1(u, lane, myex, tw);
+    for (int k1 = 0; k1 < M; ++k1) {
+      const int s = as2s[k1 + kb];
+      v[k1] = s >= 0 ? stage[s * R + rc] : c2(0.f, 0.f);
     }
-    __syncwarp();
-    if (ok && lane < A) {
-      float2 v[B];
-      TL::inv_step2(v, lane, myex, tw);
+    F::inv(v, t, tw);
+    if (ok) {
       const float2* srow = d.sens ? d.sens + ((size_t)c * d.Hf + yi + d.y0) * W : nullptr;
-      float2* rrow = red + (size_t)w * W;
+      float2* rrow = red + (size_t)r * W;
 #pragma unroll
-      for (int b = 0; b < B; ++b) {
-        int x = lane + A * b + d.oxW;
+      for (int j = 0; j < M; ++j) {
+        int x = t + L * j + d.oxW;  // IFFT slot t + L j lands on image column (slot + n/2) mod W
         if (x >= W) x -= W;
-        rrow[x] += srow ? cmulc(v[b], srow[x]) : v[b];
+        rrow[x] += srow ? cmulc(v[j], srow[x]) : v[j];
       }
     }
-    __syncwarp();
   }
   if (use_cluster) {
     cg::cluster_group cluster = cg::this_cluster();
@@ -281,72 +338,79 @@ typedef void (*FrRowsAdjFn)(CartDev, const float2*, float2*, int, int, long long
 
 constexpr int kWpbChoices[3] = {2, 4, 8};
 
-// Kernels of one compiled length, one instance per warps-per-block choice.
+// Kernels of one compiled length n = M * L, one instance per warps-per-block choice.
 struct FastRowKernels {
   FrRowsFwdFn fwd[3] = {nullptr, nullptr, nullptr};
   FrRowsAdjFn adj[3] = {nullptr, nullptr, nullptr};
-  int A = 0, B = 0;
+  int M = 0, L = 0;
   bool ok() const { return fwd[0] != nullptr; }
+  int rows_per_block(int wpb) const { return wpb * (32 / L); }
 };
 struct FastColKernels {
   FrColsFn cols[3] = {nullptr, nullptr, nullptr};
-  int A = 0, B = 0;
+  int M = 0, L = 0;
   bool ok() const { return cols[0] != nullptr; }
+  int cols_per_block(int wpb) const { return wpb * (32 / L); }
 };
 
-template <int A, int B>
+template <int M, int L>
 FastRowKernels row_kernels() {
   FastRowKernels k;
-  k.fwd[0] = fr_rows_fwd<A, B, 2>;
-  k.fwd[1] = fr_rows_fwd<A, B, 4>;
-  k.fwd[2] = fr_rows_fwd<A, B, 8>;
-  k.adj[0] = fr_rows_adj<A, B, 2>;
-  k.adj[1] = fr_rows_adj<A, B, 4>;
-  k.adj[2] = fr_rows_adj<A, B, 8>;
-  k.A = A;
-  k.B = B;
+  k.fwd[0] = fl_rows_fwd<M, L, 2>;
+  k.fwd[1] = fl_rows_fwd<M, L, 4>;
+  k.fwd[2] = fl_rows_fwd<M, L, 8>;
+  k.adj[0] = fl_rows_adj<M, L, 2>;
+  k.adj[1] = fl_rows_adj<M, L, 4>;
+  k.adj[2] = fl_rows_adj<M, L, 8>;
+  k.M = M;
+  k.L = L;
   return k;
 }
-template <int A, int B>
+template <int M, int L>
 FastColKernels col_kernels() {
   FastColKernels k;
-  k.cols[0] = fr_cols<A, B, 2>;
-  k.cols[1] = fr_cols<A, B, 4>;
-  k.cols[2] = fr_cols<A, B, 8>;
-  k.A = A;
-  k.B = B;
+  k.cols[0] = fl_cols<M, L, 2>;
+  k.cols[1] = fl_cols<M, L, 4>;
+  k.cols[2] = fl_cols<M, L, 8>;
+  k.M = M;
+  k.L = L;
   return k;
 }
 
-// Lengths with a compiled two-level split.
-#define PDT_FAST_SIZES(X) X(32, 4, 8) X(48, 6, 8) X(64, 8, 8) X(96, 8, 12) X(128, 8, 16) X(192, 12, 16) \
-  X(256, 16, 16) X(320, 16, 20) X(368, 16, 23) X(384, 16, 24) X(512, 16, 32) X(640, 32, 20) X(768, 32, 24)
+// Lengths with a compiled split n = M * L.
+#define PDT_FAST_SIZES(X) X(32, 4, 8) X(48, 6, 8) X(64, 8, 8) X(96, 6, 16) X(128, 8, 16) X(192, 12, 16) \
+  X(256, 16, 16) X(320, 10, 32) X(368, 23, 16) X(384, 12, 32) X(512, 16, 32) X(640, 20, 32) X(768, 24, 32)
 
 FastRowKernels find_row_kernels(int n) {
-#define PDT_ROWCASE(N, A, B) \
-  if (n == N) return row_kernels<A, B>();
+#define PDT_ROWCASE(N, M, L) \
+  if (n == N) return row_kernels<M, L>();
   PDT_FAST_SIZES(PDT_ROWCASE)
 #undef PDT_ROWCASE
   return FastRowKernels();
 }
 FastColKernels find_col_kernels(int n) {
-#define PDT_COLCASE(N, A, B) \
-  if (n == N) return col_kernels<A, B>();
+#define PDT_COLCASE(N, M, L) \
+  if (n == N) return col_kernels<M, L>();
   PDT_FAST_SIZES(PDT_COLCASE)
 #undef PDT_COLCASE
   return FastColKernels();
 }
 
-size_t fast_rows_smem(const CartDev& d, int A, int B, int wpb) {
-  const size_t n = (size_t)A * B, xch = (size_t)B * (A + 1);
-  return sizeof(float2) * (n + wpb * xch + (size_t)d.ns * wpb) + sizeof(int) * n;
+size_t fast_rows_smem(const CartDev& d, const FastRowKernels& k, int wpb) {
+  const size_t n = (size_t)k.M * k.L, R = (size_t)k.rows_per_block(wpb);
+  return sizeof(float2) * (n + (size_t)d.ns * R) + sizeof(int) * n;
 }
-size_t fast_rows_adj_smem(const CartDev& d, int A, int B, int wpb) {
-  return fast_rows_smem(d, A, B, wpb) + sizeof(float2) * (size_t)wpb * A * B;
+size_t fast_rows_adj_smem(const CartDev& d, const FastRowKernels& k, int wpb) {
+  const size_t n = (size_t)k.M * k.L, R = (size_t)k.rows_per_block(wpb);
+  return fast_rows_smem(d, k, wpb) + sizeof(float2) * R * n;
 }
-size_t fast_cols_smem(int A, int B, int wpb) {
-  const size_t n = (size_t)A * B, xch = (size_t)B * (A + 1);
-  return sizeof(float2) * (n + wpb * xch);
+size_t fast_cols_smem(const FastColKernels& k) { return sizeof(float2) * (size_t)k.M * k.L; }
+
+// Host bit reversal over log2(L) bits (the order LaneFft leaves a spectrum in).
+inline int host_lane_brev(int t, int L) {
+  int r = 0;
+  for (int b = 1; b < L; b <<= 1) r = (r << 1) | ((t & b) ? 1 : 0);
+  return r;
 }
 
 }  // namespace

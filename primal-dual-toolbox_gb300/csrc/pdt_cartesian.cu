@@ -17,6 +17,8 @@
 //   rows_adj  (row blocks x coil groups) t -> IFFT along W -> conj(sens) . -> coil sum
 // The k-space dual r and the data f live in the compact layout [c][s][Hf] (sampled columns only);
 // the entries of unsampled columns never reach u in the reference either (the mask zeroes them).
+// Within a column the compact order is the output row for the generic kernels and the order the
+// lane-distributed FFT leaves its spectrum in for the fast kernels (kperm maps one to the other).
 #include <algorithm>
 #include <array>
 #include <cmath>
@@ -45,7 +47,8 @@ struct CartDev {
   float scale;   // 1/sqrt(W*Hf)
   int RB, CB, ldW, ldH;
   const float2* sens;   // (W, Hf, C) or null (sampling operator)
-  const float* maskc;   // [ns][Hf] mask values of sampled columns, by output row
+  const float* maskc;   // [ns][Hf] mask values of sampled columns, in compact order
+  const int* kperm;     // [Hf] compact position -> output row (null: compact order = output row)
   const int* fwd_slot;  // [ns] forward-FFT output slot of sampled column s
   const int* col_x;     // [ns] k-space column of s
   const int* slot2s;    // [W] inverse-FFT input slot -> s (or -1)
@@ -207,7 +210,8 @@ __global__ void __launch_bounds__(kThreads) rows_adj_kernel(CartDev d, const flo
 __global__ void gather_kernel(CartDev d, const float2* __restrict__ dense, float2* __restrict__ compact) {
   const size_t n = (size_t)d.C * d.ns * d.Hf;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-    const int ypos = (int)(i % d.Hf);
+    const int P = (int)(i % d.Hf);
+    const int ypos = d.kperm ? d.kperm[P] : P;
     const size_t cs = i / d.Hf;
     const int s = (int)(cs % d.ns), c = (int)(cs / d.ns);
     compact[i] = dense[((size_t)c * d.Hf + ypos) * d.W + d.col_x[s]];
@@ -269,13 +273,13 @@ class CartesianOp : public OpImpl, public SolverHooks {
     std::ostringstream os;
     os << "W=" << dev_.W << " H=" << dev_.Hf << " C=" << dev_.C << " sampled_columns=" << dev_.ns;
     if (frow_.ok())
-      os << " rows_fwd=register_fft(" << frow_.A << "x" << frow_.B << ",warps=" << kWpbChoices[tune_.wf] << ")"
-         << " rows_adj=register_fft(warps=" << kWpbChoices[tune_.wa] << ",coil_groups=" << G_
+      os << " rows_fwd=lane_fft(" << frow_.M << "x" << frow_.L << ",warps=" << kWpbChoices[tune_.wf] << ")"
+         << " rows_adj=lane_fft(warps=" << kWpbChoices[tune_.wa] << ",coil_groups=" << G_
          << (tune_.cluster ? ",cluster" : ",partials") << ")";
     else
       os << " rows=stockham(coil_groups=" << G_ << ")";
     if (fcol_.ok())
-      os << " cols=register_fft(" << fcol_.A << "x" << fcol_.B << ",warps=" << kWpbChoices[tune_.wc] << ")";
+      os << " cols=lane_fft(" << fcol_.M << "x" << fcol_.L << ",warps=" << kWpbChoices[tune_.wc] << ")";
     else
       os << " cols=stockham";
     return os.str();
@@ -373,7 +377,7 @@ class CartesianOp : public OpImpl, public SolverHooks {
   void invalidate() override { prepared_ = false; }
 
  private:
-  // Launch configuration of the register-FFT kernels, chosen by the autotuner in prepare().
+  // Launch configuration of the lane-FFT kernels, chosen by the autotuner in prepare().
   struct Tune {
     int wf = 2, wc = 2, wa = 2;  // warps-per-block index (kWpbChoices) of rows_fwd, cols, rows_adj
     bool cluster = false;        // coil groups of a row block reduced in a cluster (else partial images)
@@ -382,8 +386,9 @@ class CartesianOp : public OpImpl, public SolverHooks {
   void launch_rows_fwd(const float2* ubar, float2* t1, int* tick, cudaStream_t st) {
     if (frow_.ok()) {
       const int wpb = kWpbChoices[tune_.wf];
-      dim3 grid((dev_.Hi + wpb - 1) / wpb, dev_.C);
-      frow_.fwd[tune_.wf]<<<grid, 32 * wpb, fast_rows_smem(dev_, frow_.A, frow_.B, wpb), st>>>(dev_, ubar, t1, tick);
+      const int R = frow_.rows_per_block(wpb);
+      dim3 grid((dev_.Hi + R - 1) / R, dev_.C);
+      frow_.fwd[tune_.wf]<<<grid, 32 * wpb, fast_rows_smem(dev_, frow_, wpb), st>>>(dev_, ubar, t1, tick);
       PDT_LAUNCH_CHECK();
       count_launch();
       return;
@@ -397,8 +402,9 @@ class CartesianOp : public OpImpl, public SolverHooks {
                    float2* kout, float sigma, float lambda, cudaStream_t st) {
     if (fcol_.ok()) {
       const int wpb = kWpbChoices[tune_.wc];
-      dim3 grid((dev_.ns + wpb - 1) / wpb, dev_.C);
-      fcol_.cols[tune_.wc]<<<grid, 32 * wpb, fast_cols_smem(fcol_.A, fcol_.B, wpb), st>>>(dev_, mode, tin, tout, r, fc,
+      const int S = fcol_.cols_per_block(wpb);
+      dim3 grid((dev_.ns + S - 1) / S, dev_.C);
+      fcol_.cols[tune_.wc]<<<grid, 32 * wpb, fast_cols_smem(fcol_), st>>>(dev_, mode, tin, tout, r, fc,
                                                                                         kin, kout, sigma, lambda);
       PDT_LAUNCH_CHECK();
       count_launch();
@@ -415,9 +421,10 @@ class CartesianOp : public OpImpl, public SolverHooks {
       const int wpb = kWpbChoices[tune_.wa];
       const bool cl = tune_.cluster && G > 1;
       cudaLaunchConfig_t cfg = {};
-      cfg.gridDim = dim3((dev_.Hi + wpb - 1) / wpb, G);
+      const int R = frow_.rows_per_block(wpb);
+      cfg.gridDim = dim3((dev_.Hi + R - 1) / R, G);
       cfg.blockDim = dim3(32 * wpb);
-      cfg.dynamicSmemBytes = fast_rows_adj_smem(dev_, frow_.A, frow_.B, wpb);
+      cfg.dynamicSmemBytes = fast_rows_adj_smem(dev_, frow_, wpb);
       cfg.stream = st;
       cudaLaunchAttribute attr[1];
       attr[0].id = cudaLaunchAttributeClusterDimension;
@@ -486,6 +493,22 @@ class CartesianOp : public OpImpl, public SolverHooks {
           break;
         }
     d.ns = (int)col_x.size();
+    // lane-FFT kernels where the length has a compiled split (they fix the compact k-space order)
+    frow_ = find_row_kernels(W);
+    fcol_ = find_col_kernels(Hf);
+    if (frow_.ok() && fast_rows_adj_smem(d, frow_, 8) > (size_t)g_max_smem) frow_ = FastRowKernels();
+    if (fcol_.ok() && fast_cols_smem(fcol_) > (size_t)g_max_smem) fcol_ = FastColKernels();
+    // compact position P -> output row: P = k1 L + t holds spectrum index k1 + M brev_L(t), which the
+    // fftshift puts on row (k + Hf/2) mod Hf
+    std::vector<int> kperm(Hf);
+    for (int P = 0; P < Hf; ++P) {
+      if (fcol_.ok()) {
+        const int k = P / fcol_.L + fcol_.M * host_lane_brev(P % fcol_.L, fcol_.L);
+        kperm[P] = (k + d.oyH) % Hf;
+      } else {
+        kperm[P] = P;
+      }
+    }
     std::vector<int> fwd_slot(d.ns), slot2s(W, -1), fslot2s(W, -1);
     std::vector<float> maskc((size_t)d.ns * Hf);
     for (int s = 0; s < d.ns; ++s) {
@@ -493,7 +516,7 @@ class CartesianOp : public OpImpl, public SolverHooks {
       fwd_slot[s] = ((x - d.oxW) % W + W) % W;
       fslot2s[fwd_slot[s]] = s;
       slot2s[(x + d.mxW) % W] = s;
-      for (int y = 0; y < Hf; ++y) maskc[(size_t)s * Hf + y] = mask[(size_t)y * W + x];
+      for (int P = 0; P < Hf; ++P) maskc[(size_t)s * Hf + P] = mask[(size_t)kperm[P] * W + x];
     }
     // launch shapes
     d.ldW = W + 1;
@@ -508,8 +531,8 @@ class CartesianOp : public OpImpl, public SolverHooks {
     std::vector<float2> twW(W), twH(Hf);
     fill_twiddles(W, twW.data());
     fill_twiddles(Hf, twH.data());
-    const size_t need = 16 * 8 + sizeof(int) * (2 * (size_t)d.ns + 2 * (size_t)W) + sizeof(float) * maskc.size() +
-                        sizeof(float2) * ((size_t)W + Hf);
+    const size_t need = 16 * 9 + sizeof(int) * (2 * (size_t)d.ns + 2 * (size_t)W + Hf) +
+                        sizeof(float) * maskc.size() + sizeof(float2) * ((size_t)W + Hf);
     tables_.ensure(need);
     char* base = tables_.as<char>();
     size_t off = 0;
@@ -527,12 +550,8 @@ class CartesianOp : public OpImpl, public SolverHooks {
     d.slot2s = reinterpret_cast<const int*>(put(slot2s.data(), sizeof(int) * W));
     d.fslot2s = reinterpret_cast<const int*>(put(fslot2s.data(), sizeof(int) * W));
     d.maskc = reinterpret_cast<const float*>(put(maskc.data(), sizeof(float) * maskc.size()));
+    d.kperm = fcol_.ok() ? reinterpret_cast<const int*>(put(kperm.data(), sizeof(int) * Hf)) : nullptr;
     scratch_.ensure(std::max<size_t>(1, (size_t)C * d.ns * d.Hi) * sizeof(float2));
-    // register-FFT kernels where the length has a compiled split
-    frow_ = find_row_kernels(W);
-    fcol_ = find_col_kernels(Hf);
-    if (frow_.ok() && fast_rows_adj_smem(d, frow_.A, frow_.B, 8) > (size_t)g_max_smem) frow_ = FastRowKernels();
-    if (fcol_.ok() && fast_cols_smem(fcol_.A, fcol_.B, 8) > (size_t)g_max_smem) fcol_ = FastColKernels();
     for (int w = 0; w < 3; ++w) {
       if (frow_.ok()) {
         PDT_CUDA_CHECK(cudaFuncSetAttribute(frow_.fwd[w], cudaFuncAttributeMaxDynamicSharedMemorySize, g_max_smem));
@@ -549,7 +568,7 @@ class CartesianOp : public OpImpl, public SolverHooks {
     prepared_ = true;
   }
 
-  // Times the candidate launch shapes of the register-FFT kernels on scratch buffers (CUDA events, a
+  // Times the candidate launch shapes of the lane-FFT kernels on scratch buffers (CUDA events, a
   // few launches each) and keeps the fastest: warps per block of each kernel, and for the adjoint rows
   // the number of coil groups and cluster reduction versus partial images. Results are cached per
   // (W, H, coils, sampled columns).

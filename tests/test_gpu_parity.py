@@ -277,3 +277,26 @@ def test_consecutive_solves_with_changing_max_iter(pdt, oracle):
                                      alpha1=float(np.float32(case["alpha1"])), reduction=float(np.float32(0.3)),
                                      max_iter=max_iter, prec=32, return_state=True, state=state)
         assert rel_l2(opt.getResult(), ref) <= SOLVE_TOL, max_iter
+
+
+# (C, H, W, roos): every length in the list has a compiled lane-FFT split (8, 16 and 32 lanes per
+# sequence), so the solve runs the fast kernels and the transform-ordered compact k-space
+@pytest.mark.parametrize("C,H,W,roos", [(3, 32, 48, False), (2, 96, 64, True), (2, 128, 192, False),
+                                        (3, 320, 96, True), (2, 768, 32, False), (2, 384, 320, True),
+                                        (4, 368, 256, False), (2, 512, 128, True)])
+def test_short_solve_on_fast_lengths(pdt, oracle, C, H, W, roos):
+    case = _cart_case(C=C, H=H, W=W, roos=roos, seed=H + W)
+    kind = "cartesian_roos" if roos else "cartesian"
+    op = (pdt.mri.MriCartesianRemoveROOSOperator if roos else pdt.mri.MriCartesianOperator)()
+    op.setCoilSens(case["sens"])
+    op.setMask(case["mask"])
+    opt = pdt.mri.TgvMriOptimizer_2c3c()
+    prm = opt.getParameters()
+    prm.reduction, prm.max_iter, prm.alpha1 = 0.1, 40, case["alpha1"]
+    prm.alpha0 = 2 * prm.alpha1
+    opt.setOperator(op)
+    opt.setNoisyData(case["rawdata"])
+    opt.solve()
+    ref = oracle.op_solve(kind, case["sens"], case["mask"], case["rawdata"], "tgv_mri", alpha0=prm.alpha0,
+                          alpha1=prm.alpha1, reduction=prm.reduction, max_iter=40, prec=32)
+    assert rel_l2(opt.getResult(), ref) <= SOLVE_TOL
