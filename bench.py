@@ -150,8 +150,10 @@ def _phase_bytes(ns, G):
         "cart_cols_prox": c8 * (C * ns * Hi + 3 * C * ns * H + C * ns * Hi) + 4 * ns * H,
         # t2 + sens rows in, K^H r partial sums out
         "cart_rows_adj": c8 * (C * ns * Hi + C * Hi * W + G * Hi * W),
-        # ub, vb(2), p(2), q(3), u, v(2), G khr partials in; ub, vb(2), p(2), q(3), u, v(2) out
-        "mri_image_step_tgv": c8 * Hi * W * (11 + G + 11),
+        # dual: ub, vb(2), p(2), q(3) in; p(2), q(3) out
+        "mri_dual_tgv": c8 * Hi * W * (8 + 5),
+        # primal: u, v(2), p(2), q(3), G K^H r partials in; u, ub, v(2), vb(2) out
+        "mri_primal_tgv": c8 * Hi * W * (8 + G + 6),
     }
 
 

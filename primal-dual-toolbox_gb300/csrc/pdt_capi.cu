@@ -2,6 +2,7 @@
 // mapping. Status codes and thread-local messages replace the reference's IuException.
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <functional>
 #include <iostream>
@@ -15,6 +16,14 @@
 namespace pdt {
 
 std::atomic<uint64_t> g_launches{0};
+
+bool pdl_enabled() {
+  static const bool on = [] {
+    const char* e = std::getenv("PDT_LAUNCH_PDL");
+    return !(e && e[0] == '0');
+  }();
+  return on;
+}
 
 std::shared_ptr<OpImpl> make_cartesian_operator(pdt_op_kind kind);
 
@@ -216,6 +225,9 @@ class OptImpl {
     graph_.reset();
     if (own_) cudaStreamDestroy(own_);
     if (cap_) cudaStreamDestroy(cap_);
+    if (aux_) cudaStreamDestroy(aux_);
+    if (ev_fork_) cudaEventDestroy(ev_fork_);
+    if (ev_join_) cudaEventDestroy(ev_join_);
   }
 
   bool with_op() const { return kind_ == PDT_OPT_TV_OP || kind_ == PDT_OPT_TGV_OP || kind_ == PDT_OPT_TGV_MRI; }
@@ -417,6 +429,12 @@ class OptImpl {
     if (!cap_) PDT_CUDA_CHECK(cudaStreamCreateWithFlags(&cap_, cudaStreamNonBlocking));
     return cap_;
   }
+  // side stream and fork/join events of the concurrent dual update
+  void ensure_aux() {
+    if (!aux_) PDT_CUDA_CHECK(cudaStreamCreateWithFlags(&aux_, cudaStreamNonBlocking));
+    if (!ev_fork_) PDT_CUDA_CHECK(cudaEventCreateWithFlags(&ev_fork_, cudaEventDisableTiming));
+    if (!ev_join_) PDT_CUDA_CHECK(cudaEventCreateWithFlags(&ev_join_, cudaEventDisableTiming));
+  }
 
  private:
   static void copy_in(void* dst, const void* src, size_t bytes, bool is_device, cudaStream_t st) {
@@ -581,7 +599,7 @@ class OptImpl {
       PDT_CUDA_CHECK(cudaStreamSynchronize(st));
       alpha_host_ = tab;
     }
-    PDT_CUDA_CHECK(cudaMemsetAsync(iter, 0xFF, sizeof(int), st));  // -1: the first round ticks it to 0
+    PDT_CUDA_CHECK(cudaMemsetAsync(iter, 0, sizeof(int), st));  // the primal kernel advances it
     const bool is_tgv = kind_ != PDT_OPT_TV_OP;
     const int p0 = parity_;
     const float* atab = reinterpret_cast<const float*>(alpha_.as<char>() + kAlphaHeader);
@@ -590,12 +608,28 @@ class OptImpl {
     pl.n = n;
     pl.p0 = p0;
     pl.verbose = verbose;
+    ensure_aux();
+    cudaStream_t aux = aux_;
+    cudaEvent_t ev_fork = ev_fork_, ev_join = ev_join_;
+    // one iteration: the dual update runs on `aux`, forked from and joined back into `s`, concurrently
+    // with the operator's round (profiling runs it in line so that every phase has its own interval)
     pl.body = [=](int par, cudaStream_t s) {
       const int in = p0 ^ par, out = in ^ 1;
-      hk->round(static_cast<const float2*>(field(F_UB, in)), r_.as<float2>(), fc_.as<float2>(), sigma, lambda, khr,
-                iter, s, prof_);
-      launch_mri_image_step(is_tgv, W_, H_, ptrs(in), ptrs(out), khr, G, gstride, tau, sigma, atab, iter, s);
-      if (prof_) prof_->mark(is_tgv ? "mri_image_step_tgv" : "mri_image_step_tv", s);
+      const float2* ubar = static_cast<const float2*>(field(F_UB, in));
+      if (prof_) {
+        launch_mri_dual(is_tgv, W_, H_, ptrs(in), ptrs(out), sigma, atab, iter, s);
+        prof_->mark(is_tgv ? "mri_dual_tgv" : "mri_dual_tv", s);
+        hk->round(ubar, r_.as<float2>(), fc_.as<float2>(), sigma, lambda, khr, nullptr, s, prof_);
+      } else {
+        PDT_CUDA_CHECK(cudaEventRecord(ev_fork, s));
+        PDT_CUDA_CHECK(cudaStreamWaitEvent(aux, ev_fork, 0));
+        launch_mri_dual(is_tgv, W_, H_, ptrs(in), ptrs(out), sigma, atab, iter, aux);
+        PDT_CUDA_CHECK(cudaEventRecord(ev_join, aux));
+        hk->round(ubar, r_.as<float2>(), fc_.as<float2>(), sigma, lambda, khr, nullptr, s, nullptr);
+        PDT_CUDA_CHECK(cudaStreamWaitEvent(s, ev_join, 0));
+      }
+      launch_mri_primal(is_tgv, W_, H_, ptrs(out), khr, G, gstride, tau, iter, s);
+      if (prof_) prof_->mark(is_tgv ? "mri_primal_tgv" : "mri_primal_tv", s);
     };
     pl.key = graph_key({(uintptr_t)img_.p, (uintptr_t)r_.p, (uintptr_t)fc_.p, (uintptr_t)khr_.p,
                         (uintptr_t)alpha_.p, (uintptr_t)alpha_.bytes, (uintptr_t)op_.get(),
@@ -673,7 +707,8 @@ class OptImpl {
   IterGraph graph_;
   PhaseMarker* prof_ = nullptr;
   bool profiling_ = false;
-  cudaStream_t own_ = nullptr, cap_ = nullptr;
+  cudaStream_t own_ = nullptr, cap_ = nullptr, aux_ = nullptr;
+  cudaEvent_t ev_fork_ = nullptr, ev_join_ = nullptr;
 };
 
 

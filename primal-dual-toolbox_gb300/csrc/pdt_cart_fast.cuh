@@ -92,11 +92,12 @@ __global__ void __launch_bounds__(32 * WPB) fl_rows_fwd(CartDev d, const float2*
   float2* tw = sm;
   float2* stage = tw + W;  // [ns][R]
   int* fs2s = reinterpret_cast<int*>(stage + (size_t)d.ns * R);
-  if (tick && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) atomicAdd(tick, 1);
   for (int i = threadIdx.x; i < W; i += blockDim.x) {
     tw[i] = d.twW[i];
     fs2s[i] = d.fslot2s[i];
   }
+  pdl_wait();  // ubar comes from the previous kernel; t1 may still be read by it
+  if (tick && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) atomicAdd(tick, 1);
   __syncthreads();
   const int lane = threadIdx.x & 31, t = lane & (L - 1);
   const int r = (threadIdx.x >> 5) * (32 / L) + lane / L;
@@ -143,6 +144,7 @@ __global__ void __launch_bounds__(32 * WPB) fl_cols(CartDev d, int mode, const f
   extern __shared__ float2 sm[];
   float2* tw = sm;
   for (int i = threadIdx.x; i < Hf; i += blockDim.x) tw[i] = d.twH[i];
+  pdl_wait();  // t_in, r and fc come from earlier kernels
   __syncthreads();
   const int lane = threadIdx.x & 31, t = lane & (L - 1);
   const int s0 = (blockIdx.x * WPB + (threadIdx.x >> 5)) * (32 / L) + lane / L;
@@ -252,6 +254,7 @@ __global__ void __launch_bounds__(32 * WPB) fl_rows_adj(CartDev d, const float2*
     as2s[i] = d.slot2s[i];
   }
   for (int i = threadIdx.x; i < R * W; i += blockDim.x) red[i] = c2(0.f, 0.f);
+  pdl_wait();  // t2 comes from the previous kernel; out may still be read by earlier ones
   const int lane = threadIdx.x & 31, t = lane & (L - 1);
   const int r = (threadIdx.x >> 5) * (32 / L) + lane / L;
   const int yi0 = blockIdx.x * R;

@@ -387,9 +387,8 @@ class CartesianOp : public OpImpl, public SolverHooks {
     if (frow_.ok()) {
       const int wpb = kWpbChoices[tune_.wf];
       const int R = frow_.rows_per_block(wpb);
-      dim3 grid((dev_.Hi + R - 1) / R, dev_.C);
-      frow_.fwd[tune_.wf]<<<grid, 32 * wpb, fast_rows_smem(dev_, frow_, wpb), st>>>(dev_, ubar, t1, tick);
-      PDT_LAUNCH_CHECK();
+      LaunchEx lx(dim3((dev_.Hi + R - 1) / R, dev_.C), dim3(32 * wpb), fast_rows_smem(dev_, frow_, wpb), st);
+      PDT_CUDA_CHECK(cudaLaunchKernelEx(&lx.cfg, frow_.fwd[tune_.wf], dev_, ubar, t1, tick));
       count_launch();
       return;
     }
@@ -403,10 +402,9 @@ class CartesianOp : public OpImpl, public SolverHooks {
     if (fcol_.ok()) {
       const int wpb = kWpbChoices[tune_.wc];
       const int S = fcol_.cols_per_block(wpb);
-      dim3 grid((dev_.ns + S - 1) / S, dev_.C);
-      fcol_.cols[tune_.wc]<<<grid, 32 * wpb, fast_cols_smem(fcol_), st>>>(dev_, mode, tin, tout, r, fc,
-                                                                                        kin, kout, sigma, lambda);
-      PDT_LAUNCH_CHECK();
+      LaunchEx lx(dim3((dev_.ns + S - 1) / S, dev_.C), dim3(32 * wpb), fast_cols_smem(fcol_), st);
+      PDT_CUDA_CHECK(cudaLaunchKernelEx(&lx.cfg, fcol_.cols[tune_.wc], dev_, mode, tin, tout, r, fc, kin, kout, sigma,
+                                        lambda));
       count_launch();
       return;
     }
@@ -420,20 +418,10 @@ class CartesianOp : public OpImpl, public SolverHooks {
     if (frow_.ok()) {
       const int wpb = kWpbChoices[tune_.wa];
       const bool cl = tune_.cluster && G > 1;
-      cudaLaunchConfig_t cfg = {};
       const int R = frow_.rows_per_block(wpb);
-      cfg.gridDim = dim3((dev_.Hi + R - 1) / R, G);
-      cfg.blockDim = dim3(32 * wpb);
-      cfg.dynamicSmemBytes = fast_rows_adj_smem(dev_, frow_, wpb);
-      cfg.stream = st;
-      cudaLaunchAttribute attr[1];
-      attr[0].id = cudaLaunchAttributeClusterDimension;
-      attr[0].val.clusterDim.x = 1;
-      attr[0].val.clusterDim.y = cl ? G : 1;
-      attr[0].val.clusterDim.z = 1;
-      cfg.attrs = attr;
-      cfg.numAttrs = 1;
-      PDT_CUDA_CHECK(cudaLaunchKernelEx(&cfg, frow_.adj[tune_.wa], dev_, t2, out, cl ? 1 : 0, G,
+      LaunchEx lx(dim3((dev_.Hi + R - 1) / R, G), dim3(32 * wpb), fast_rows_adj_smem(dev_, frow_, wpb), st,
+                  cl ? G : 0);
+      PDT_CUDA_CHECK(cudaLaunchKernelEx(&lx.cfg, frow_.adj[tune_.wa], dev_, t2, out, cl ? 1 : 0, G,
                                         (long long)dev_.Hi * dev_.W));
       count_launch();
       return;

@@ -25,6 +25,13 @@ __host__ __device__ __forceinline__ float2 cmul(float2 a, float2 b) { return c2(
 __host__ __device__ __forceinline__ float2 cmulc(float2 a, float2 b) { return c2(a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y); }
 __host__ __device__ __forceinline__ float2 conjf2(float2 a) { return c2(a.x, -a.y); }
 
+#ifndef PDT_HOST_EMULATION
+// Programmatic dependent launch: a kernel launched with programmatic stream serialisation may be
+// launched while its predecessor in the stream finishes; pdl_wait() blocks until the predecessor grid
+// has completed and its writes are visible (it returns at once for an ordinary launch).
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+#endif
+
 // |z|^2 of a pixel (real or complex).
 __device__ __forceinline__ float abs2(float a) { return a * a; }
 __device__ __forceinline__ float abs2(float2 a) { return a.x * a.x + a.y * a.y; }

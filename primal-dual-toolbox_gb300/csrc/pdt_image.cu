@@ -1,10 +1,11 @@
 // pdt_image.cu -- fused image-side primal-dual steps (TV, TGV^2, TV/TGV with an operator).
 //
-// Each kernel does one whole iteration's image-side work for a 32 x 8 tile: it stages the over-relaxed
-// primal (u-bar, v-bar) plus a one-pixel halo in shared memory, recomputes the dual update on the halo
-// pixels it needs, and finishes the primal update from shared memory. The reference does the same
-// arithmetic in two to four separate launches (tgv_kernels.cuh:225-324, 432-467, 568-605, 647-686),
-// each re-reading its neighbours from global memory.
+// The denoising kernels do one whole iteration's image-side work for a 32 x 8 tile: they stage the
+// over-relaxed primal (u-bar, v-bar) plus a one-pixel halo in shared memory, recompute the dual update
+// on the halo pixels they need, and finish the primal update from shared memory. The reference does
+// the same arithmetic in two to four separate launches (tgv_kernels.cuh:225-324, 432-467, 568-605,
+// 647-686), each re-reading its neighbours from global memory. The with-operator solvers split the
+// image side into a dual and a primal kernel instead (see below).
 //
 // Fields read at a neighbour (u-bar, v-bar, p, q -- and u, v for the primal-first TGV order) ping-pong
 // between an `in` and an `out` buffer so that tiles never read a neighbour's freshly written values.
@@ -190,153 +191,107 @@ __global__ void __launch_bounds__(NT) tgv_denoise_step_kernel(int W, int H, ImgP
 }
 
 // ------------------------------------------------------------------------------------------------
-// TgvMriOptimizer / TgvOptimizerWithOp / TvOptimizerWithOp image side (dual first, K^H r given).
-//   p <- proj_a1(p + sigma (grad+ ub - vb)),  q <- proj_a0(q + sigma eps(vb))
-//   u+ = u + tau (div- p - K^H r),            v+ = v + tau (div_h- q + p)
-// u and v are read only at their own pixel and update in place.
+// TgvMriOptimizer / TgvOptimizerWithOp / TvOptimizerWithOp image side (dual first, K^H r given), as two
+// kernels so that the dual update runs concurrently with the operator chain (it needs only u-bar and
+// v-bar of the previous iteration):
+//   dual    p <- proj_a1(p + sigma (grad+ ub - vb)),  q <- proj_a0(q + sigma eps(vb))   (in -> out)
+//   primal  u+ = u + tau (div- p - K^H r),            v+ = v + tau (div_h- q + p)       (p, q from out)
+// u and v are read only at their own pixel and update in place; u-bar and v-bar go to `out`.
+// iter[0] is the iteration index (incremented by the primal kernel, which runs after the dual kernel
+// has read it), iter[1] the length of the alpha table.
 // ------------------------------------------------------------------------------------------------
 template <bool TGV>
-__global__ void __launch_bounds__(NT) mri_image_step_kernel(int W, int H, ImgPtrs in, ImgPtrs out,
-                                                            const float2* __restrict__ khr, int G, long long gstride,
-                                                            float tau, float sigma,
-                                                            const float* __restrict__ alpha_tab,
-                                                            const int* __restrict__ iter) {
-  __shared__ float2 s_ub[TY + 2][TX + 2];
-  __shared__ float2 s_vbx[TGV ? TY + 2 : 1][TX + 2], s_vby[TGV ? TY + 2 : 1][TX + 2];
-  __shared__ float2 s_px[TY + 1][TX + 1], s_py[TY + 1][TX + 1];
-  __shared__ float2 s_qxx[TGV ? TY + 1 : 1][TX + 1], s_qyy[TGV ? TY + 1 : 1][TX + 1], s_qxy[TGV ? TY + 1 : 1][TX + 1];
-  const int tid = threadIdx.x;
-  const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
+__global__ void __launch_bounds__(NT) mri_dual_kernel(int W, int H, ImgPtrs in, ImgPtrs out, float sigma,
+                                                      const float* __restrict__ alpha_tab,
+                                                      const int* __restrict__ iter) {
+  const int x = blockIdx.x * TX + threadIdx.x % TX, y = blockIdx.y * TY + threadIdx.x / TX;
+  if (x >= W || y >= H) return;
+  const size_t idx = (size_t)y * W + x;
+  const bool xn = x < W - 1, yn = y < H - 1;
   const float2* ub = static_cast<const float2*>(in.ub);
-  const float2 z = c2(0.f, 0.f);
-
-  // Every global load of this thread is issued before the first barrier: its own pixel's duals and
-  // primals (dual-region position (lx, ly), lx, ly >= 1), one halo dual position (left column / top row),
-  // and its share of the u-bar / v-bar staging.
-  const int lx = tid % TX + 1, ly = tid / TX + 1;
-  const int gx = x0 + lx - 1, gy = y0 + ly - 1;
-  const bool own = gx < W && gy < H;
-  const size_t idx = (size_t)gy * W + gx;
-  float2 opx = z, opy = z, oqxx = z, oqyy = z, oqxy = z, ou = z, ovx = z, ovy = z, okh = z;
-  if (own) {
-    opx = static_cast<const float2*>(in.px)[idx];
-    opy = static_cast<const float2*>(in.py)[idx];
-    ou = static_cast<const float2*>(out.u)[idx];
-    okh = khr[idx];
-    for (int g = 1; g < G; ++g) okh += khr[idx + (size_t)g * gstride];
-    if constexpr (TGV) {
-      oqxx = static_cast<const float2*>(in.qxx)[idx];
-      oqyy = static_cast<const float2*>(in.qyy)[idx];
-      oqxy = static_cast<const float2*>(in.qxy)[idx];
-      ovx = static_cast<const float2*>(out.vx)[idx];
-      ovy = static_cast<const float2*>(out.vy)[idx];
-    }
-  }
-  // halo dual positions: top row (hy = 0, hx = 1..TX) then left column (hx = 0, hy = 1..TY)
-  int hx = -1, hy = -1;
-  if (tid < TX + TY) {
-    hx = tid < TX ? tid + 1 : 0;
-    hy = tid < TX ? 0 : tid - TX + 1;
-  }
-  const int hgx = x0 - 1 + hx, hgy = y0 - 1 + hy;
-  const bool halo = hx >= 0 && hgx >= 0 && hgx < W && hgy >= 0 && hgy < H;
-  const size_t hidx = (size_t)hgy * W + hgx;
-  float2 hpx = z, hpy = z, hqxx = z, hqyy = z, hqxy = z;
-  if (halo) {
-    hpx = static_cast<const float2*>(in.px)[hidx];
-    hpy = static_cast<const float2*>(in.py)[hidx];
-    if constexpr (TGV) {
-      hqxx = static_cast<const float2*>(in.qxx)[hidx];
-      hqyy = static_cast<const float2*>(in.qyy)[hidx];
-      hqxy = static_cast<const float2*>(in.qxy)[hidx];
-    }
-  }
-  for (int i = tid; i < (TX + 2) * (TY + 2); i += NT) {
-    const int sy = i / (TX + 2), sx = i - sy * (TX + 2);
-    const int ggx = x0 - 1 + sx, ggy = y0 - 1 + sy;
-    if (ggx >= 0 && ggx < W && ggy >= 0 && ggy < H) {
-      const size_t j = (size_t)ggy * W + ggx;
-      s_ub[sy][sx] = ub[j];
-      if constexpr (TGV) {
-        s_vbx[sy][sx] = static_cast<const float2*>(in.vbx)[j];
-        s_vby[sy][sx] = static_cast<const float2*>(in.vby)[j];
-      }
-    }
-  }
   float alpha0 = 1.f, alpha1 = 1.f;
   if constexpr (TGV) {
-    // iter[0] = this round's index, iter[1] = table length
     const int k = min(max(iter[0], 0), iter[1] - 1);
     alpha0 = alpha_tab[2 * k];
     alpha1 = alpha_tab[2 * k + 1];
   }
-  __syncthreads();
+  const float2 c = ub[idx];
+  const float2 ux = xn ? ub[idx + 1] : c, uy = yn ? ub[idx + W] : c;
+  const float2 pxo = static_cast<const float2*>(in.px)[idx], pyo = static_cast<const float2*>(in.py)[idx];
+  float2 a, b;
+  float2 vx, vy, vxx, vxy, vyx, vyy;
+  if constexpr (TGV) {
+    const float2* vbx = static_cast<const float2*>(in.vbx);
+    const float2* vby = static_cast<const float2*>(in.vby);
+    vx = vbx[idx];
+    vy = vby[idx];
+    vxx = xn ? vbx[idx + 1] : vx;
+    vxy = yn ? vbx[idx + W] : vx;
+    vyx = xn ? vby[idx + 1] : vy;
+    vyy = yn ? vby[idx + W] : vy;
+    a = pxo + sigma * ((ux - c) - vx);
+    b = pyo + sigma * ((uy - c) - vy);
+  } else {
+    a = pxo + sigma * (ux - c);
+    b = pyo + sigma * (uy - c);
+  }
+  const float sp = proj_scale(sqrtf(abs2(a) + abs2(b)), alpha1);
+  static_cast<float2*>(out.px)[idx] = a * sp;
+  static_cast<float2*>(out.py)[idx] = b * sp;
+  if constexpr (TGV) {
+    const float2 gxx = vxx - vx;
+    const float2 gxy = 0.5f * (vxy - vx + vyx - vy);
+    const float2 gyy = vyy - vy;
+    const float2 qa = static_cast<const float2*>(in.qxx)[idx] + sigma * gxx;
+    const float2 qb = static_cast<const float2*>(in.qyy)[idx] + sigma * gyy;
+    const float2 qc = static_cast<const float2*>(in.qxy)[idx] + sigma * gxy;
+    const float sq = proj_scale(sqrtf(abs2(qa) + abs2(qb) + 2.0f * abs2(qc)), alpha0);
+    static_cast<float2*>(out.qxx)[idx] = qa * sq;
+    static_cast<float2*>(out.qyy)[idx] = qb * sq;
+    static_cast<float2*>(out.qxy)[idx] = qc * sq;
+  }
+}
 
-  // dual update at dual-region position (qx, qy) with global (qgx, qgy)
-  auto dual = [&](int qx, int qy, int qgx, int qgy, float2 pxo, float2 pyo, float2 qxxo, float2 qyyo, float2 qxyo,
-                  bool write, size_t qidx) {
-    const int xp = qx + (qgx < W - 1), yp = qy + (qgy < H - 1);
-    const float2 c = s_ub[qy][qx];
-    float2 a, b;
-    if constexpr (TGV) {
-      a = pxo + sigma * ((s_ub[qy][xp] - c) - s_vbx[qy][qx]);
-      b = pyo + sigma * ((s_ub[yp][qx] - c) - s_vby[qy][qx]);
-    } else {
-      a = pxo + sigma * (s_ub[qy][xp] - c);
-      b = pyo + sigma * (s_ub[yp][qx] - c);
-    }
-    const float sp = proj_scale(sqrtf(abs2(a) + abs2(b)), alpha1);
-    a = a * sp;
-    b = b * sp;
-    s_px[qy][qx] = a;
-    s_py[qy][qx] = b;
-    if (write) {
-      static_cast<float2*>(out.px)[qidx] = a;
-      static_cast<float2*>(out.py)[qidx] = b;
-    }
-    if constexpr (TGV) {
-      const float2 vx = s_vbx[qy][qx], vy = s_vby[qy][qx];
-      const float2 gxx = s_vbx[qy][xp] - vx;
-      const float2 gxy = 0.5f * (s_vbx[yp][qx] - vx + s_vby[qy][xp] - vy);
-      const float2 gyy = s_vby[yp][qx] - vy;
-      const float2 qa = qxxo + sigma * gxx;
-      const float2 qb = qyyo + sigma * gyy;
-      const float2 qc = qxyo + sigma * gxy;
-      const float sq = proj_scale(sqrtf(abs2(qa) + abs2(qb) + 2.0f * abs2(qc)), alpha0);
-      const float2 na = qa * sq, nb = qb * sq, nc = qc * sq;
-      s_qxx[qy][qx] = na;
-      s_qyy[qy][qx] = nb;
-      s_qxy[qy][qx] = nc;
-      if (write) {
-        static_cast<float2*>(out.qxx)[qidx] = na;
-        static_cast<float2*>(out.qyy)[qidx] = nb;
-        static_cast<float2*>(out.qxy)[qidx] = nc;
-      }
-    }
-  };
-  if (own) dual(lx, ly, gx, gy, opx, opy, oqxx, oqyy, oqxy, true, idx);
-  if (halo) dual(hx, hy, hgx, hgy, hpx, hpy, hqxx, hqyy, hqxy, false, hidx);
-  __syncthreads();
+// div- of a component at (x, y) along x (dir 0) or y (dir 1) with the reference's boundary rows.
+__device__ __forceinline__ float2 bdiff(const float2* __restrict__ f, size_t idx, int pos, int n, size_t step) {
+  return (pos > 0) ? ((pos < n - 1) ? f[idx] - f[idx - step] : -f[idx - step]) : f[idx];
+}
 
-  if (own) {
-    // TGV_primal_u_noprox_kernel (tgv_kernels.cuh:432-467)
-    const float2 d = div_minus<float2, TX + 1>(s_px, s_py, lx, ly, gx, gy, W, H);
-    const float2 un = ou + tau * (d - okh);
-    static_cast<float2*>(out.u)[idx] = un;
-    static_cast<float2*>(out.ub)[idx] = 2.0f * un - ou;
-    if constexpr (TGV) {
-      // TGV_primal_v_kernel (tgv_kernels.cuh:647-686)
-      const float2 dqxx = (gx > 0) ? ((gx < W - 1) ? s_qxx[ly][lx] - s_qxx[ly][lx - 1] : -s_qxx[ly][lx - 1]) : s_qxx[ly][lx];
-      const float2 dqyy = (gy > 0) ? ((gy < H - 1) ? s_qyy[ly][lx] - s_qyy[ly - 1][lx] : -s_qyy[ly - 1][lx]) : s_qyy[ly][lx];
-      const float2 dqxyx = (gx > 0) ? ((gx < W - 1) ? s_qxy[ly][lx] - s_qxy[ly][lx - 1] : -s_qxy[ly][lx - 1]) : s_qxy[ly][lx];
-      const float2 dqxyy = (gy > 0) ? ((gy < H - 1) ? s_qxy[ly][lx] - s_qxy[ly - 1][lx] : -s_qxy[ly - 1][lx]) : s_qxy[ly][lx];
-      const float2 vxn = ovx + tau * ((dqxx + dqxyy) + s_px[ly][lx]);
-      const float2 vyn = ovy + tau * ((dqyy + dqxyx) + s_py[ly][lx]);
-      static_cast<float2*>(out.vx)[idx] = vxn;
-      static_cast<float2*>(out.vy)[idx] = vyn;
-      static_cast<float2*>(out.vbx)[idx] = 2.0f * vxn - ovx;
-      static_cast<float2*>(out.vby)[idx] = 2.0f * vyn - ovy;
-    }
+template <bool TGV>
+__global__ void __launch_bounds__(NT) mri_primal_kernel(int W, int H, ImgPtrs out, const float2* __restrict__ khr,
+                                                        int G, long long gstride, float tau, int* __restrict__ iter) {
+  pdl_wait();  // K^H r comes from the previous kernel
+  if (iter && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) atomicAdd(iter, 1);
+  const int x = blockIdx.x * TX + threadIdx.x % TX, y = blockIdx.y * TY + threadIdx.x / TX;
+  if (x >= W || y >= H) return;
+  const size_t idx = (size_t)y * W + x;
+  const float2* px = static_cast<const float2*>(out.px);
+  const float2* py = static_cast<const float2*>(out.py);
+  float2 kh = khr[idx];
+  for (int g = 1; g < G; ++g) kh += khr[idx + (size_t)g * gstride];
+  float2* u = static_cast<float2*>(out.u);
+  const float2 ou = u[idx];
+  // TGV_primal_u_noprox_kernel (tgv_kernels.cuh:432-467)
+  const float2 d = bdiff(px, idx, x, W, 1) + bdiff(py, idx, y, H, (size_t)W);
+  const float2 un = ou + tau * (d - kh);
+  u[idx] = un;
+  static_cast<float2*>(out.ub)[idx] = 2.0f * un - ou;
+  if constexpr (TGV) {
+    // TGV_primal_v_kernel (tgv_kernels.cuh:647-686)
+    const float2* qxx = static_cast<const float2*>(out.qxx);
+    const float2* qyy = static_cast<const float2*>(out.qyy);
+    const float2* qxy = static_cast<const float2*>(out.qxy);
+    float2* vx = static_cast<float2*>(out.vx);
+    float2* vy = static_cast<float2*>(out.vy);
+    const float2 ovx = vx[idx], ovy = vy[idx];
+    const float2 dqxx = bdiff(qxx, idx, x, W, 1), dqyy = bdiff(qyy, idx, y, H, (size_t)W);
+    const float2 dqxyx = bdiff(qxy, idx, x, W, 1), dqxyy = bdiff(qxy, idx, y, H, (size_t)W);
+    const float2 vxn = ovx + tau * ((dqxx + dqxyy) + px[idx]);
+    const float2 vyn = ovy + tau * ((dqyy + dqxyx) + py[idx]);
+    vx[idx] = vxn;
+    vy[idx] = vyn;
+    static_cast<float2*>(out.vbx)[idx] = 2.0f * vxn - ovx;
+    static_cast<float2*>(out.vby)[idx] = 2.0f * vyn - ovy;
   }
 }
 
@@ -370,16 +325,23 @@ void launch_tgv_denoise_step(bool complex_, int W, int H, const ImgPtrs& in, con
   count_launch();
 }
 
-void launch_mri_image_step(bool tgv, int W, int H, const ImgPtrs& in, const ImgPtrs& out, const float2* khr, int G,
-                           long long gstride, float tau, float sigma, const float* alpha_tab, const int* iter,
-                           cudaStream_t st) {
+void launch_mri_dual(bool tgv, int W, int H, const ImgPtrs& in, const ImgPtrs& out, float sigma,
+                     const float* alpha_tab, const int* iter, cudaStream_t st) {
   if (tgv)
-    mri_image_step_kernel<true><<<tile_grid(W, H), NT, 0, st>>>(W, H, in, out, khr, G, gstride, tau, sigma,
-                                                                alpha_tab, iter);
+    mri_dual_kernel<true><<<tile_grid(W, H), NT, 0, st>>>(W, H, in, out, sigma, alpha_tab, iter);
   else
-    mri_image_step_kernel<false><<<tile_grid(W, H), NT, 0, st>>>(W, H, in, out, khr, G, gstride, tau, sigma,
-                                                                 alpha_tab, iter);
+    mri_dual_kernel<false><<<tile_grid(W, H), NT, 0, st>>>(W, H, in, out, sigma, alpha_tab, iter);
   PDT_LAUNCH_CHECK();
+  count_launch();
+}
+
+void launch_mri_primal(bool tgv, int W, int H, const ImgPtrs& out, const float2* khr, int G, long long gstride,
+                       float tau, int* iter, cudaStream_t st) {
+  LaunchEx lx(tile_grid(W, H), dim3(NT), 0, st);
+  if (tgv)
+    PDT_CUDA_CHECK(cudaLaunchKernelEx(&lx.cfg, mri_primal_kernel<true>, W, H, out, khr, G, gstride, tau, iter));
+  else
+    PDT_CUDA_CHECK(cudaLaunchKernelEx(&lx.cfg, mri_primal_kernel<false>, W, H, out, khr, G, gstride, tau, iter));
   count_launch();
 }
 

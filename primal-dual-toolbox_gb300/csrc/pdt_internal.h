@@ -82,13 +82,49 @@ void launch_tv_step(bool complex_, int W, int H, const ImgPtrs& in, const ImgPtr
 void launch_tgv_denoise_step(bool complex_, int W, int H, const ImgPtrs& in, const ImgPtrs& out, const void* f,
                              float tau, float sigma, float lambda, float alpha0, float alpha1, cudaStream_t st);
 
-// Image side of one TgvMri / TgvWithOp / TvWithOp iteration after K^H r is known
-// (tgvmrioptimizer.cu:177-197): dual p, q then primal u, v, fused. khr holds G partial sums of K^H r
-// spaced gstride elements apart. alpha_tab[2k], alpha_tab[2k+1] = alpha0, alpha1 of iteration
-// k = *iter. tgv = false gives the TvOptimizerWithOp step (no v, q; unit-ball projection).
-void launch_mri_image_step(bool tgv, int W, int H, const ImgPtrs& in, const ImgPtrs& out, const float2* khr, int G,
-                           long long gstride, float tau, float sigma, const float* alpha_tab, const int* iter,
-                           cudaStream_t st);
+// Image side of one TgvMri / TgvWithOp / TvWithOp iteration (tgvmrioptimizer.cu:177-197).
+// Dual: p, q from u-bar, v-bar of `in` into `out`; alpha_tab[2k], alpha_tab[2k+1] = alpha0, alpha1 of
+// iteration k = iter[0] (clamped to the table length iter[1]). It does not depend on K^H r, so it may
+// run concurrently with the operator. tgv = false gives the TvOptimizerWithOp step (no v, q; unit-ball
+// projection).
+void launch_mri_dual(bool tgv, int W, int H, const ImgPtrs& in, const ImgPtrs& out, float sigma,
+                     const float* alpha_tab, const int* iter, cudaStream_t st);
+// Primal: u, v in place and u-bar, v-bar into `out` from the new p, q of `out` and K^H r (G partial
+// sums spaced gstride elements apart); increments iter[0] when iter is non-null.
+void launch_mri_primal(bool tgv, int W, int H, const ImgPtrs& out, const float2* khr, int G, long long gstride,
+                       float tau, int* iter, cudaStream_t st);
+
+// Programmatic dependent launch of the solver kernels (default on; PDT_LAUNCH_PDL=0 turns it off).
+bool pdl_enabled();
+
+// Launch configuration for cudaLaunchKernelEx: with pdl_enabled(), on an explicit stream, the kernel
+// may be launched while its predecessor finishes (programmatic dependent launch; the kernel calls
+// pdl_wait() before it reads the predecessor's results); cluster_y > 0 groups cluster_y blocks along y
+// into a thread-block cluster.
+struct LaunchEx {
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute attr[2];
+  LaunchEx(dim3 grid, dim3 block, size_t smem, cudaStream_t st, int cluster_y = 0) {
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cfg.attrs = attr;
+    cfg.numAttrs = 0;
+    if (st && pdl_enabled()) {
+      attr[cfg.numAttrs].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+      attr[cfg.numAttrs].val.programmaticStreamSerializationAllowed = 1;
+      ++cfg.numAttrs;
+    }
+    if (cluster_y > 0) {
+      attr[cfg.numAttrs].id = cudaLaunchAttributeClusterDimension;
+      attr[cfg.numAttrs].val.clusterDim.x = 1;
+      attr[cfg.numAttrs].val.clusterDim.y = cluster_y;
+      attr[cfg.numAttrs].val.clusterDim.z = 1;
+      ++cfg.numAttrs;
+    }
+  }
+};
 
 // Records a CUDA event after each phase of an iteration (per-kernel timing); null in normal runs.
 struct PhaseMarker {
