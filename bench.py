@@ -139,6 +139,21 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(self.rows)}
 
 
+def _phase_bytes_case(C, Hf, W, ns, G, roos):
+    """Algorithmic bytes of one iteration of a Cartesian TGV-MRI problem under the engine's layout
+    (sampled columns only; each logical array read or written once), per kernel phase."""
+    Hi = Hf // 2 if roos else Hf
+    N = Hi * W
+    c8 = 8
+    return {
+        "cart_rows_fwd": c8 * (N + C * N + C * ns * Hi),
+        "cart_cols_prox": c8 * (C * ns * Hi + 3 * C * ns * Hf + C * ns * Hi) + 4 * ns * Hf,
+        "cart_rows_adj": c8 * (C * ns * Hi + C * N + G * N),
+        "mri_dual_tgv": c8 * N * (8 + 5),
+        "mri_primal_tgv": c8 * N * (8 + G + 6),
+    }
+
+
 def _phase_bytes(ns, G):
     """Algorithmic bytes per launch of each kernel phase (each logical array read or written once)."""
     Hi = H // 2
@@ -266,6 +281,10 @@ def run_ours(args):
     e2e_s = max_over_ranks(time.perf_counter() - t0, dist)
     e2e_val = replica_throughput(ITERS, e_steps, world, e2e_s)
 
+    batched = None
+    if args.batch_cases > 0:
+        batched = run_batched(pdt, torch, args.batch_cases, args.batch_iters, steps=2, warmup=1)
+
     line = None
     if rank == 0:
         cpu = _cpu_baseline(case, seconds=args.cpu_seconds)
@@ -288,6 +307,7 @@ def run_ours(args):
             "tuning": op.tuning(),
             "cpu_baseline": cpu,
             "time_to_1e-4": conv,
+            "batched": batched,
             "clocks": clk.summary(),
             "wall_s": round(wall, 3),
         }
@@ -425,6 +445,79 @@ def _cpu_baseline(case, seconds=10.0, threads=None):
             "sample": f"{n} of the {ITERS} iterations of one solve (includes the initial A^H f), FP32 mirror"}
 
 
+BATCH_SIZES = [(192, 192), (256, 256), (320, 320), (640, 368)]
+
+
+def _batch_specs(n, seed0=3000):
+    """Config-3 style batch: sizes from BATCH_SIZES, coils U{8..32}, acceleration U{2..8}, regular or
+    random phase-encode masks, plain (no ROOS) Cartesian operators, one seed per case."""
+    rng = np.random.default_rng(seed0)
+    out = []
+    for i in range(n):
+        Hf, Wd = BATCH_SIZES[int(rng.integers(len(BATCH_SIZES)))]
+        out.append(dict(C=int(rng.integers(8, 33)), H=Hf, W=Wd, roos=False, accel=int(rng.integers(2, 9)),
+                        mask_kind="regular" if rng.random() < 0.5 else "random", seed=seed0 + i))
+    return out
+
+
+def run_batched(pdt, torch, n_cases, iters, steps, warmup):
+    """n_cases independent TGV-MRI reconstructions solved together (primaldualtoolbox.batch, one CUDA
+    graph per 10 iterations). Returns problem-iterations/s and the whole-iteration HBM roofline: the
+    working set (several GB) is far larger than L2, so the bytes come from HBM."""
+    import concurrent.futures
+    import multiprocessing
+
+    from primaldualtoolbox import warmstart
+
+    specs = _batch_specs(n_cases)
+    t0 = time.perf_counter()
+    with concurrent.futures.ProcessPoolExecutor(max(1, min(16, (os.cpu_count() or 2) - 1)),
+                                                mp_context=multiprocessing.get_context("spawn")) as pool:
+        cases = list(pool.map(warmstart._case, specs, chunksize=1))
+    t_gen = time.perf_counter() - t0
+    opts, ops, nbytes, pix = [], [], 0, 0
+    for spec, case in zip(specs, cases):
+        op = pdt.mri.MriCartesianOperator()
+        op.setCoilSens(case["sens"])
+        op.setMask(case["mask"])
+        opt = pdt.mri.TgvMriOptimizer_2c3c()
+        prm = opt.getParameters()
+        prm.max_iter, prm.reduction, prm.alpha1 = iters - 1, REDUCTION, case["alpha1"]
+        prm.alpha0 = 2 * prm.alpha1
+        opt.setOperator(op)
+        opt.setNoisyData(case["rawdata"])
+        ns = int((case["mask"] != 0).any(axis=0).sum())
+        G = _khr_planes(op.tuning())
+        nbytes += sum(_phase_bytes_case(spec["C"], spec["H"], spec["W"], ns, G, False).values())
+        pix += spec["H"] * spec["W"]
+        opts.append(opt)
+        ops.append(op)
+    del cases
+    batch = pdt.batch.BatchSolver(opts)
+    stream = torch.cuda.current_stream()
+    for _ in range(warmup):
+        batch.solve(stream=stream)
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(steps):
+        batch.solve(stream=stream)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    dt = ev0.elapsed_time(ev1) / 1e3
+    hbm, src = _peaks()
+    achieved = nbytes * iters * steps / dt / 1e9
+    return {"workload": f"batch_{n_cases}_cartesian_tgv2_mixed", "cases": n_cases, "iterations_per_case": iters,
+            "sizes": [f"{a}x{b}" for a, b in BATCH_SIZES], "coils": "U{8..32}", "accel": "U{2..8}",
+            "steps": steps, "warmup": warmup, "value": round(n_cases * iters * steps / dt, 1),
+            "unit": "problem-iterations/s", "ms_per_step": round(dt / steps * 1e3, 3),
+            "pixel_iterations_per_s": round(pix * iters * steps / dt, 1),
+            "roofline": {"bound": "hbm", "kernel": "whole iteration (all phases)", "achieved": round(achieved, 1),
+                         "peak": hbm, "peak_source": src, "unit": "GB/s", "frac": round(achieved / hbm, 4),
+                         "algorithmic_bytes_per_iteration_all_cases": int(nbytes)},
+            "case_generation_s": round(t_gen, 1)}
+
+
 def run_ncu_case(args):
     """The workload's kernels for an ncu capture: operator set-up, autotuning and graph capture run first,
     then one solve of --ncu-iters iterations runs between cudaProfilerStart and cudaProfilerStop, so
@@ -500,6 +593,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--accuracy", type=int, default=1, help="measure iterations/time to rel-L2 1e-4 (1) or skip (0)")
+    ap.add_argument("--batch-cases", type=int, default=64, help="batched leg: independent problems (0 skips)")
+    ap.add_argument("--batch-iters", type=int, default=200, help="batched leg: iterations per problem and step")
     ap.add_argument("--ncu-iters", type=int, default=0,
                     help="profiling mode: one solve of this many iterations between cudaProfilerStart/Stop")
     args = ap.parse_args()

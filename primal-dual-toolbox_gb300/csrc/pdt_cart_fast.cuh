@@ -50,14 +50,19 @@ struct LaneFft {
     reg_fft<M, L>(v, tw, -1.f);
 #pragma unroll
     for (int k1 = 1; k1 < M; ++k1) v[k1] = cmul(v[k1], tw[t * k1]);  // t k1 < n
+    // stage h: the lower lane of a pair keeps a + b, the upper (p - v) w_2h^(t mod h); the last stage
+    // (h = 1) has no twiddle
 #pragma unroll
     for (int h = L / 2; h >= 1; h >>= 1) {
       const bool up = (t & h) != 0;
-      const float2 w = tw[(t & (h - 1)) * (n / (2 * h))];  // w_2h^(t mod h)
+      const float sg = up ? -1.f : 1.f;
+      float2 w = c2(1.f, 0.f);
+      if (h > 1 && up) w = tw[(t & (h - 1)) * (n / (2 * h))];
 #pragma unroll
       for (int k1 = 0; k1 < M; ++k1) {
         const float2 p = shfl_xor2(v[k1], h);
-        v[k1] = up ? cmul(p - v[k1], w) : v[k1] + p;
+        const float2 y = c2(fmaf(sg, v[k1].x, p.x), fmaf(sg, v[k1].y, p.y));
+        v[k1] = (h > 1) ? cmul(y, w) : y;
       }
     }
   }
@@ -67,12 +72,14 @@ struct LaneFft {
 #pragma unroll
     for (int h = 1; h < L; h <<= 1) {
       const bool up = (t & h) != 0;
-      const float2 w = conjf2(tw[(t & (h - 1)) * (n / (2 * h))]);
+      const float sg = up ? -1.f : 1.f;
+      float2 w = c2(1.f, 0.f);
+      if (h > 1 && up) w = conjf2(tw[(t & (h - 1)) * (n / (2 * h))]);
 #pragma unroll
       for (int k1 = 0; k1 < M; ++k1) {
-        const float2 m = up ? cmul(v[k1], w) : v[k1];
+        const float2 m = (h > 1) ? cmul(v[k1], w) : v[k1];
         const float2 p = shfl_xor2(m, h);
-        v[k1] = up ? p - m : m + p;
+        v[k1] = c2(fmaf(sg, m.x, p.x), fmaf(sg, m.y, p.y));  // lower m + p, upper p - m
       }
     }
 #pragma unroll
@@ -238,7 +245,7 @@ __global__ void __launch_bounds__(32 * WPB) fl_cols(CartDev d, int mode, const f
 // through distributed shared memory in rank order (deterministic) into one K^H r plane; otherwise each
 // block writes its group's partial sum to out + g * gstride.
 template <int M, int L, int WPB>
-__global__ void __launch_bounds__(32 * WPB) fl_rows_adj(CartDev d, const float2* __restrict__ t2,
+__global__ void __launch_bounds__(32 * WPB, 16 / WPB) fl_rows_adj(CartDev d, const float2* __restrict__ t2,
                                                         float2* __restrict__ out, int use_cluster, int G,
                                                         long long gstride) {
   using F = LaneFft<M, L>;
