@@ -167,9 +167,17 @@ PDT_API pdt_status pdt_opt_set_input0_uv(pdt_opt* opt, const void* u0, const voi
 /* Copies one state plane: 0 u, 1 u-bar, 2 vx, 3 vy, 4 v-bar x, 5 v-bar y, 6 px, 7 py, 8 qxx, 9 qyy, 10 qxy. */
 PDT_API pdt_status pdt_opt_get_field(pdt_opt* opt, int field, void* dst, int is_device, void* stream);
 /* Energy of the current state accumulated in FP64: out = {total, data, first-order, second-order} --
- * 1/2 ||K u - f||^2 + alpha1 sum |grad u - v| + alpha0 sum |eps(v)| (TGV-MRI at its final alpha), or the
- * TV / denoising forms. */
+ * 1/2 ||K u - f||^2 + alpha1 sum |grad u - v| + alpha0 sum |eps(v)| (TGV-MRI at its final alpha); the
+ * TGV / TV with-operator optimizers weight the data term 1 / (2 lambda) (their r-prox), the denoising
+ * optimizers lambda / 2 ||u - f||^2. */
 PDT_API pdt_status pdt_opt_energy(pdt_opt* opt, void* stream, double out[4]);
+/* Primal-dual gap of a with-operator optimizer (TGV-MRI, TGV / TV with operator) in FP64:
+ * out = {gap, primal, dual, |div- p - K^H r|_2, |p + div_h- q|_2, |K^H r|_2} with primal the energy above,
+ * dual = -Re<f, r> - lambda/2 |r|^2 (lambda = 1 for TGV-MRI; the k-space dual r continued by its limit
+ * -f / lambda on phase-encode lines that are never sampled), and the two residuals of the dual
+ * constraints K^H r = div- p and p = -div_h- q (0 for TV). gap -> 0 and both residuals -> 0 at the
+ * saddle point. */
+PDT_API pdt_status pdt_opt_gap(pdt_opt* opt, void* stream, double out[6]);
 /* Operator norm ||K|| by `iters` power iterations on K^H K (FP64 norms). */
 PDT_API pdt_status pdt_op_norm(pdt_op* op, int iters, uint64_t seed, double* out);
 /* sum |a - b|^2 of two device arrays (b may be NULL) accumulated in FP64. */

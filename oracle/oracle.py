@@ -68,6 +68,8 @@ def lib():
         L.orc_cnn_grad.argtypes = [i, i, i, vp, vp, vp, vp, vp, vp]
         L.orc_tgv_energy_f64.restype = d
         L.orc_tgv_energy_f64.argtypes = [i, i, i, i, vp, vp, vp, vp, vp, vp, d, d]
+        L.orc_op_gap.restype = None
+        L.orc_op_gap.argtypes = [i, i, i, i, vp, vp, vp, vp, i, d, d, d, vp]
         _lib = L
     return _lib
 
@@ -189,6 +191,25 @@ def tgv_energy(kind, sens, mask, f, u, vx, vy, alpha0, alpha1):
     C = 1 if k == 2 else s.shape[0]
     arrs = [np.ascontiguousarray(a, dtype=np.complex128) for a in (f, u, vx, vy)]
     return lib().orc_tgv_energy_f64(k, W, Hf, C, _ptr(s), _ptr(mask), *[_ptr(a) for a in arrs], alpha0, alpha1)
+
+
+STATE_NAMES = ["u", "ubar", "vx", "vy", "vbx", "vby", "px", "py", "qxx", "qyy", "qxy"]
+
+
+def op_gap(kind, sens, mask, f, state, variant="tgv_mri", alpha0=1.0, alpha1=1.0, lam=1.0):
+    """FP64 primal-dual gap and dual-constraint residuals of a with-operator state (op_solve's
+    return_state dict): {'gap', 'primal', 'dual', 'residual_u', 'residual_v', 'norm_khr'}."""
+    k = KIND[kind]
+    mask = np.ascontiguousarray(mask, dtype=np.float64)
+    Hf, W = mask.shape
+    s = None if k == 2 else np.ascontiguousarray(sens, dtype=np.complex128)
+    C = 1 if k == 2 else s.shape[0]
+    f = np.ascontiguousarray(f, dtype=np.complex128)
+    flat = np.concatenate([np.ravel(state[nm]) for nm in STATE_NAMES] + [np.ravel(state["r"])]).astype(np.complex128)
+    out = np.zeros(6)
+    lib().orc_op_gap(k, W, Hf, C, _ptr(s), _ptr(mask), _ptr(f), _ptr(flat), VARIANT[variant], alpha0, alpha1, lam,
+                     _ptr(out))
+    return dict(zip(("gap", "primal", "dual", "residual_u", "residual_v", "norm_khr"), out.tolist()))
 
 
 def _radial_args(traj, dcf, sens, prec):

@@ -1053,6 +1053,79 @@ double orc_tgv_energy_f64(int kind, int W, int Hf, int C, const double* sens, co
                             (const cx<double>*)vy, alpha0, alpha1);
 }
 
+// Primal-dual gap of the with-operator saddle problems from a full state, in FP64 (the engine's
+// pdt_opt_gap). state = {u, ubar, vx, vy, vbx, vby, px, py, qxx, qyy, qxy} (image planes) then r (k-space),
+// as op_solve returns it. The r-prox (r + sigma (K u - f)) / (1 + sigma lambda) (tgv_kernels.cuh:213-223)
+// is the resolvent of F*(r) = <f, r> + lambda/2 |r|^2, so F(z) = |z - f|^2 / (2 lambda) and the dual value
+// is -F*(r) when K^H r = div- p and p = -div_h- q. Phase-encode columns without a sampled entry contribute
+// |f|^2 / (2 lambda) to both sides (r -> -f / lambda there) and are taken at that limit.
+// out = {gap, primal, dual, |div- p - K^H r|, |p + div_h- q|, |K^H r|}; variant as op_solve (2 = TV).
+void orc_op_gap(int kind, int W, int Hf, int C, const double* sens, const double* mask, const double* f,
+                const double* state, int variant, double alpha0, double alpha1, double lambda, double* out) {
+  typedef cx<double> P;
+  CartOp<double> op(kind, W, Hf, C, (const P*)sens, mask);
+  const size_t ni = op.img_n(), nk = op.ksp_n();
+  const int H = op.img_h();
+  const double lam = variant == 0 ? 1.0 : lambda;
+  const P* st = (const P*)state;
+  const P *u = st, *vx = st + 2 * ni, *vy = st + 3 * ni, *px = st + 6 * ni, *py = st + 7 * ni;
+  const P *qxx = st + 8 * ni, *qyy = st + 9 * ni, *qxy = st + 10 * ni, *r = st + 11 * ni;
+  const P* F = (const P*)f;
+  std::vector<P> k(nk), khr(ni);
+  op.forward(u, k.data());
+  double data = 0;
+  for (size_t i = 0; i < nk; ++i) {
+    const double dx = k[i].x - F[i].x, dy = k[i].y - F[i].y;
+    data += dx * dx + dy * dy;
+  }
+  data *= 0.5 / lam;
+  double t1 = 0, t0 = 0, ru = 0, rv = 0;
+  op.adjoint(r, khr.data());
+  for (int y = 0; y < H; ++y)
+    for (int x = 0; x < W; ++x) {
+      const size_t i = x + (size_t)W * y;
+      P gx, gy;
+      dp(u, W, H, x, y, gx, gy);
+      if (variant != 2) {
+        P gxx, gyy, gxy, dx, dy;
+        dp_sym(vx, vy, W, H, x, y, gxx, gyy, gxy);
+        gx = gx - vx[i];
+        gy = gy - vy[i];
+        t0 += std::sqrt(gxx.x * gxx.x + gxx.y * gxx.y + gyy.x * gyy.x + gyy.y * gyy.y +
+                        2.0 * (gxy.x * gxy.x + gxy.y * gxy.y));
+        dm_sym(qxx, qyy, qxy, W, H, x, y, dx, dy);
+        const P a = px[i] + dx, b = py[i] + dy;
+        rv += a.x * a.x + a.y * a.y + b.x * b.x + b.y * b.y;
+      }
+      t1 += std::sqrt(gx.x * gx.x + gx.y * gx.y + gy.x * gy.x + gy.y * gy.y);
+      const P d = dm(px, py, W, H, x, y) - khr[i];
+      ru += d.x * d.x + d.y * d.y;
+    }
+  const double primal = data + (variant == 2 ? t1 : alpha1 * t1 + alpha0 * t0);
+  std::vector<char> sampled(W, 0);
+  for (int y = 0; y < Hf; ++y)
+    for (int x = 0; x < W; ++x)
+      if (mask[(size_t)y * W + x] != 0.0) sampled[x] = 1;
+  double fr = 0, rr = 0, fu = 0;
+  for (size_t i = 0; i < nk; ++i) {
+    if (sampled[i % W]) {
+      fr += F[i].x * r[i].x + F[i].y * r[i].y;
+      rr += r[i].x * r[i].x + r[i].y * r[i].y;
+    } else {
+      fu += F[i].x * F[i].x + F[i].y * F[i].y;
+    }
+  }
+  double nkhr = 0;
+  for (size_t i = 0; i < ni; ++i) nkhr += khr[i].x * khr[i].x + khr[i].y * khr[i].y;
+  const double dual = -fr - 0.5 * lam * rr + 0.5 * fu / lam;
+  out[0] = primal - dual;
+  out[1] = primal;
+  out[2] = dual;
+  out[3] = std::sqrt(ru);
+  out[4] = std::sqrt(rv);
+  out[5] = std::sqrt(nkhr);
+}
+
 // Radial operators. mode: 0 forward (NUFFT), 1 adjoint, 2 exact NDFT forward. sens may be null (single coil).
 // traj {Ns, 2} planar, dcf {Ns}. Pointers are float (prec 32) or double (prec 64).
 void orc_radial_apply(int prec, int mode, int N, double osf, int kw, int C, int Ns, const void* traj, const void* dcf,

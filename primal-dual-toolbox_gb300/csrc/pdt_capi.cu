@@ -314,8 +314,10 @@ class OptImpl {
       DevBuf ku;
       ku.ensure(std::max<size_t>(numel_of(fsize_) * sizeof(float2), 1));
       op_->forward(static_cast<const float2*>(field(F_U, parity_)), usize_, ku.as<float2>(), fsize_, st);
+      // the with-operator r-prox (r + sigma (K u - f)) / (1 + sigma lambda) (tgv_kernels.cuh:213-223) is
+      // the resolvent of F*(r) = <f, r> + lambda/2 |r|^2, i.e. F(z) = |z - f|^2 / (2 lambda)
       data = 0.5 * reduce_dist2(true, ku.p, f_.p, numel_of(fsize_), st);
-      if (kind_ == PDT_OPT_TV_OP) data *= params_.lambda;
+      if (kind_ != PDT_OPT_TGV_MRI) data /= params_.lambda;
     } else {
       data = 0.5 * params_.lambda * reduce_dist2(cplx_, field(F_U, parity_), f_.p, (size_t)W_ * H_, st);
     }
@@ -328,6 +330,45 @@ class OptImpl {
       out[3] = 0;
     }
     out[0] = out[1] + out[2] + out[3];
+  }
+
+  // Primal-dual gap and dual-constraint residuals (pdt_opt_gap). The compact k-space holds every row
+  // of the sampled phase-encode lines; on the other lines r converges to -f, where primal and dual
+  // terms are both |f|^2 / 2 and cancel in the gap.
+  void gap(cudaStream_t st, double out[6]) {
+    if (!with_op()) throw Error(PDT_ERR_INVALID_ARGUMENT, "the gap is defined for the with-operator optimizers");
+    check_ready();
+    if (!has_state_) throw Error(PDT_ERR_STATE, "There is no result yet!");
+    SolverHooks* hk = op_->hooks();
+    ensure_fc(hk, st);
+    const size_t nk = hk->compact_elems();
+    if (r_.bytes != std::max<size_t>(nk, 1) * sizeof(float2) || r_reset_)
+      throw Error(PDT_ERR_STATE, "There is no dual state yet: solve() first");
+    double e[4];
+    energy(st, e);
+    const double lam = kind_ == PDT_OPT_TGV_MRI ? 1.0 : params_.lambda;
+    const double f_all = reduce_dist2(true, f_.p, nullptr, numel_of(fsize_), st);
+    const double f_cmp = reduce_dist2(true, fc_.p, nullptr, nk, st);
+    const double rr = reduce_dist2(true, r_.p, nullptr, nk, st);
+    const double fr = reduce_dot_re(fc_.as<float2>(), r_.as<float2>(), nk, st);
+    // -F*(r) = -<f, r> - lambda/2 |r|^2 on the stored lines; |f|^2 / (2 lambda) on the others (r = -f / lambda)
+    const double dual = -fr - 0.5 * lam * rr + 0.5 * (f_all - f_cmp) / lam;
+    DevBuf khr;
+    khr.ensure((size_t)W_ * H_ * sizeof(float2));
+    hk->adjoint_compact(r_.as<float2>(), khr.as<float2>(), st);
+    const bool v = kind_ != PDT_OPT_TV_OP;
+    double kkt[2];
+    reduce_kkt(W_, H_, khr.as<float2>(), static_cast<const float2*>(field(F_PX, parity_)),
+               static_cast<const float2*>(field(F_PY, parity_)),
+               v ? static_cast<const float2*>(field(F_QXX, parity_)) : nullptr,
+               v ? static_cast<const float2*>(field(F_QYY, parity_)) : nullptr,
+               v ? static_cast<const float2*>(field(F_QXY, parity_)) : nullptr, kkt, st);
+    out[0] = e[0] - dual;
+    out[1] = e[0];
+    out[2] = dual;
+    out[3] = std::sqrt(kkt[0]);
+    out[4] = std::sqrt(kkt[1]);
+    out[5] = std::sqrt(reduce_dist2(true, khr.p, nullptr, (size_t)W_ * H_, st));
   }
 
   // A solve split in three: plan() enqueues the set-up on `st` and returns the per-iteration body,
@@ -1169,6 +1210,15 @@ pdt_status pdt_opt_get_field(pdt_opt* opt, int field, void* dst, int is_device, 
     cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : opt->impl->own_stream();
     opt->impl->get_field(field, dst, is_device != 0, st);
     if (!stream) PDT_CUDA_CHECK(cudaStreamSynchronize(st));
+  });
+}
+
+pdt_status pdt_opt_gap(pdt_opt* opt, void* stream, double out[6]) {
+  return guarded([&] {
+    need(opt, "optimizer");
+    need(out, "out");
+    cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : opt->impl->own_stream();
+    opt->impl->gap(st, out);
   });
 }
 

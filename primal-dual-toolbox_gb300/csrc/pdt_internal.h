@@ -139,6 +139,9 @@ double reduce_dist2(bool complex_, const void* a, const void* b, size_t n, cudaS
 void reduce_regularizer(bool complex_, const void* u, const void* vx, const void* vy, int W, int H, double out[2],
                         cudaStream_t st);
 void launch_scale(float2* x, float s, size_t n, cudaStream_t st);
+double reduce_dot_re(const float2* a, const float2* b, size_t n, cudaStream_t st);
+void reduce_kkt(int W, int H, const float2* khr, const float2* px, const float2* py, const float2* qxx,
+                const float2* qyy, const float2* qxy, double out[2], cudaStream_t st);
 // *tick += 1 (one thread).
 void launch_tick(int* tick, cudaStream_t st);
 

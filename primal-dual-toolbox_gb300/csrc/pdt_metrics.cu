@@ -80,6 +80,48 @@ __global__ void __launch_bounds__(kRedThreads) regularizer_kernel(const P* __res
   }
 }
 
+// partial[b] = sum over this block's elements of Re(a . conj(b))
+__global__ void __launch_bounds__(kRedThreads) dot_re_kernel(const float2* __restrict__ a, const float2* __restrict__ b,
+                                                            size_t n, double* __restrict__ partial) {
+  double s = 0;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    s += (double)a[i].x * b[i].x + (double)a[i].y * b[i].y;
+  s = block_sum(s);
+  if (threadIdx.x == 0) partial[blockIdx.x] = s;
+}
+
+// Optimality residuals of the with-operator saddle point, as partial sums of squares:
+//   partial[2 b]     = sum |div- p - K^H r|^2            (u-stationarity: the primal u step is zero)
+//   partial[2 b + 1] = sum |p + div_h- q|^2              (v-stationarity; TGV only)
+// with the reference's div- boundary rules (x == 0: p(0); x == W-1: -p(W-2); else p(x) - p(x-1)).
+__device__ __forceinline__ float2 dm_at(const float2* __restrict__ f, size_t i, int pos, int n, size_t step) {
+  return (pos > 0) ? ((pos < n - 1) ? f[i] - f[i - step] : -f[i - step]) : f[i];
+}
+__global__ void __launch_bounds__(kRedThreads) kkt_kernel(int W, int H, const float2* __restrict__ khr,
+                                                         const float2* __restrict__ px, const float2* __restrict__ py,
+                                                         const float2* __restrict__ qxx, const float2* __restrict__ qyy,
+                                                         const float2* __restrict__ qxy, double* __restrict__ partial) {
+  double su = 0, sv = 0;
+  const size_t n = (size_t)W * H;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const int x = (int)(i % W), y = (int)(i / W);
+    const float2 d = dm_at(px, i, x, W, 1) + dm_at(py, i, y, H, (size_t)W);
+    su += ddist2(d, khr[i]);
+    if (qxx) {
+      const float2 dx = dm_at(qxx, i, x, W, 1) + dm_at(qxy, i, y, H, (size_t)W);
+      const float2 dy = dm_at(qyy, i, y, H, (size_t)W) + dm_at(qxy, i, x, W, 1);
+      sv += ddist2(c2(-px[i].x, -px[i].y), dx) + ddist2(c2(-py[i].x, -py[i].y), dy);
+    }
+  }
+  su = block_sum(su);
+  __syncthreads();
+  sv = block_sum(sv);
+  if (threadIdx.x == 0) {
+    partial[2 * blockIdx.x] = su;
+    partial[2 * blockIdx.x + 1] = sv;
+  }
+}
+
 __global__ void scale_kernel(float2* __restrict__ x, float s, size_t n) {
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
     x[i] = x[i] * s;
@@ -111,6 +153,39 @@ double reduce_dist2(bool complex_, const void* a, const void* b, size_t n, cudaS
   double s = 0;
   for (double v : h) s += v;  // fixed order: deterministic
   return s;
+}
+
+// Sum of Re(a . conj(b)) over n complex elements, in double. Synchronises `st`.
+double reduce_dot_re(const float2* a, const float2* b, size_t n, cudaStream_t st) {
+  DevBuf part;
+  part.ensure(kRedBlocks * sizeof(double));
+  dot_re_kernel<<<kRedBlocks, kRedThreads, 0, st>>>(a, b, n, part.as<double>());
+  PDT_LAUNCH_CHECK();
+  count_launch();
+  std::vector<double> h(kRedBlocks);
+  PDT_CUDA_CHECK(cudaMemcpyAsync(h.data(), part.p, kRedBlocks * sizeof(double), cudaMemcpyDeviceToHost, st));
+  PDT_CUDA_CHECK(cudaStreamSynchronize(st));
+  double s = 0;
+  for (double v : h) s += v;
+  return s;
+}
+
+// {sum |div- p - K^H r|^2, sum |p + div_h- q|^2} (q null: second entry 0), in double. Synchronises `st`.
+void reduce_kkt(int W, int H, const float2* khr, const float2* px, const float2* py, const float2* qxx,
+                const float2* qyy, const float2* qxy, double out[2], cudaStream_t st) {
+  DevBuf part;
+  part.ensure(2 * kRedBlocks * sizeof(double));
+  kkt_kernel<<<kRedBlocks, kRedThreads, 0, st>>>(W, H, khr, px, py, qxx, qyy, qxy, part.as<double>());
+  PDT_LAUNCH_CHECK();
+  count_launch();
+  std::vector<double> h(2 * kRedBlocks);
+  PDT_CUDA_CHECK(cudaMemcpyAsync(h.data(), part.p, h.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
+  PDT_CUDA_CHECK(cudaStreamSynchronize(st));
+  out[0] = out[1] = 0;
+  for (int b = 0; b < kRedBlocks; ++b) {
+    out[0] += h[2 * b];
+    out[1] += h[2 * b + 1];
+  }
 }
 
 // {sum |grad+ u - v|, sum |eps(v)|_F} (TV: {sum |grad+ u|, 0}), in double. Synchronises `st`.

@@ -259,6 +259,15 @@ class _Optimizer:
         check(lib.pdt_opt_energy(self._h, _lib.stream_handle(stream), out))
         return {"total": out[0], "data": out[1], "first_order": out[2], "second_order": out[3]}
 
+    def gap(self, stream=None):
+        """FP64 primal-dual gap of a with-operator optimizer: {'gap', 'primal', 'dual', 'residual_u'
+        (|div p - K^H r|), 'residual_v' (|p + div_h q|), 'norm_khr' (|K^H r|)}; gap and residuals vanish
+        at the saddle point."""
+        out = (ctypes.c_double * 6)()
+        check(lib.pdt_opt_gap(self._h, _lib.stream_handle(stream), out))
+        keys = ("gap", "primal", "dual", "residual_u", "residual_v", "norm_khr")
+        return {k: out[i] for i, k in enumerate(keys)}
+
     def solve(self, verbose=False, stream=None):
         """Run max_iter + 1 primal-dual iterations (asynchronous when a stream is given)."""
         check(lib.pdt_opt_solve(self._h, int(bool(verbose)), _lib.stream_handle(stream)))

@@ -74,3 +74,38 @@ def test_dist2(pdt):
     got = pdt.dist2(a, b)
     want = float((a.cpu().numpy().astype(np.complex128) - b.cpu().numpy()).__abs__().__pow__(2).sum())
     assert abs(got - want) / want < 1e-12
+
+
+@pytest.mark.parametrize("variant,lam", [("tgv_mri", 1.0), ("tgv_op", 2.0), ("tv_op", 0.5)])
+def test_gap_matches_oracle(pdt, oracle, variant, lam):
+    from primaldualtoolbox import synthetic
+
+    case = synthetic.cartesian_case(C=4, H=64, W=48, roos=False, seed=3)
+    op = pdt.mri.MriCartesianOperator()
+    op.setCoilSens(case["sens"])
+    op.setMask(case["mask"])
+    cls = {"tgv_mri": pdt.mri.TgvMriOptimizer_2c3c, "tgv_op": pdt.mri.TgvOptimizer_2c3c,
+           "tv_op": pdt.mri.TvOptimizerWithOp_2c3c}[variant]
+    opt = cls()
+    prm = opt.getParameters()
+    prm.max_iter = 79
+    if variant == "tgv_mri":
+        prm.reduction = 1.0
+    else:
+        prm.Lambda = lam
+    a0, a1 = (float(np.float32(case["alpha0"])), float(np.float32(case["alpha1"])))
+    if variant != "tv_op":
+        prm.alpha0, prm.alpha1 = a0, a1
+    opt.setOperator(op)
+    opt.setNoisyData(case["rawdata"])
+    opt.solve()
+    got = opt.gap()
+    _, st = oracle.op_solve("cartesian", case["sens"], case["mask"], case["rawdata"], variant, alpha0=a0, alpha1=a1,
+                            reduction=1.0, lam=lam, max_iter=79, prec=32, return_state=True)
+    ref = oracle.op_gap("cartesian", case["sens"], case["mask"], case["rawdata"], st, variant, alpha0=a0, alpha1=a1,
+                        lam=lam)
+    for k in ("primal", "dual", "norm_khr"):
+        assert abs(got[k] - ref[k]) <= 1e-5 * abs(ref[k]), k
+    for k in ("gap", "residual_u") + (() if variant == "tv_op" else ("residual_v",)):
+        assert abs(got[k] - ref[k]) <= 2e-3 * abs(ref[k]), k
+    assert got["gap"] > 0

@@ -159,3 +159,20 @@ def test_op_solve_continues_from_state(oracle):
     u = oracle.op_solve(*args, max_iter=29, **kw)
     assert rel_l2(u2, u) < 1e-12
     assert rel_l2(oracle.op_solve(*args, max_iter=19, **kw), u) > 1e-3  # the state did carry over
+
+
+@pytest.mark.parametrize("variant,lam", [("tgv_mri", 1.0), ("tgv_op", 2.0), ("tv_op", 0.5)])
+def test_primal_dual_gap_closes(oracle, variant, lam):
+    from primaldualtoolbox import synthetic
+
+    case = synthetic.cartesian_case(C=3, H=32, W=24, roos=False, seed=8)
+    kw = dict(alpha0=case["alpha0"], alpha1=case["alpha1"], lam=lam)
+    gaps = []
+    for it in (30, 300, 3000):
+        _, st = oracle.op_solve("cartesian", case["sens"], case["mask"], case["rawdata"], variant, reduction=1.0,
+                                max_iter=it - 1, prec=64, return_state=True, **kw)
+        gaps.append(oracle.op_gap("cartesian", case["sens"], case["mask"], case["rawdata"], st, variant, **kw))
+    assert gaps[0]["gap"] > gaps[1]["gap"] > gaps[2]["gap"] > -1e-9 * gaps[2]["primal"]
+    assert gaps[2]["residual_u"] < 0.05 * gaps[0]["residual_u"]
+    if variant != "tv_op":
+        assert gaps[2]["residual_v"] < 0.05 * gaps[0]["residual_v"]
