@@ -113,6 +113,14 @@ PDT_API pdt_status pdt_op_destroy(pdt_op* op);
  * Radial: #0 trajectory F32 {Ns,2}, #1 dcf F32 {Ns,1}, #2 coil sensitivities C64 {N,N,C} (multi-coil). */
 PDT_API pdt_status pdt_op_add_constant(pdt_op* op, pdt_dtype dtype, int ndim, const int64_t* size, const void* data,
                                int is_device);
+/* Replaces constant `idx` with one of the same type and rank, ordered on `stream` (NULL: the legacy
+ * default stream, synchronised before returning). No counterpart in the reference, whose constants can
+ * only be appended; it lets one operator serve a sequence of slices without reallocation. The device
+ * buffer is kept when the size is unchanged. An F32 constant (mask, trajectory, density weights) equal
+ * to the current one is a no-op; a different one waits for the work already queued on `stream`, then
+ * rebuilds the operator's tables (given on the device, it is first read back, waiting for `stream`). */
+PDT_API pdt_status pdt_op_replace_constant(pdt_op* op, int idx, pdt_dtype dtype, int ndim, const int64_t* size,
+                                           const void* data, int is_device, void* stream);
 /* OperatorBase::getInputSize / getOutputSize (operatorbase.h:328-340). */
 PDT_API pdt_status pdt_op_input_size(pdt_op* op, int out_ndim, const int64_t* out_size, int* in_ndim, int64_t* in_size);
 PDT_API pdt_status pdt_op_output_size(pdt_op* op, int in_ndim, const int64_t* in_size, int* out_ndim, int64_t* out_size);

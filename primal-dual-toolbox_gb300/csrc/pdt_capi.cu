@@ -76,6 +76,55 @@ void OpImpl::add_constant(pdt_dtype dtype, const Dims& size, const void* data, b
   invalidate();
 }
 
+// Replacing a constant keeps its device buffer when the size is unchanged, so graphs and launch
+// parameters that point at it stay valid; the copy is ordered on `st`. F32 constants (masks,
+// trajectories, density weights) define the operator's tables: an unchanged value is a no-op, a changed
+// one waits for the work already queued on `st` (which may still read the tables), then rebuilds them
+// and starts a new generation. Complex constants (coil sensitivities) only change values the kernels
+// read, so they need neither.
+void OpImpl::replace_constant(unsigned idx, pdt_dtype dtype, const Dims& size, const void* data, bool is_device,
+                              cudaStream_t st) {
+  if (idx >= constants_.size()) {
+    std::ostringstream os;
+    os << "Operator '" << name_ << "': Requested index (" << idx
+       << ") is not valid. Constants available: " << constants_.size();
+    throw Error(PDT_ERR_CONSTANTS, os.str());
+  }
+  Constant& c = *constants_[idx];
+  if (c.dtype != dtype || c.size.size() != size.size())
+    throw Error(PDT_ERR_CONSTANTS, "Operator '" + name_ + "': constant " + std::to_string(idx) +
+                                       " can only be replaced by one of the same type and rank");
+  const size_t bytes = numel_of(size) * c.elem_bytes();
+  const bool resized = size != c.size;
+  bool changed = resized;
+  if (dtype == PDT_F32) {
+    std::vector<unsigned char> h(bytes);
+    if (bytes) {
+      if (is_device) {
+        PDT_CUDA_CHECK(cudaMemcpyAsync(h.data(), data, bytes, cudaMemcpyDeviceToHost, st));
+        PDT_CUDA_CHECK(cudaStreamSynchronize(st));
+      } else {
+        std::memcpy(h.data(), data, bytes);
+      }
+    }
+    changed = changed || h != c.host;
+    if (!changed) return;
+    PDT_CUDA_CHECK(cudaStreamSynchronize(st));
+    c.host.swap(h);
+  }
+  if (resized) {
+    c.dev.ensure(std::max<size_t>(bytes, 1));
+    c.size = size;
+  }
+  if (bytes)
+    PDT_CUDA_CHECK(cudaMemcpyAsync(c.dev.p, data, bytes, is_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                                   st));
+  if (changed) {
+    gen_ = next_generation();
+    invalidate();
+  }
+}
+
 uint64_t OpImpl::next_generation() {
   static std::atomic<uint64_t> g_gen{0};
   return ++g_gen;
@@ -968,6 +1017,19 @@ pdt_status pdt_op_add_constant(pdt_op* op, pdt_dtype dtype, int ndim, const int6
     const Dims d = dims_in(ndim, size);
     if (numel_of(d)) need(data, "data");
     op->impl->add_constant(dtype, d, data, is_device != 0);
+  });
+}
+
+pdt_status pdt_op_replace_constant(pdt_op* op, int idx, pdt_dtype dtype, int ndim, const int64_t* size,
+                                   const void* data, int is_device, void* stream) {
+  return guarded([&] {
+    need(op, "operator");
+    if (dtype != PDT_F32 && dtype != PDT_C64) throw Error(PDT_ERR_INVALID_ARGUMENT, "bad dtype");
+    if (idx < 0) throw Error(PDT_ERR_INVALID_ARGUMENT, "negative constant index");
+    const Dims d = dims_in(ndim, size);
+    if (numel_of(d)) need(data, "data");
+    op->impl->replace_constant((unsigned)idx, dtype, d, data, is_device != 0, static_cast<cudaStream_t>(stream));
+    if (!stream) PDT_CUDA_CHECK(cudaStreamSynchronize(nullptr));
   });
 }
 

@@ -61,6 +61,9 @@ class OpImpl {
 
   // OperatorBase::addConstant (operatorbase.h:238-257)
   void add_constant(pdt_dtype dtype, const Dims& size, const void* data, bool is_device);
+  // Replaces constant idx (same type and rank), stream-ordered on st (no counterpart in the reference).
+  void replace_constant(unsigned idx, pdt_dtype dtype, const Dims& size, const void* data, bool is_device,
+                        cudaStream_t st);
 
   // OperatorBase::forward / adjoint with operatorCheck (operatorbase.h:297-312, 491-506); device pointers.
   void forward(const float2* src, const Dims& src_size, float2* dst, const Dims& dst_size, cudaStream_t st);

@@ -9,7 +9,7 @@
 
 Everything runs in libpdt.so (hand-written CUDA for sm_103a); there is no CPU fallback.
 """
-from . import batch, denoising, mri  # noqa: F401
+from . import batch, denoising, mri, pipeline  # noqa: F401
 from ._lib import LIB_PATH, PdtError, launch_count, pinned_empty  # noqa: F401
 
 

@@ -131,6 +131,16 @@ class _Operator:
         size = _lib.iu_size(b.shape)
         check(lib.pdt_op_add_constant(self._h, pdt_dtype, len(b.shape), size, b.ptr, b.is_device))
 
+    def replaceConstant(self, idx, arr, stream=None):
+        """Replaces constant `idx` (same type and rank) in place, ordered on `stream` -- e.g. the coil
+        sensitivities of the next slice. No counterpart in the reference (pdt_op_replace_constant)."""
+        types = self._constant_types
+        c = types[idx] if 0 <= idx < len(types) else (np.asarray(arr).dtype, _lib.C64)  # the engine reports it
+        b = Buffer(arr, c[0])
+        size = _lib.iu_size(b.shape)
+        check(lib.pdt_op_replace_constant(self._h, int(idx), c[1], len(b.shape), size, b.ptr, b.is_device,
+                                          _lib.stream_handle(stream)))
+
     def _apply(self, adjoint, arr, out=None, stream=None):
         src = Buffer(arr, np.complex64)
         ssize = _lib.iu_size(src.shape)

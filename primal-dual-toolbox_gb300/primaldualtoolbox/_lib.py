@@ -28,7 +28,7 @@ OPT_TV, OPT_TGV, OPT_TV_OP, OPT_TGV_OP, OPT_TGV_MRI = range(5)
 EXPORTED = ["pdt_last_error", "pdt_version", "pdt_launch_count", "pdt_host_alloc", "pdt_host_free",
             "pdt_stream_synchronize", "pdt_op_create", "pdt_op_destroy", "pdt_op_add_constant", "pdt_op_input_size",
             "pdt_op_output_size", "pdt_op_forward", "pdt_op_adjoint", "pdt_op_describe", "pdt_op_adjointness",
-            "pdt_op_tuning",
+            "pdt_op_tuning", "pdt_op_replace_constant",
             "pdt_opt_create", "pdt_opt_destroy", "pdt_opt_get_params", "pdt_opt_set_params", "pdt_opt_set_operator",
             "pdt_opt_set_noisy_data", "pdt_opt_set_input0", "pdt_opt_solve", "pdt_opt_result_size",
             "pdt_opt_get_result", "pdt_opt_profile", "pdt_opt_set_input0_uv", "pdt_opt_get_field", "pdt_opt_energy",
@@ -94,6 +94,7 @@ def _load():
     L.pdt_opt_get_field.argtypes = [vp, i, vp, i, vp]
     L.pdt_opt_energy.argtypes = [vp, vp, ctypes.POINTER(ctypes.c_double)]
     L.pdt_opt_gap.argtypes = [vp, vp, ctypes.POINTER(ctypes.c_double)]
+    L.pdt_op_replace_constant.argtypes = [vp, i, i, i, ctypes.POINTER(ctypes.c_int64), vp, i, vp]
     L.pdt_op_norm.argtypes = [vp, i, ctypes.c_uint64, ctypes.POINTER(ctypes.c_double)]
     L.pdt_dist2.argtypes = [i, vp, vp, ctypes.c_size_t, vp, ctypes.POINTER(ctypes.c_double)]
     L.pdt_batch_create.argtypes = [ctypes.POINTER(vp)]

@@ -18,8 +18,10 @@ __all__ = ["TgvMriParameters", "TgvParameters", "TvParameters", "MriCartesianOpe
 
 
 class MriCartesianOperator(_Operator):
-    """Multi-coil Cartesian operator: constants setCoilSens (#0) then setMask (#1), in that order."""
+    """Multi-coil Cartesian operator: constants setCoilSens (#0) then setMask (#1), in that order.
+    replaceCoilSens / replaceMask swap them in place for the next slice (no reference counterpart)."""
     _kind = _lib.OP_CARTESIAN
+    _constant_types = ((np.complex64, _lib.C64), (np.float32, _lib.F32))
 
     def __init__(self):
         super().__init__(None)
@@ -29,6 +31,12 @@ class MriCartesianOperator(_Operator):
 
     def setCoilSens(self, sens):
         self._add_constant(sens, np.complex64, _lib.C64)
+
+    def replaceCoilSens(self, sens, stream=None):
+        self.replaceConstant(0, sens, stream)
+
+    def replaceMask(self, mask, stream=None):
+        self.replaceConstant(1, mask, stream)
 
 
 class MriCartesianRemoveROOSOperator(MriCartesianOperator):
@@ -39,6 +47,7 @@ class MriCartesianRemoveROOSOperator(MriCartesianOperator):
 class MriSamplingOperator(_Operator):
     """Single-coil centred FFT + mask; constant setMask (#0)."""
     _kind = _lib.OP_SAMPLING
+    _constant_types = ((np.float32, _lib.F32),)
 
     def __init__(self):
         super().__init__(None)
@@ -46,11 +55,15 @@ class MriSamplingOperator(_Operator):
     def setMask(self, mask):
         self._add_constant(mask, np.float32, _lib.F32)
 
+    def replaceMask(self, mask, stream=None):
+        self.replaceConstant(0, mask, stream)
+
 
 class MriRadialOperator(_Operator):
     """Radial multi-coil operator; config dict with osf, sector_width, kernel_width, img_dim.
     Constants in order: setTrajectory (2, Ns) float32, setDcf (1, Ns) float32, setCoilSens (C, N, N)."""
     _kind = _lib.OP_RADIAL
+    _constant_types = ((np.float32, _lib.F32), (np.float32, _lib.F32), (np.complex64, _lib.C64))
 
     def __init__(self, config):
         super().__init__(config)
@@ -64,10 +77,20 @@ class MriRadialOperator(_Operator):
     def setCoilSens(self, sens):
         self._add_constant(sens, np.complex64, _lib.C64)
 
+    def replaceTrajectory(self, traj, stream=None):
+        self.replaceConstant(0, traj, stream)
+
+    def replaceDcf(self, dcf, stream=None):
+        self.replaceConstant(1, dcf, stream)
+
+    def replaceCoilSens(self, sens, stream=None):
+        self.replaceConstant(2, sens, stream)
+
 
 class MriRadialSinglecoilOperator(_Operator):
     """Radial single-coil operator; constants setTrajectory then setDcf."""
     _kind = _lib.OP_RADIAL_SINGLECOIL
+    _constant_types = ((np.float32, _lib.F32), (np.float32, _lib.F32))
 
     def __init__(self, config):
         super().__init__(config)
@@ -77,6 +100,12 @@ class MriRadialSinglecoilOperator(_Operator):
 
     def setDcf(self, dcf):
         self._add_constant(dcf, np.float32, _lib.F32)
+
+    def replaceTrajectory(self, traj, stream=None):
+        self.replaceConstant(0, traj, stream)
+
+    def replaceDcf(self, dcf, stream=None):
+        self.replaceConstant(1, dcf, stream)
 
 
 _OPS_3C = (MriCartesianOperator, MriCartesianRemoveROOSOperator)
