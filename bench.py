@@ -304,6 +304,10 @@ def run_ours(args):
                     "h2d_bytes_per_slice": int(2 * C * H * W * 8), "d2h_bytes_per_slice": int((H // 2) * W * 8),
                     "note": "host rawdata + coil maps in, host image out; same mask for all slices"}
 
+    radial = None
+    if args.radial_slices > 0:
+        radial = run_radial(pdt, torch, args.radial_slices, args.radial_iters)
+
     batched = None
     if args.batch_cases > 0:
         batched = run_batched(pdt, torch, args.batch_cases, args.batch_iters, steps=2, warmup=1)
@@ -332,6 +336,7 @@ def run_ours(args):
             "time_to_1e-4": conv,
             "e2e_streamed": streamed,
             "batched": batched,
+            "radial": radial,
             "clocks": clk.summary(),
             "wall_s": round(wall, 3),
         }
@@ -542,6 +547,86 @@ def run_batched(pdt, torch, n_cases, iters, steps, warmup):
             "case_generation_s": round(t_gen, 1)}
 
 
+RAD_N, RAD_C, RAD_SPOKES, RAD_RO, RAD_OSF, RAD_KW = 256, 12, 64, 512, 1.5, 3
+
+
+def _radial_problem(pdt, seed):
+    """Config 5: 256 x 256 image, 12 coils, 64 golden-angle spokes x 512 readout samples (2x readout
+    oversampling), Kaiser-Bessel width 3 on a 1.5x grid, density weights sqrt|k|, a seeded phantom and
+    seeded coil maps; f = A u + 1 % complex noise."""
+    from primaldualtoolbox import synthetic
+
+    ang = np.arange(RAD_SPOKES) * np.pi * (np.sqrt(5) - 1) / 2
+    r = (np.arange(RAD_RO) - RAD_RO / 2) / RAD_RO
+    k = (r[:, None] * np.exp(1j * ang[None, :])).ravel()
+    traj = np.array([k.imag, k.real]).astype(np.float32)  # [imag, real] as bin/mri_radial_test.py:38
+    dcf = np.sqrt(np.abs(k)).astype(np.float32)[None, :]
+    op = pdt.mri.MriRadialOperator({"osf": RAD_OSF, "sector_width": 8, "kernel_width": RAD_KW, "img_dim": RAD_N})
+    op.setTrajectory(traj)
+    op.setDcf(dcf)
+    op.setCoilSens(synthetic.coil_maps(RAD_C, RAD_N, RAD_N, seed=seed))
+    f = op.forward(synthetic.mri_phantom(RAD_N, RAD_N, seed=seed))
+    rng = np.random.default_rng(seed)
+    f = f + (0.01 * np.abs(f).max() * (rng.standard_normal(f.shape) + 1j * rng.standard_normal(f.shape))).astype(
+        np.complex64)
+    alpha1 = 0.02 * float(np.abs(op.adjoint(f)).max())
+    return op, f, alpha1
+
+
+def _radial_bytes():
+    """Algorithmic bytes of one radial TGV-MRI iteration, each array pass counted once: image x coil maps
+    in and out, the padded row transforms and the oversampled grid written and read in both directions,
+    the samples' dual r (read, write), data and weights, and the image side (dual 13 + primal 15 planes)."""
+    G = int(np.ceil(RAD_OSF * RAD_N))
+    Ns = RAD_SPOKES * RAD_RO
+    c8 = 8
+    fwd = c8 * (RAD_N * RAD_N * (1 + RAD_C) + 2 * RAD_C * RAD_N * G + 2 * RAD_C * G * G)
+    prox = c8 * RAD_C * Ns * 4 + 4 * Ns
+    adj = c8 * (2 * RAD_C * G * G + 2 * RAD_C * RAD_N * G + RAD_N * RAD_N * (RAD_C + 1))
+    return fwd + prox + adj + c8 * RAD_N * RAD_N * 28
+
+
+def run_radial(pdt, torch, slices, iters):
+    """Config 5: one radial slice alone, and `slices` slices advanced together (BatchSolver)."""
+    probs = [_radial_problem(pdt, seed=s) for s in range(slices)]
+    opts = []
+    for op, f, a1 in probs:
+        opt = pdt.mri.TgvMriOptimizer_2c2c()
+        prm = opt.getParameters()
+        prm.max_iter, prm.reduction, prm.alpha1 = iters - 1, 2.0 ** -8, a1
+        prm.alpha0 = 2 * a1
+        opt.setOperator(op)
+        opt.setNoisyData(f)
+        opts.append(opt)
+    stream = torch.cuda.current_stream()
+    hbm, src = _peaks()
+    nbytes = _radial_bytes()
+
+    def timed(fn, reps):
+        fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / 1e3 / reps
+
+    t1 = timed(lambda: opts[0].solve(stream=stream), 3)
+    batch = pdt.batch.BatchSolver(opts)
+    tb = timed(lambda: batch.solve(stream=stream), 2)
+    return {"workload": f"radial_tgv2_{RAD_C}c_{RAD_N}x{RAD_N}_{RAD_SPOKES}spokes_x{RAD_RO}",
+            "osf": RAD_OSF, "kernel_width": RAD_KW, "iterations_per_slice": iters, "tuning": probs[0][0].tuning(),
+            "single_slice": {"value": round(iters / t1, 1), "unit": "iters/s"},
+            "batched": {"slices": slices, "value": round(slices * iters / tb, 1), "unit": "slice-iterations/s",
+                        "roofline": {"bound": "hbm", "kernel": "whole iteration (all phases)",
+                                     "achieved": round(nbytes * slices * iters / tb / 1e9, 1), "peak": hbm,
+                                     "peak_source": src, "unit": "GB/s",
+                                     "frac": round(nbytes * slices * iters / tb / 1e9 / hbm, 4),
+                                     "algorithmic_bytes_per_slice_iteration": int(nbytes)}}}
+
+
 def run_ncu_case(args):
     """The workload's kernels for an ncu capture: operator set-up, autotuning and graph capture run first,
     then one solve of --ncu-iters iterations runs between cudaProfilerStart and cudaProfilerStop, so
@@ -618,6 +703,8 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--accuracy", type=int, default=1, help="measure iterations/time to rel-L2 1e-4 (1) or skip (0)")
     ap.add_argument("--stream-slices", type=int, default=12, help="streamed e2e leg: slices (0 skips)")
+    ap.add_argument("--radial-slices", type=int, default=32, help="radial leg (config 5): slices (0 skips)")
+    ap.add_argument("--radial-iters", type=int, default=200, help="radial leg: iterations per slice")
     ap.add_argument("--batch-cases", type=int, default=64, help="batched leg: independent problems (0 skips)")
     ap.add_argument("--batch-iters", type=int, default=200, help="batched leg: iterations per problem and step")
     ap.add_argument("--ncu-iters", type=int, default=0,

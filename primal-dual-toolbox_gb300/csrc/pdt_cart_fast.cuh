@@ -2,13 +2,8 @@
 // compiled split n = M * L (L = 8, 16 or 32 lanes per sequence, M values per lane). Included by
 // pdt_cartesian.cu after CartDev.
 //
-// LaneFft<M, L>: lane t of a group of L lanes holds x[t + L j] (j < M) in registers. The forward
-// transform is an M-point register FFT per lane, a twiddle w_n^(t k1), and an L-point FFT across the
-// lanes (radix-2 decimation in frequency, one __shfl_xor_sync butterfly per stage and value):
-//   X[k1 + M k2] = sum_t w_L^(t k2) w_n^(t k1) sum_j w_M^(j k1) x[t + L j]
-// leaving X[k1 + M brev_L(t)] in register k1 of lane t. The inverse runs the same network backwards
-// (decimation in time) with conjugate twiddles, from that order back to natural order. Every lane
-// works in every stage and no shared-memory exchange is needed.
+// The transforms are LaneFft<M, L> (pdt_regfft.cuh): lane t of a group of L lanes holds x[t + L j] in
+// registers and ends with X[k1 + M brev_L(t)] in register k1.
 //
 // Kernels (one sequence per lane group; 32 / L sequences per warp):
 //   fl_rows_fwd   rows of ubar . sens_c -> FFT along W -> sampled columns t1[c][s][yi]
@@ -27,66 +22,6 @@ namespace cg = cooperative_groups;
 
 namespace pdt {
 namespace {
-
-constexpr int ct_log2(int n) { return n <= 1 ? 0 : 1 + ct_log2(n / 2); }
-
-__device__ __forceinline__ float2 shfl_xor2(float2 v, int m) {
-  return c2(__shfl_xor_sync(0xffffffffu, v.x, m), __shfl_xor_sync(0xffffffffu, v.y, m));
-}
-
-// bit reversal of t over log2(L) bits
-template <int L>
-__device__ __forceinline__ int lane_brev(int t) {
-  return (int)(__brev((unsigned)t) >> (32 - ct_log2(L)));
-}
-
-template <int M, int L>
-struct LaneFft {
-  static_assert(L == 8 || L == 16 || L == 32, "lanes per sequence");
-  static constexpr int n = M * L;
-
-  // Forward: v[j] = x[t + L j] on entry; v[k1] = X[k1 + M brev_L(t)] on exit. tw[i] = exp(-2 pi i i / n).
-  static __device__ __forceinline__ void fwd(float2 (&v)[M], int t, const float2* __restrict__ tw) {
-    reg_fft<M, L>(v, tw, -1.f);
-#pragma unroll
-    for (int k1 = 1; k1 < M; ++k1) v[k1] = cmul(v[k1], tw[t * k1]);  // t k1 < n
-    // stage h: the lower lane of a pair keeps a + b, the upper (p - v) w_2h^(t mod h); the last stage
-    // (h = 1) has no twiddle
-#pragma unroll
-    for (int h = L / 2; h >= 1; h >>= 1) {
-      const bool up = (t & h) != 0;
-      const float sg = up ? -1.f : 1.f;
-      float2 w = c2(1.f, 0.f);
-      if (h > 1 && up) w = tw[(t & (h - 1)) * (n / (2 * h))];
-#pragma unroll
-      for (int k1 = 0; k1 < M; ++k1) {
-        const float2 p = shfl_xor2(v[k1], h);
-        const float2 y = c2(fmaf(sg, v[k1].x, p.x), fmaf(sg, v[k1].y, p.y));
-        v[k1] = (h > 1) ? cmul(y, w) : y;
-      }
-    }
-  }
-
-  // Unnormalised inverse: v[k1] = Z[k1 + M brev_L(t)] on entry; v[j] = n z[t + L j] on exit.
-  static __device__ __forceinline__ void inv(float2 (&v)[M], int t, const float2* __restrict__ tw) {
-#pragma unroll
-    for (int h = 1; h < L; h <<= 1) {
-      const bool up = (t & h) != 0;
-      const float sg = up ? -1.f : 1.f;
-      float2 w = c2(1.f, 0.f);
-      if (h > 1 && up) w = conjf2(tw[(t & (h - 1)) * (n / (2 * h))]);
-#pragma unroll
-      for (int k1 = 0; k1 < M; ++k1) {
-        const float2 m = (h > 1) ? cmul(v[k1], w) : v[k1];
-        const float2 p = shfl_xor2(m, h);
-        v[k1] = c2(fmaf(sg, m.x, p.x), fmaf(sg, m.y, p.y));  // lower m + p, upper p - m
-      }
-    }
-#pragma unroll
-    for (int k1 = 1; k1 < M; ++k1) v[k1] = cmul(v[k1], conjf2(tw[t * k1]));
-    reg_fft<M, L>(v, tw, 1.f);
-  }
-};
 
 // Phase 1: rows of ubar . sens_c -> FFT along W -> sampled columns t1[c][s][yi]. A block takes
 // R = WPB * 32 / L consecutive rows of one coil and writes each sampled column's R rows as one run.

@@ -14,8 +14,9 @@
 //   rad_rows_fwd   image rows . sens_c / deap  -> zero-padded FFT along x   -> T[c][gx][image row]
 //   rad_cols       FFT along y of each grid column (input on the N image rows) -> F[c][gx][gy]
 //   rad_degrid     per sample: 9 (W^2) taps of F, dcf weight; solver mode adds the k-space dual prox
-//   rad_grid       gridding as a gather: one block per 16 x 16 grid tile walks the samples that touch it
-//                  in sample order (lists built at set-up) -- deterministic, no atomics
+//   rad_grid       gridding as a gather: one thread per grid cell walks the samples whose footprint covers
+//                  the cell, in sample order, with their tap weights (lists built at set-up) --
+//                  deterministic, no atomics
 //   rad_cols_inv   IFFT along y of each grid column, keep the N image rows
 //   rad_rows_inv   IFFT along x, crop, / deap, conj(sens_c) . and the coil sum
 #include <algorithm>
@@ -31,11 +32,9 @@ namespace pdt {
 namespace {
 
 constexpr int kRT = 256;   // threads per block
-constexpr int kTile = 16;  // gridding tile edge (grid cells)
 constexpr int kMaxKw = 8;  // largest supported kernel width
 constexpr int kRR = 4;     // rows per block in the row passes
 constexpr int kRC = 4;     // columns per block in the column passes
-constexpr int kChunk = 64; // samples staged per chunk in the gridding gather
 
 struct RadDev {
   int N, G, C, Ns, kw;
@@ -47,9 +46,9 @@ struct RadDev {
   const float* w;       // [Ns] density compensation
   const int* g0;        // [2*Ns] gx0, gy0 (may be negative; wrap mod G)
   const float* wt;      // [Ns][2][kw] tap weights (x then y)
-  const int* tile_ptr;  // [ntiles+1]
-  const int* tile_idx;  // sample indices per tile, ascending
-  int tiles_x;          // G / kTile rounded up
+  const int* cell_ptr;  // [G*G+1] per grid cell gx * G + gy: range of its entries
+  const int* cell_idx;  // samples whose footprint covers the cell, ascending
+  const float* cell_w;  // their tap weights wx * wy
   const float2* tw;     // [G]
   FftPlan plan;
 };
@@ -109,7 +108,7 @@ __global__ void __launch_bounds__(kRT) rad_cols(RadDev d, const float2* __restri
 }
 
 // Degridding. mode 0: kout[c][j] = A u. mode 1 (solver): r <- (r + sigma (A u - f)) / (1 + sigma lambda),
-// s[c][j] = w_j r (the weighted values the adjoint grids).
+// s[j][c] = w_j r (the weighted values the adjoint grids, sample-major).
 __global__ void __launch_bounds__(kRT) rad_degrid(RadDev d, int mode, const float2* __restrict__ F,
                                                   float2* __restrict__ kout, float2* __restrict__ r,
                                                   const float2* __restrict__ f, float2* __restrict__ s,
@@ -142,65 +141,62 @@ __global__ void __launch_bounds__(kRT) rad_degrid(RadDev d, int mode, const floa
     } else {
       const float2 rn = (r[o] + sigma * (a - f[o])) / (1.0f + sigma * lambda);
       r[o] = rn;
-      s[o] = rn * wj;
+      s[(size_t)j * d.C + c] = rn * wj;  // sample-major for the gridding gather
     }
   }
 }
 
-// s[c][j] = w_j k[c][j] (adjoint input weighting for a dense k-space).
+// s[j][c] = w_j k[c][j] (adjoint input weighting for a dense k-space, sample-major).
 __global__ void rad_weight(RadDev d, const float2* __restrict__ k, float2* __restrict__ s) {
   const size_t n = (size_t)d.C * d.Ns;
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
-    s[i] = k[i] * d.w[i % d.Ns];
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const size_t c = i / d.Ns, j = i - c * d.Ns;
+    s[j * d.C + c] = k[i] * d.w[j];
+  }
 }
 
-// Gridding as a gather over the samples whose footprint touches this 16 x 16 tile, in sample order.
-// H[c][gx][gy] receives sum_j s[c][j] wx[gx - gx0_j] wy[gy - gy0_j] for every coil.
+// Gridding as a gather: H[c][gx][gy] = sum_j s[j][c] wx[gx - gx0_j] wy[gy - gy0_j] over the samples j whose
+// footprint covers the cell, in sample order (so the result does not depend on scheduling). A sample's
+// coil values are contiguous, and four entries are fetched at a time so that the cells near k = 0, whose
+// lists are longest, keep many loads in flight.
 template <int MAXC>
 __global__ void __launch_bounds__(kRT) rad_grid(RadDev d, const float2* __restrict__ s, float2* __restrict__ H) {
-  __shared__ int s_g0[2 * kChunk];
-  __shared__ float s_wt[kChunk * 2 * kMaxKw];
-  __shared__ float2 s_val[kChunk * MAXC];
-  const int tile = blockIdx.x;
-  const int tx0 = (tile % d.tiles_x) * kTile, ty0 = (tile / d.tiles_x) * kTile;
-  const int lx = threadIdx.x / kTile, ly = threadIdx.x % kTile;  // ly fastest -> coalesced along gy
-  const int gx = tx0 + lx, gy = ty0 + ly;
-  const bool inside = gx < d.G && gy < d.G;
-  const int kw = d.kw;
+  const size_t ncell = (size_t)d.G * d.G;
+  const size_t cell = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (cell >= ncell) return;
+  const int beg = d.cell_ptr[cell], end = d.cell_ptr[cell + 1];
   for (int cbase = 0; cbase < d.C; cbase += MAXC) {
     const int nc = min(MAXC, d.C - cbase);
     float2 acc[MAXC];
 #pragma unroll
     for (int c = 0; c < MAXC; ++c) acc[c] = c2(0.f, 0.f);
-    const int beg = d.tile_ptr[tile], end = d.tile_ptr[tile + 1];
-    for (int p0 = beg; p0 < end; p0 += kChunk) {
-      const int n = min(kChunk, end - p0);
-      __syncthreads();
-      for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        const int j = d.tile_idx[p0 + i];
-        s_g0[2 * i] = d.g0[2 * j];
-        s_g0[2 * i + 1] = d.g0[2 * j + 1];
-        for (int t = 0; t < 2 * kw; ++t) s_wt[i * 2 * kMaxKw + t] = d.wt[(size_t)j * 2 * kw + t];
-      }
-      for (int i = threadIdx.x; i < n * nc; i += blockDim.x) {
-        const int q = i / nc, c = i - q * nc;
-        s_val[q * MAXC + c] = s[(size_t)(cbase + c) * d.Ns + d.tile_idx[p0 + q]];
-      }
-      __syncthreads();
-      if (inside) {
-        for (int q = 0; q < n; ++q) {
-          const int dx = wrapG(gx - s_g0[2 * q], d.G), dy = wrapG(gy - s_g0[2 * q + 1], d.G);
-          if (dx < kw && dy < kw) {
-            const float wgt = s_wt[q * 2 * kMaxKw + dx] * s_wt[q * 2 * kMaxKw + kw + dy];
+    int e = beg;
+    for (; e + 4 <= end; e += 4) {
+      const float2* s0 = s + (size_t)d.cell_idx[e] * d.C + cbase;
+      const float2* s1 = s + (size_t)d.cell_idx[e + 1] * d.C + cbase;
+      const float2* s2 = s + (size_t)d.cell_idx[e + 2] * d.C + cbase;
+      const float2* s3 = s + (size_t)d.cell_idx[e + 3] * d.C + cbase;
+      const float w0 = d.cell_w[e], w1 = d.cell_w[e + 1], w2 = d.cell_w[e + 2], w3 = d.cell_w[e + 3];
 #pragma unroll
-            for (int c = 0; c < MAXC; ++c)
-              if (c < nc) acc[c] += s_val[q * MAXC + c] * wgt;
-          }
+      for (int c = 0; c < MAXC; ++c)
+        if (c < nc) {
+          const float2 a0 = s0[c], a1 = s1[c], a2 = s2[c], a3 = s3[c];
+          acc[c] += a0 * w0;
+          acc[c] += a1 * w1;
+          acc[c] += a2 * w2;
+          acc[c] += a3 * w3;
         }
-      }
     }
-    if (inside)
-      for (int c = 0; c < nc; ++c) H[((size_t)(cbase + c) * d.G + gx) * d.G + gy] = acc[c];
+    for (; e < end; ++e) {
+      const float2* sj = s + (size_t)d.cell_idx[e] * d.C + cbase;
+      const float wgt = d.cell_w[e];
+#pragma unroll
+      for (int c = 0; c < MAXC; ++c)
+        if (c < nc) acc[c] += sj[c] * wgt;
+    }
+#pragma unroll
+    for (int c = 0; c < MAXC; ++c)
+      if (c < nc) H[(size_t)(cbase + c) * ncell + cell] = acc[c];
   }
 }
 
@@ -261,6 +257,14 @@ __global__ void __launch_bounds__(kRT) rad_rows_inv(RadDev d, const float2* __re
 }
 
 int g_rad_sms = 0, g_rad_smem = 0;
+
+}  // namespace
+}  // namespace pdt
+
+#include "pdt_rad_fast.cuh"
+
+namespace pdt {
+namespace {
 
 // Kaiser-Bessel kernel and its continuous Fourier transform (host, double precision).
 double kb(double dd, int kw, double beta) {
@@ -396,6 +400,20 @@ class RadialOp : public OpImpl, public SolverHooks {
 
   // grid_ <- FFT2 of the deapodised, zero-padded coil images.
   void forward_grid(const float2* u, cudaStream_t st, PhaseMarker* mk) {
+    if (fast_.ok()) {
+      const int R = fast_.per_block();
+      fast_.rows_fwd<<<dim3((dev_.N + R - 1) / R, dev_.C), 32 * kRadWpb, rad_fast_rows_smem(fast_), st>>>(
+          dev_, u, tbuf_.as<float2>());
+      PDT_LAUNCH_CHECK();
+      count_launch();
+      if (mk) mk->mark("rad_rows_fwd", st);
+      fast_.cols<<<dim3((dev_.G + R - 1) / R, dev_.C), 32 * kRadWpb, rad_fast_cols_smem(fast_), st>>>(
+          dev_, tbuf_.as<float2>(), grid_.as<float2>());
+      PDT_LAUNCH_CHECK();
+      count_launch();
+      if (mk) mk->mark("rad_cols_fwd", st);
+      return;
+    }
     const size_t smr = sizeof(float2) * ((size_t)dev_.G + 2 * (size_t)kRR * dev_.ldG);
     const size_t smc = sizeof(float2) * ((size_t)dev_.G + 2 * (size_t)kRC * dev_.ldG);
     rad_rows_fwd<<<dim3((dev_.N + kRR - 1) / kRR, dev_.C), kRT, smr, st>>>(dev_, u, tbuf_.as<float2>());
@@ -410,16 +428,30 @@ class RadialOp : public OpImpl, public SolverHooks {
 
   // out (G partial images) <- K^H applied to the already weighted samples s.
   void adjoint_from_weighted(const float2* s, float2* out, int G, cudaStream_t st, PhaseMarker* mk) {
-    const int ntiles = dev_.tiles_x * dev_.tiles_x;
+    const int nblk = (int)(((size_t)dev_.G * dev_.G + kRT - 1) / kRT);
     if (dev_.C <= 4)
-      rad_grid<4><<<ntiles, kRT, 0, st>>>(dev_, s, grid_.as<float2>());
+      rad_grid<4><<<nblk, kRT, 0, st>>>(dev_, s, grid_.as<float2>());
     else if (dev_.C <= 8)
-      rad_grid<8><<<ntiles, kRT, 0, st>>>(dev_, s, grid_.as<float2>());
+      rad_grid<8><<<nblk, kRT, 0, st>>>(dev_, s, grid_.as<float2>());
     else
-      rad_grid<16><<<ntiles, kRT, 0, st>>>(dev_, s, grid_.as<float2>());
+      rad_grid<16><<<nblk, kRT, 0, st>>>(dev_, s, grid_.as<float2>());
     PDT_LAUNCH_CHECK();
     count_launch();
     if (mk) mk->mark("rad_grid", st);
+    if (fast_.ok()) {
+      const int R = fast_.per_block();
+      fast_.cols_inv<<<dim3((dev_.G + R - 1) / R, dev_.C), 32 * kRadWpb, rad_fast_cols_smem(fast_), st>>>(
+          dev_, grid_.as<float2>(), tbuf_.as<float2>());
+      PDT_LAUNCH_CHECK();
+      count_launch();
+      if (mk) mk->mark("rad_cols_inv", st);
+      fast_.rows_inv<<<dim3((dev_.N + R - 1) / R, G), 32 * kRadWpb, rad_fast_rows_inv_smem(fast_, dev_.N), st>>>(
+          dev_, tbuf_.as<float2>(), out, G, (long long)dev_.N * dev_.N);
+      PDT_LAUNCH_CHECK();
+      count_launch();
+      if (mk) mk->mark("rad_rows_inv", st);
+      return;
+    }
     const size_t smc = sizeof(float2) * ((size_t)dev_.G + 2 * (size_t)kRC * dev_.ldG);
     rad_cols_inv<<<dim3((dev_.G + kRC - 1) / kRC, dev_.C), kRT, smc, st>>>(dev_, grid_.as<float2>(),
                                                                            tbuf_.as<float2>());
@@ -492,32 +524,30 @@ class RadialOp : public OpImpl, public SolverHooks {
       }
     }
     for (int x = 0; x < N; ++x) deap[x] = (float)kb_ft(x - N / 2, G, kw, beta);
-    const int tx = (G + kTile - 1) / kTile;
-    d.tiles_x = tx;
-    std::vector<std::vector<int>> lists((size_t)tx * tx);
+    // per-cell gather lists: every (sample, tap) pair lands in the list of the grid cell it covers;
+    // samples are visited in ascending order, so each list is ascending
     auto wrap = [G](int g) { g %= G; return g < 0 ? g + G : g; };
-    for (int j = 0; j < Ns; ++j) {
-      int seen[kMaxKw * kMaxKw], ns = 0;
+    const size_t ncell = (size_t)G * G;
+    std::vector<int> ptr(ncell + 1, 0);
+    for (int j = 0; j < Ns; ++j)
       for (int ty = 0; ty < kw; ++ty)
-        for (int txx = 0; txx < kw; ++txx) {
-          const int t = (wrap(g0[2 * j + 1] + ty) / kTile) * tx + wrap(g0[2 * j] + txx) / kTile;
-          bool dup = false;
-          for (int q = 0; q < ns; ++q) dup |= seen[q] == t;
-          if (!dup) {
-            seen[ns++] = t;
-            lists[t].push_back(j);
-          }
+        for (int txx = 0; txx < kw; ++txx)
+          ++ptr[(size_t)wrap(g0[2 * j] + txx) * G + wrap(g0[2 * j + 1] + ty) + 1];
+    for (size_t c = 0; c < ncell; ++c) ptr[c + 1] += ptr[c];
+    std::vector<int> idx((size_t)ptr[ncell]), fill(ptr.begin(), ptr.end() - 1);
+    std::vector<float> cw(idx.size());
+    for (int j = 0; j < Ns; ++j)
+      for (int txx = 0; txx < kw; ++txx)
+        for (int ty = 0; ty < kw; ++ty) {
+          const size_t cell = (size_t)wrap(g0[2 * j] + txx) * G + wrap(g0[2 * j + 1] + ty);
+          const int e = fill[cell]++;
+          idx[e] = j;
+          cw[e] = wt[((size_t)j * 2 + 0) * kw + txx] * wt[((size_t)j * 2 + 1) * kw + ty];
         }
-    }
-    std::vector<int> ptr(lists.size() + 1, 0), idx;
-    for (size_t t = 0; t < lists.size(); ++t) {
-      ptr[t + 1] = ptr[t] + (int)lists[t].size();
-      idx.insert(idx.end(), lists[t].begin(), lists[t].end());
-    }
     std::vector<float2> tw(G);
     fill_twiddles(G, tw.data());
     std::vector<float> w(dcf, dcf + Ns);
-    const size_t need = 64 * 8 + sizeof(float2) * G + sizeof(float) * (N + (size_t)Ns + wt.size()) +
+    const size_t need = 64 * 9 + sizeof(float2) * G + sizeof(float) * (N + (size_t)Ns + wt.size() + cw.size()) +
                         sizeof(int) * (g0.size() + ptr.size() + idx.size());
     tables_.ensure(need);
     char* base = tables_.as<char>();
@@ -534,12 +564,24 @@ class RadialOp : public OpImpl, public SolverHooks {
     d.w = reinterpret_cast<const float*>(put(w.data(), sizeof(float) * Ns));
     d.wt = reinterpret_cast<const float*>(put(wt.data(), sizeof(float) * wt.size()));
     d.g0 = reinterpret_cast<const int*>(put(g0.data(), sizeof(int) * g0.size()));
-    d.tile_ptr = reinterpret_cast<const int*>(put(ptr.data(), sizeof(int) * ptr.size()));
-    d.tile_idx = reinterpret_cast<const int*>(put(idx.data(), sizeof(int) * idx.size()));
+    d.cell_ptr = reinterpret_cast<const int*>(put(ptr.data(), sizeof(int) * ptr.size()));
+    d.cell_idx = reinterpret_cast<const int*>(put(idx.data(), sizeof(int) * idx.size()));
+    d.cell_w = reinterpret_cast<const float*>(put(cw.data(), sizeof(float) * cw.size()));
     tbuf_.ensure(sizeof(float2) * (size_t)C * G * N);
     grid_.ensure(sizeof(float2) * (size_t)C * G * G);
     svals_.ensure(sizeof(float2) * std::max<size_t>((size_t)C * Ns, 1));
-    const int row_blocks = (N + kRR - 1) / kRR;
+    // lane-FFT passes where the grid length has a compiled split
+    fast_ = find_rad_kernels(G);
+    if (fast_.ok() && (rad_fast_rows_inv_smem(fast_, N) > (size_t)g_rad_smem ||
+                       rad_fast_cols_smem(fast_) > (size_t)g_rad_smem))
+      fast_ = RadFastKernels();
+    if (fast_.ok()) {
+      for (const void* fn : {(const void*)fast_.rows_fwd, (const void*)fast_.cols, (const void*)fast_.cols_inv,
+                             (const void*)fast_.rows_inv})
+        PDT_CUDA_CHECK(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, g_rad_smem));
+    }
+    const int rows_per_block = fast_.ok() ? fast_.per_block() : kRR;
+    const int row_blocks = (N + rows_per_block - 1) / rows_per_block;
     G_ = std::max(1, std::min(C, (2 * g_rad_sms + row_blocks - 1) / row_blocks));
     dev_ = d;
     prepared_ = true;
@@ -549,6 +591,7 @@ class RadialOp : public OpImpl, public SolverHooks {
   int64_t sector_width_ = 0, kernel_width_ = 0, img_dim_ = 0;
   bool prepared_ = false;
   RadDev dev_{};
+  RadFastKernels fast_;
   int G_ = 1;
   DevBuf tables_, tbuf_, grid_, svals_;
 };
