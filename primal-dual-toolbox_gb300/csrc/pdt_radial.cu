@@ -35,6 +35,7 @@ constexpr int kRT = 256;   // threads per block
 constexpr int kMaxKw = 8;  // largest supported kernel width
 constexpr int kRR = 4;     // rows per block in the row passes
 constexpr int kRC = 4;     // columns per block in the column passes
+constexpr int kHeavy = 12; // gridding: cells with longer sample lists get a warp each
 
 struct RadDev {
   int N, G, C, Ns, kw;
@@ -49,6 +50,8 @@ struct RadDev {
   const int* cell_ptr;  // [G*G+1] per grid cell gx * G + gy: range of its entries
   const int* cell_idx;  // samples whose footprint covers the cell, ascending
   const float* cell_w;  // their tap weights wx * wy
+  const int* heavy;     // cells with more than kHeavy entries (gridded one warp per cell)
+  int n_heavy;
   const float2* tw;     // [G]
   FftPlan plan;
 };
@@ -108,7 +111,9 @@ __global__ void __launch_bounds__(kRT) rad_cols(RadDev d, const float2* __restri
 }
 
 // Degridding. mode 0: kout[c][j] = A u. mode 1 (solver): r <- (r + sigma (A u - f)) / (1 + sigma lambda),
-// s[j][c] = w_j r (the weighted values the adjoint grids, sample-major).
+// s[j][c] = w_j r (the weighted values the adjoint grids, sample-major). Coils in chunks of MAXC, fully
+// unrolled, so that every tap load of a chunk is in flight at once.
+template <int MAXC>
 __global__ void __launch_bounds__(kRT) rad_degrid(RadDev d, int mode, const float2* __restrict__ F,
                                                   float2* __restrict__ kout, float2* __restrict__ r,
                                                   const float2* __restrict__ f, float2* __restrict__ s,
@@ -125,23 +130,37 @@ __global__ void __launch_bounds__(kRT) rad_degrid(RadDev d, int mode, const floa
     gys[t] = wrapG(d.g0[2 * j + 1] + t, d.G);
   }
   const float wj = d.w[j];
-  for (int c = 0; c < d.C; ++c) {
-    float2 a = c2(0.f, 0.f);
-    const float2* Fc = F + (size_t)c * d.G * d.G;
+  const size_t plane = (size_t)d.G * d.G;
+  for (int cbase = 0; cbase < d.C; cbase += MAXC) {
+    const int nc = min(MAXC, d.C - cbase);
+    float2 a[MAXC];
+#pragma unroll
+    for (int c = 0; c < MAXC; ++c) a[c] = c2(0.f, 0.f);
     for (int tx = 0; tx < kw; ++tx) {
-      float2 col = c2(0.f, 0.f);
-      const float2* Fx = Fc + (size_t)gxs[tx] * d.G;
-      for (int ty = 0; ty < kw; ++ty) col += Fx[gys[ty]] * wy[ty];
-      a += col * wx[tx];
+      float2 col[MAXC];
+#pragma unroll
+      for (int c = 0; c < MAXC; ++c) col[c] = c2(0.f, 0.f);
+      for (int ty = 0; ty < kw; ++ty) {
+        const float2* Fp = F + (size_t)cbase * plane + (size_t)gxs[tx] * d.G + gys[ty];
+#pragma unroll
+        for (int c = 0; c < MAXC; ++c)
+          if (c < nc) col[c] += Fp[(size_t)c * plane] * wy[ty];
+      }
+#pragma unroll
+      for (int c = 0; c < MAXC; ++c) a[c] += col[c] * wx[tx];
     }
-    a = a * wj;
-    const size_t o = (size_t)c * d.Ns + j;
-    if (mode == 0) {
-      kout[o] = a;
-    } else {
-      const float2 rn = (r[o] + sigma * (a - f[o])) / (1.0f + sigma * lambda);
-      r[o] = rn;
-      s[(size_t)j * d.C + c] = rn * wj;  // sample-major for the gridding gather
+#pragma unroll
+    for (int c = 0; c < MAXC; ++c) {
+      if (c >= nc) break;
+      const float2 av = a[c] * wj;
+      const size_t o = (size_t)(cbase + c) * d.Ns + j;
+      if (mode == 0) {
+        kout[o] = av;
+      } else {
+        const float2 rn = (r[o] + sigma * (av - f[o])) / (1.0f + sigma * lambda);
+        r[o] = rn;
+        s[(size_t)j * d.C + cbase + c] = rn * wj;  // sample-major for the gridding gather
+      }
     }
   }
 }
@@ -165,6 +184,7 @@ __global__ void __launch_bounds__(kRT) rad_grid(RadDev d, const float2* __restri
   const size_t cell = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
   if (cell >= ncell) return;
   const int beg = d.cell_ptr[cell], end = d.cell_ptr[cell + 1];
+  if (end - beg > kHeavy) return;  // rad_grid_heavy
   for (int cbase = 0; cbase < d.C; cbase += MAXC) {
     const int nc = min(MAXC, d.C - cbase);
     float2 acc[MAXC];
@@ -197,6 +217,40 @@ __global__ void __launch_bounds__(kRT) rad_grid(RadDev d, const float2* __restri
 #pragma unroll
     for (int c = 0; c < MAXC; ++c)
       if (c < nc) H[(size_t)(cbase + c) * ncell + cell] = acc[c];
+  }
+}
+
+// The cells near k = 0 (more than kHeavy samples): one warp per cell, lane l taking entries l, l + 32, ...,
+// then an xor-butterfly sum (every lane ends with the same, run-to-run identical value).
+template <int MAXC>
+__global__ void __launch_bounds__(128) rad_grid_heavy(RadDev d, const float2* __restrict__ s, float2* __restrict__ H) {
+  const int wi = blockIdx.x * 4 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+  if (wi >= d.n_heavy) return;  // uniform per warp
+  const size_t ncell = (size_t)d.G * d.G;
+  const int cell = d.heavy[wi];
+  const int beg = d.cell_ptr[cell], end = d.cell_ptr[cell + 1];
+  for (int cbase = 0; cbase < d.C; cbase += MAXC) {
+    const int nc = min(MAXC, d.C - cbase);
+    float2 acc[MAXC];
+#pragma unroll
+    for (int c = 0; c < MAXC; ++c) acc[c] = c2(0.f, 0.f);
+    for (int e = beg + lane; e < end; e += 32) {
+      const float2* sj = s + (size_t)d.cell_idx[e] * d.C + cbase;
+      const float wgt = d.cell_w[e];
+#pragma unroll
+      for (int c = 0; c < MAXC; ++c)
+        if (c < nc) acc[c] += sj[c] * wgt;
+    }
+#pragma unroll
+    for (int c = 0; c < MAXC; ++c) {
+      if (c < nc) {
+        for (int o = 16; o > 0; o >>= 1) {
+          acc[c].x += __shfl_xor_sync(0xffffffffu, acc[c].x, o);
+          acc[c].y += __shfl_xor_sync(0xffffffffu, acc[c].y, o);
+        }
+        if (lane == 0) H[(size_t)(cbase + c) * ncell + cell] = acc[c];
+      }
+    }
   }
 }
 
@@ -332,10 +386,7 @@ class RadialOp : public OpImpl, public SolverHooks {
     prepare();
     if (tick) launch_tick(tick, st);
     forward_grid(ubar, st, mk);
-    rad_degrid<<<(dev_.Ns + kRT - 1) / kRT, kRT, 0, st>>>(dev_, 1, grid_.as<float2>(), nullptr, r, fc,
-                                                         svals_.as<float2>(), sigma, lambda);
-    PDT_LAUNCH_CHECK();
-    count_launch();
+    launch_degrid(1, nullptr, r, fc, sigma, lambda, st);
     if (mk) mk->mark("rad_degrid_prox", st);
     adjoint_from_weighted(svals_.as<float2>(), khr, G_, st, mk);
   }
@@ -358,10 +409,7 @@ class RadialOp : public OpImpl, public SolverHooks {
   void execute_forward(const float2* src, float2* dst, cudaStream_t st) override {
     prepare();
     forward_grid(src, st, nullptr);
-    rad_degrid<<<(dev_.Ns + kRT - 1) / kRT, kRT, 0, st>>>(dev_, 0, grid_.as<float2>(), dst, nullptr, nullptr,
-                                                         nullptr, 0.f, 0.f);
-    PDT_LAUNCH_CHECK();
-    count_launch();
+    launch_degrid(0, dst, nullptr, nullptr, 0.f, 0.f, st);
   }
   void execute_adjoint(const float2* src, float2* dst, cudaStream_t st) override {
     prepare();
@@ -389,6 +437,21 @@ class RadialOp : public OpImpl, public SolverHooks {
       throw Error(PDT_ERR_CONFIG, why + "\nOperator '" + name_ + "': could not parse configuration parameter '" +
                                       key + "'!\n");
     return v;
+  }
+
+  // mode 0: kout = A u; mode 1: k-space dual prox into r and the weighted samples svals_
+  void launch_degrid(int mode, float2* kout, float2* r, const float2* fc, float sigma, float lambda,
+                     cudaStream_t st) {
+    const int nb = (dev_.Ns + kRT - 1) / kRT;
+    float2* sv = svals_.as<float2>();
+    if (dev_.C <= 4)
+      rad_degrid<4><<<nb, kRT, 0, st>>>(dev_, mode, grid_.as<float2>(), kout, r, fc, sv, sigma, lambda);
+    else if (dev_.C <= 8)
+      rad_degrid<8><<<nb, kRT, 0, st>>>(dev_, mode, grid_.as<float2>(), kout, r, fc, sv, sigma, lambda);
+    else
+      rad_degrid<16><<<nb, kRT, 0, st>>>(dev_, mode, grid_.as<float2>(), kout, r, fc, sv, sigma, lambda);
+    PDT_LAUNCH_CHECK();
+    count_launch();
   }
 
   void launch_weight(const float2* k, cudaStream_t st) {
@@ -429,14 +492,19 @@ class RadialOp : public OpImpl, public SolverHooks {
   // out (G partial images) <- K^H applied to the already weighted samples s.
   void adjoint_from_weighted(const float2* s, float2* out, int G, cudaStream_t st, PhaseMarker* mk) {
     const int nblk = (int)(((size_t)dev_.G * dev_.G + kRT - 1) / kRT);
-    if (dev_.C <= 4)
+    const int hblk = (dev_.n_heavy + 3) / 4;
+    if (dev_.C <= 4) {
       rad_grid<4><<<nblk, kRT, 0, st>>>(dev_, s, grid_.as<float2>());
-    else if (dev_.C <= 8)
+      if (hblk) rad_grid_heavy<4><<<hblk, 128, 0, st>>>(dev_, s, grid_.as<float2>());
+    } else if (dev_.C <= 8) {
       rad_grid<8><<<nblk, kRT, 0, st>>>(dev_, s, grid_.as<float2>());
-    else
+      if (hblk) rad_grid_heavy<8><<<hblk, 128, 0, st>>>(dev_, s, grid_.as<float2>());
+    } else {
       rad_grid<16><<<nblk, kRT, 0, st>>>(dev_, s, grid_.as<float2>());
+      if (hblk) rad_grid_heavy<16><<<hblk, 128, 0, st>>>(dev_, s, grid_.as<float2>());
+    }
     PDT_LAUNCH_CHECK();
-    count_launch();
+    count_launch(hblk ? 2 : 1);
     if (mk) mk->mark("rad_grid", st);
     if (fast_.ok()) {
       const int R = fast_.per_block();
@@ -536,6 +604,9 @@ class RadialOp : public OpImpl, public SolverHooks {
     for (size_t c = 0; c < ncell; ++c) ptr[c + 1] += ptr[c];
     std::vector<int> idx((size_t)ptr[ncell]), fill(ptr.begin(), ptr.end() - 1);
     std::vector<float> cw(idx.size());
+    std::vector<int> heavy;
+    for (size_t c = 0; c < ncell; ++c)
+      if (ptr[c + 1] - ptr[c] > kHeavy) heavy.push_back((int)c);
     for (int j = 0; j < Ns; ++j)
       for (int txx = 0; txx < kw; ++txx)
         for (int ty = 0; ty < kw; ++ty) {
@@ -547,8 +618,8 @@ class RadialOp : public OpImpl, public SolverHooks {
     std::vector<float2> tw(G);
     fill_twiddles(G, tw.data());
     std::vector<float> w(dcf, dcf + Ns);
-    const size_t need = 64 * 9 + sizeof(float2) * G + sizeof(float) * (N + (size_t)Ns + wt.size() + cw.size()) +
-                        sizeof(int) * (g0.size() + ptr.size() + idx.size());
+    const size_t need = 64 * 10 + sizeof(float2) * G + sizeof(float) * (N + (size_t)Ns + wt.size() + cw.size()) +
+                        sizeof(int) * (g0.size() + ptr.size() + idx.size() + heavy.size());
     tables_.ensure(need);
     char* base = tables_.as<char>();
     size_t off = 0;
@@ -567,6 +638,8 @@ class RadialOp : public OpImpl, public SolverHooks {
     d.cell_ptr = reinterpret_cast<const int*>(put(ptr.data(), sizeof(int) * ptr.size()));
     d.cell_idx = reinterpret_cast<const int*>(put(idx.data(), sizeof(int) * idx.size()));
     d.cell_w = reinterpret_cast<const float*>(put(cw.data(), sizeof(float) * cw.size()));
+    d.heavy = reinterpret_cast<const int*>(put(heavy.data(), sizeof(int) * heavy.size()));
+    d.n_heavy = (int)heavy.size();
     tbuf_.ensure(sizeof(float2) * (size_t)C * G * N);
     grid_.ensure(sizeof(float2) * (size_t)C * G * G);
     svals_.ensure(sizeof(float2) * std::max<size_t>((size_t)C * Ns, 1));
