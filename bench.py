@@ -630,14 +630,33 @@ def run_radial(pdt, torch, slices, iters):
 def run_ncu_case(args):
     """The workload's kernels for an ncu capture: operator set-up, autotuning and graph capture run first,
     then one solve of --ncu-iters iterations runs between cudaProfilerStart and cudaProfilerStop, so
-    `ncu --profile-from-start off` sees exactly those launches (4 kernels per iteration)."""
+    `ncu --profile-from-start off` sees exactly those launches (5 kernels per Cartesian iteration, 9 per
+    radial iteration)."""
     import torch
 
     import primaldualtoolbox as pdt
 
+    stream = torch.cuda.current_stream()
+    if args.ncu_workload == "radial":
+        op, f, a1 = _radial_problem(pdt, seed=0)
+        opt = pdt.mri.TgvMriOptimizer_2c2c()
+        prm = opt.getParameters()
+        prm.max_iter, prm.reduction, prm.alpha1 = args.ncu_iters - 1, 2.0 ** -8, a1
+        prm.alpha0 = 2 * a1
+        opt.setOperator(op)
+        opt.setNoisyData(f)
+        for _ in range(3):
+            opt.solve(stream=stream)
+        torch.cuda.synchronize()
+        torch.cuda.profiler.start()
+        opt.solve(stream=stream)
+        torch.cuda.synchronize()
+        torch.cuda.profiler.stop()
+        print(json.dumps({"ncu_case": "radial_tgv2_12c_256x256_64spokes_x512", "iterations": args.ncu_iters}),
+              flush=True)
+        return
     case = _problem(seed=0)
     dev = {k: torch.from_numpy(np.ascontiguousarray(case[k])).cuda() for k in ("rawdata", "sens", "mask")}
-    stream = torch.cuda.current_stream()
     op = pdt.mri.MriCartesianRemoveROOSOperator()
     op.setCoilSens(dev["sens"])
     op.setMask(dev["mask"])
@@ -707,6 +726,8 @@ def main():
     ap.add_argument("--radial-iters", type=int, default=200, help="radial leg: iterations per slice")
     ap.add_argument("--batch-cases", type=int, default=64, help="batched leg: independent problems (0 skips)")
     ap.add_argument("--batch-iters", type=int, default=200, help="batched leg: iterations per problem and step")
+    ap.add_argument("--ncu-workload", default="cartesian", choices=["cartesian", "radial"],
+                    help="profiling mode: the config-2 Cartesian problem or the config-5 radial slice")
     ap.add_argument("--ncu-iters", type=int, default=0,
                     help="profiling mode: one solve of this many iterations between cudaProfilerStart/Stop")
     args = ap.parse_args()

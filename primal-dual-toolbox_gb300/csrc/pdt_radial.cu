@@ -111,8 +111,8 @@ __global__ void __launch_bounds__(kRT) rad_cols(RadDev d, const float2* __restri
 }
 
 // Degridding. mode 0: kout[c][j] = A u. mode 1 (solver): r <- (r + sigma (A u - f)) / (1 + sigma lambda),
-// s[j][c] = w_j r (the weighted values the adjoint grids, sample-major). Coils in chunks of MAXC, fully
-// unrolled, so that every tap load of a chunk is in flight at once.
+// s[j][c] = w_j r (the weighted values the adjoint grids, sample-major). blockIdx.y selects a chunk of MAXC
+// coils, fully unrolled, so that a sample's tap loads of the chunk are all in flight at once.
 template <int MAXC>
 __global__ void __launch_bounds__(kRT) rad_degrid(RadDev d, int mode, const float2* __restrict__ F,
                                                   float2* __restrict__ kout, float2* __restrict__ r,
@@ -131,7 +131,8 @@ __global__ void __launch_bounds__(kRT) rad_degrid(RadDev d, int mode, const floa
   }
   const float wj = d.w[j];
   const size_t plane = (size_t)d.G * d.G;
-  for (int cbase = 0; cbase < d.C; cbase += MAXC) {
+  {
+    const int cbase = blockIdx.y * MAXC;
     const int nc = min(MAXC, d.C - cbase);
     float2 a[MAXC];
 #pragma unroll
@@ -175,16 +176,49 @@ __global__ void rad_weight(RadDev d, const float2* __restrict__ k, float2* __res
 }
 
 // Gridding as a gather: H[c][gx][gy] = sum_j s[j][c] wx[gx - gx0_j] wy[gy - gy0_j] over the samples j whose
-// footprint covers the cell, in sample order (so the result does not depend on scheduling). A sample's
-// coil values are contiguous, and four entries are fetched at a time so that the cells near k = 0, whose
-// lists are longest, keep many loads in flight.
+// footprint covers the cell (lists built at set-up, entries in sample order). One launch, two kinds of
+// block: the first heavy_blocks blocks give each of the cells near k = 0 (more than kHeavy entries) a
+// warp, lane l taking entries l, l + 32, ... and an xor-butterfly sum (every lane ends with the same,
+// run-to-run identical value); the others give every remaining cell a thread that walks its list in
+// order, four entries at a time so that many loads are in flight. A sample's coil values are contiguous.
 template <int MAXC>
-__global__ void __launch_bounds__(kRT) rad_grid(RadDev d, const float2* __restrict__ s, float2* __restrict__ H) {
+__global__ void __launch_bounds__(kRT) rad_grid(RadDev d, const float2* __restrict__ s, float2* __restrict__ H,
+                                                int heavy_blocks) {
   const size_t ncell = (size_t)d.G * d.G;
-  const size_t cell = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if ((int)blockIdx.x < heavy_blocks) {
+    const int wi = blockIdx.x * (kRT / 32) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+    if (wi >= d.n_heavy) return;  // uniform per warp
+    const int cell = d.heavy[wi];
+    const int beg = d.cell_ptr[cell], end = d.cell_ptr[cell + 1];
+    for (int cbase = 0; cbase < d.C; cbase += MAXC) {
+      const int nc = min(MAXC, d.C - cbase);
+      float2 acc[MAXC];
+#pragma unroll
+      for (int c = 0; c < MAXC; ++c) acc[c] = c2(0.f, 0.f);
+      for (int e = beg + lane; e < end; e += 32) {
+        const float2* sj = s + (size_t)d.cell_idx[e] * d.C + cbase;
+        const float wgt = d.cell_w[e];
+#pragma unroll
+        for (int c = 0; c < MAXC; ++c)
+          if (c < nc) acc[c] += sj[c] * wgt;
+      }
+#pragma unroll
+      for (int c = 0; c < MAXC; ++c) {
+        if (c < nc) {
+          for (int o = 16; o > 0; o >>= 1) {
+            acc[c].x += __shfl_xor_sync(0xffffffffu, acc[c].x, o);
+            acc[c].y += __shfl_xor_sync(0xffffffffu, acc[c].y, o);
+          }
+          if (lane == 0) H[(size_t)(cbase + c) * ncell + cell] = acc[c];
+        }
+      }
+    }
+    return;
+  }
+  const size_t cell = (blockIdx.x - heavy_blocks) * (size_t)blockDim.x + threadIdx.x;
   if (cell >= ncell) return;
   const int beg = d.cell_ptr[cell], end = d.cell_ptr[cell + 1];
-  if (end - beg > kHeavy) return;  // rad_grid_heavy
+  if (end - beg > kHeavy) return;  // a heavy block's warp grids it
   for (int cbase = 0; cbase < d.C; cbase += MAXC) {
     const int nc = min(MAXC, d.C - cbase);
     float2 acc[MAXC];
@@ -217,40 +251,6 @@ __global__ void __launch_bounds__(kRT) rad_grid(RadDev d, const float2* __restri
 #pragma unroll
     for (int c = 0; c < MAXC; ++c)
       if (c < nc) H[(size_t)(cbase + c) * ncell + cell] = acc[c];
-  }
-}
-
-// The cells near k = 0 (more than kHeavy samples): one warp per cell, lane l taking entries l, l + 32, ...,
-// then an xor-butterfly sum (every lane ends with the same, run-to-run identical value).
-template <int MAXC>
-__global__ void __launch_bounds__(128) rad_grid_heavy(RadDev d, const float2* __restrict__ s, float2* __restrict__ H) {
-  const int wi = blockIdx.x * 4 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
-  if (wi >= d.n_heavy) return;  // uniform per warp
-  const size_t ncell = (size_t)d.G * d.G;
-  const int cell = d.heavy[wi];
-  const int beg = d.cell_ptr[cell], end = d.cell_ptr[cell + 1];
-  for (int cbase = 0; cbase < d.C; cbase += MAXC) {
-    const int nc = min(MAXC, d.C - cbase);
-    float2 acc[MAXC];
-#pragma unroll
-    for (int c = 0; c < MAXC; ++c) acc[c] = c2(0.f, 0.f);
-    for (int e = beg + lane; e < end; e += 32) {
-      const float2* sj = s + (size_t)d.cell_idx[e] * d.C + cbase;
-      const float wgt = d.cell_w[e];
-#pragma unroll
-      for (int c = 0; c < MAXC; ++c)
-        if (c < nc) acc[c] += sj[c] * wgt;
-    }
-#pragma unroll
-    for (int c = 0; c < MAXC; ++c) {
-      if (c < nc) {
-        for (int o = 16; o > 0; o >>= 1) {
-          acc[c].x += __shfl_xor_sync(0xffffffffu, acc[c].x, o);
-          acc[c].y += __shfl_xor_sync(0xffffffffu, acc[c].y, o);
-        }
-        if (lane == 0) H[(size_t)(cbase + c) * ncell + cell] = acc[c];
-      }
-    }
   }
 }
 
@@ -442,14 +442,10 @@ class RadialOp : public OpImpl, public SolverHooks {
   // mode 0: kout = A u; mode 1: k-space dual prox into r and the weighted samples svals_
   void launch_degrid(int mode, float2* kout, float2* r, const float2* fc, float sigma, float lambda,
                      cudaStream_t st) {
-    const int nb = (dev_.Ns + kRT - 1) / kRT;
-    float2* sv = svals_.as<float2>();
-    if (dev_.C <= 4)
-      rad_degrid<4><<<nb, kRT, 0, st>>>(dev_, mode, grid_.as<float2>(), kout, r, fc, sv, sigma, lambda);
-    else if (dev_.C <= 8)
-      rad_degrid<8><<<nb, kRT, 0, st>>>(dev_, mode, grid_.as<float2>(), kout, r, fc, sv, sigma, lambda);
-    else
-      rad_degrid<16><<<nb, kRT, 0, st>>>(dev_, mode, grid_.as<float2>(), kout, r, fc, sv, sigma, lambda);
+    constexpr int kDegridCoils = 4;  // coils per thread; the chunks are spread over grid.y
+    const dim3 nb((dev_.Ns + kRT - 1) / kRT, (dev_.C + kDegridCoils - 1) / kDegridCoils);
+    rad_degrid<kDegridCoils><<<nb, kRT, 0, st>>>(dev_, mode, grid_.as<float2>(), kout, r, fc, svals_.as<float2>(),
+                                                 sigma, lambda);
     PDT_LAUNCH_CHECK();
     count_launch();
   }
@@ -491,20 +487,16 @@ class RadialOp : public OpImpl, public SolverHooks {
 
   // out (G partial images) <- K^H applied to the already weighted samples s.
   void adjoint_from_weighted(const float2* s, float2* out, int G, cudaStream_t st, PhaseMarker* mk) {
-    const int nblk = (int)(((size_t)dev_.G * dev_.G + kRT - 1) / kRT);
-    const int hblk = (dev_.n_heavy + 3) / 4;
-    if (dev_.C <= 4) {
-      rad_grid<4><<<nblk, kRT, 0, st>>>(dev_, s, grid_.as<float2>());
-      if (hblk) rad_grid_heavy<4><<<hblk, 128, 0, st>>>(dev_, s, grid_.as<float2>());
-    } else if (dev_.C <= 8) {
-      rad_grid<8><<<nblk, kRT, 0, st>>>(dev_, s, grid_.as<float2>());
-      if (hblk) rad_grid_heavy<8><<<hblk, 128, 0, st>>>(dev_, s, grid_.as<float2>());
-    } else {
-      rad_grid<16><<<nblk, kRT, 0, st>>>(dev_, s, grid_.as<float2>());
-      if (hblk) rad_grid_heavy<16><<<hblk, 128, 0, st>>>(dev_, s, grid_.as<float2>());
-    }
+    const int hblk = (dev_.n_heavy + kRT / 32 - 1) / (kRT / 32);
+    const int nblk = hblk + (int)(((size_t)dev_.G * dev_.G + kRT - 1) / kRT);
+    if (dev_.C <= 4)
+      rad_grid<4><<<nblk, kRT, 0, st>>>(dev_, s, grid_.as<float2>(), hblk);
+    else if (dev_.C <= 8)
+      rad_grid<8><<<nblk, kRT, 0, st>>>(dev_, s, grid_.as<float2>(), hblk);
+    else
+      rad_grid<16><<<nblk, kRT, 0, st>>>(dev_, s, grid_.as<float2>(), hblk);
     PDT_LAUNCH_CHECK();
-    count_launch(hblk ? 2 : 1);
+    count_launch();
     if (mk) mk->mark("rad_grid", st);
     if (fast_.ok()) {
       const int R = fast_.per_block();
