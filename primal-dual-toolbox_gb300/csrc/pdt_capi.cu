@@ -423,11 +423,13 @@ class OptImpl {
   // A solve split in three: plan() enqueues the set-up on `st` and returns the per-iteration body,
   // the iterations run (graph replay or direct), finish() records the new state parity.
   struct Plan {
-    int n = 0;
+    int n = 0;     // calls of body
+    int tail = 0;  // then calls of tail_body (parity continues)
+    int iters = 0;  // primal-dual iterations in all (for the verbose report)
     int p0 = 0;
     uint64_t key = 0;
     bool verbose = false;
-    std::function<void(int, cudaStream_t)> body;
+    std::function<void(int, cudaStream_t)> body, tail_body;
   };
 
   Plan plan(bool verbose, cudaStream_t st) {
@@ -435,12 +437,13 @@ class OptImpl {
     return with_op() ? plan_with_op(verbose, st) : plan_denoise(verbose, st);
   }
   void finish(const Plan& p) {
-    parity_ = p.p0 ^ (p.n & 1);
-    if (p.verbose && !with_op()) print_iters(p.n);
+    parity_ = p.p0 ^ ((p.n + p.tail) & 1);
+    if (p.verbose && !with_op()) print_iters(p.iters ? p.iters : p.n);
   }
   void solve(bool verbose, cudaStream_t st) {
     Plan p = plan(verbose, st);
     run_iterations(graph_, p.key, p.n, profiling_ ? p.n + 2 : kGraphIters, p.body, st, capture_stream());
+    for (int i = 0; i < p.tail; ++i) p.tail_body((p.n + i) & 1, st);
     finish(p);
   }
   const OpImpl* op_ptr() const { return op_.get(); }
@@ -537,7 +540,8 @@ class OptImpl {
   // Fields that are read at neighbouring pixels ping-pong between two copies; in the primal-first TGV
   // denoising order u, v do too.
   bool pingpong(int f) const {
-    if (f == F_U || f == F_VX || f == F_VY) return kind_ == PDT_OPT_TGV;
+    // the denoising kernels read u (and v) at neighbouring pixels (the TV kernel through its halo)
+    if (f == F_U || f == F_VX || f == F_VY) return kind_ == PDT_OPT_TGV || kind_ == PDT_OPT_TV;
     return true;
   }
   void* field(int f, int set) const {
@@ -600,18 +604,32 @@ class OptImpl {
     const float a0 = (float)params_.alpha0, a1 = (float)params_.alpha1;
     if (verbose) print_params();
     Plan pl;
-    pl.n = (int)params_.max_iter + 1;
+    pl.iters = (int)params_.max_iter + 1;
+    pl.n = pl.iters;
     pl.p0 = parity_;
     pl.verbose = verbose;
     const int p0 = parity_;
-    pl.body = [=](int par, cudaStream_t s) {
-      const int in = p0 ^ par, out = in ^ 1;
-      if (is_tgv)
+    if (is_tgv) {
+      pl.body = [=](int par, cudaStream_t s) {
+        const int in = p0 ^ par, out = in ^ 1;
         launch_tgv_denoise_step(cplx_, W_, H_, ptrs(in), ptrs(out), f_.p, tau, sigma, lambda, a0, a1, s);
-      else
+        if (prof_) prof_->mark("tgv_denoise_step", s);
+      };
+    } else {
+      // kTvStepsPerLaunch iterations per launch, then the remainder one at a time
+      pl.n = pl.iters / kTvStepsPerLaunch;
+      pl.tail = pl.iters % kTvStepsPerLaunch;
+      pl.body = [=](int par, cudaStream_t s) {
+        const int in = p0 ^ par, out = in ^ 1;
+        launch_tv_multi_step(cplx_, W_, H_, ptrs(in), ptrs(out), f_.p, tau, sigma, lambda, s);
+        if (prof_) prof_->mark("tv_multi_step", s);
+      };
+      pl.tail_body = [=](int par, cudaStream_t s) {
+        const int in = p0 ^ par, out = in ^ 1;
         launch_tv_step(cplx_, W_, H_, ptrs(in), ptrs(out), f_.p, tau, sigma, lambda, s);
-      if (prof_) prof_->mark(is_tgv ? "tgv_denoise_step" : "tv_step", s);
-    };
+        if (prof_) prof_->mark("tv_step", s);
+      };
+    }
     pl.key = graph_key({(uintptr_t)img_.p, (uintptr_t)f_.p, (uintptr_t)W_, (uintptr_t)H_, (uintptr_t)p0,
                         (uintptr_t)cplx_, fbits(lambda), fbits(a0), fbits(a1)});
     return pl;
@@ -872,6 +890,7 @@ class BatchImpl {
     // remaining iterations of every problem (uneven max_iter), concurrently
     fork_join(st, [&](size_t i, cudaStream_t w) {
       for (int it = full * kBatchIters; it < plans[i].n; ++it) plans[i].body(it & 1, w);
+      for (int t = 0; t < plans[i].tail; ++t) plans[i].tail_body((plans[i].n + t) & 1, w);
     });
     for (size_t i = 0; i < opts_.size(); ++i) opts_[i]->finish(plans[i]);
   }

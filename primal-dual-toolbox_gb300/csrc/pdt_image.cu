@@ -87,13 +87,87 @@ __global__ void __launch_bounds__(NT) tv_step_kernel(int W, int H, ImgPtrs in, I
   const int gx = x0 + lx - 1, gy = y0 + ly - 1;
   if (gx < W && gy < H) {
     const size_t idx = (size_t)gy * W + gx;
-    P* u = static_cast<P*>(out.u);
-    const P uo = u[idx];
+    const P uo = static_cast<const P*>(in.u)[idx];
     const P d = div_minus<P, TX + 1>(s_px, s_py, lx, ly, gx, gy, W, H);
     P un = uo + tau * (d + lambda * f[idx]);
     un = un * (1.0f / (1.0f + tau * lambda));
-    u[idx] = un;
+    static_cast<P*>(out.u)[idx] = un;
     static_cast<P*>(out.ub)[idx] = 2.0f * un - uo;
+  }
+}
+
+// ------------------------------------------------------------------------------------------------
+// TvOptimizer, T iterations per launch (temporal blocking): a block loads its 32 x 16 output tile plus
+// a T-pixel halo of the state (u, u-bar, p, f) into shared memory and runs T dual + primal steps there
+// with the same per-pixel arithmetic as tv_step_kernel. A step reads u-bar one pixel to the right /
+// below and p one pixel to the left / above, so the halo loses at most one valid ring per step and the
+// output tile is exact after T steps; cells next to the region edge are simply not updated. Reads the
+// state from `in`, writes the tile's final state to `out` (every field ping-pongs).
+// ------------------------------------------------------------------------------------------------
+template <class P, int T>
+__global__ void __launch_bounds__(NT) tv_multi_kernel(int W, int H, ImgPtrs in, ImgPtrs out,
+                                                      const P* __restrict__ f, float tau, float sigma, float lambda) {
+  constexpr int OX = 32, OY = 16, RX = OX + 2 * T, RY = OY + 2 * T;
+  __shared__ P s_u[RY][RX], s_ub[RY][RX], s_px[RY][RX], s_py[RY][RX], s_f[RY][RX];
+  const int tid = threadIdx.x;
+  const int rx0 = blockIdx.x * OX - T, ry0 = blockIdx.y * OY - T;  // region origin in the image
+  for (int i = tid; i < RX * RY; i += NT) {
+    const int ly = i / RX, lx = i - ly * RX;
+    const int gx = rx0 + lx, gy = ry0 + ly;
+    if (gx >= 0 && gx < W && gy >= 0 && gy < H) {
+      const size_t idx = (size_t)gy * W + gx;
+      s_u[ly][lx] = static_cast<const P*>(in.u)[idx];
+      s_ub[ly][lx] = static_cast<const P*>(in.ub)[idx];
+      s_px[ly][lx] = static_cast<const P*>(in.px)[idx];
+      s_py[ly][lx] = static_cast<const P*>(in.py)[idx];
+      s_f[ly][lx] = f[idx];
+    }
+  }
+  __syncthreads();
+  const float inv = 1.0f / (1.0f + tau * lambda);
+#pragma unroll 1
+  for (int it = 0; it < T; ++it) {
+    // TV_dual_p_kernel (tgv_kernels.cuh:294-324); needs u-bar to the right and below
+    for (int i = tid; i < RX * RY; i += NT) {
+      const int ly = i / RX, lx = i - ly * RX;
+      const int gx = rx0 + lx, gy = ry0 + ly;
+      if (gx < 0 || gx >= W || gy < 0 || gy >= H) continue;
+      if ((lx == RX - 1 && gx < W - 1) || (ly == RY - 1 && gy < H - 1)) continue;
+      const int xp = lx + (gx < W - 1), yp = ly + (gy < H - 1);
+      const P c = s_ub[ly][lx];
+      const P gux = s_ub[ly][xp] - c, guy = s_ub[yp][lx] - c;
+      const P a = s_px[ly][lx] + sigma * gux;
+      const P b = s_py[ly][lx] + sigma * guy;
+      const float sc = proj_scale(sqrtf(abs2(a) + abs2(b)), 1.0f);
+      s_px[ly][lx] = a * sc;
+      s_py[ly][lx] = b * sc;
+    }
+    __syncthreads();
+    // TV_primal_u_kernel (tgv_kernels.cuh:568-605); needs p to the left and above
+    for (int i = tid; i < RX * RY; i += NT) {
+      const int ly = i / RX, lx = i - ly * RX;
+      const int gx = rx0 + lx, gy = ry0 + ly;
+      if (gx < 0 || gx >= W || gy < 0 || gy >= H) continue;
+      if ((lx == 0 && gx > 0) || (ly == 0 && gy > 0)) continue;
+      const P uo = s_u[ly][lx];
+      const P d = div_minus<P, RX>(s_px, s_py, lx, ly, gx, gy, W, H);
+      P un = uo + tau * (d + lambda * s_f[ly][lx]);
+      un = un * inv;
+      s_u[ly][lx] = un;
+      s_ub[ly][lx] = 2.0f * un - uo;
+    }
+    __syncthreads();
+  }
+  for (int i = tid; i < OX * OY; i += NT) {
+    const int ly = T + i / OX, lx = T + i % OX;
+    const int gx = rx0 + lx, gy = ry0 + ly;
+    if (gx < W && gy < H) {
+      const size_t idx = (size_t)gy * W + gx;
+      static_cast<P*>(out.u)[idx] = s_u[ly][lx];
+      static_cast<P*>(out.ub)[idx] = s_ub[ly][lx];
+      static_cast<P*>(out.px)[idx] = s_px[ly][lx];
+      static_cast<P*>(out.py)[idx] = s_py[ly][lx];
+    }
   }
 }
 
@@ -309,6 +383,19 @@ void launch_tv_step(bool complex_, int W, int H, const ImgPtrs& in, const ImgPtr
   else
     tv_step_kernel<float><<<tile_grid(W, H), NT, 0, st>>>(W, H, in, out, static_cast<const float*>(f), tau, sigma,
                                                            lambda);
+  PDT_LAUNCH_CHECK();
+  count_launch();
+}
+
+void launch_tv_multi_step(bool complex_, int W, int H, const ImgPtrs& in, const ImgPtrs& out, const void* f,
+                          float tau, float sigma, float lambda, cudaStream_t st) {
+  const dim3 grid((W + 31) / 32, (H + 15) / 16);
+  if (complex_)
+    tv_multi_kernel<float2, kTvStepsPerLaunch><<<grid, NT, 0, st>>>(W, H, in, out, static_cast<const float2*>(f),
+                                                                    tau, sigma, lambda);
+  else
+    tv_multi_kernel<float, kTvStepsPerLaunch><<<grid, NT, 0, st>>>(W, H, in, out, static_cast<const float*>(f), tau,
+                                                                   sigma, lambda);
   PDT_LAUNCH_CHECK();
   count_launch();
 }

@@ -73,10 +73,15 @@ struct ImgPtrs {
   void *u, *ub, *vx, *vy, *vbx, *vby, *px, *py, *qxx, *qyy, *qxy;
 };
 
-// Fused TvOptimizer iteration (tgv_kernels.cuh:294-324 then 568-605): reads u-bar and p from `in`,
-// writes p and u-bar to `out`, updates u in place (in.u == out.u).
+// Fused TvOptimizer iteration (tgv_kernels.cuh:294-324 then 568-605): reads u, u-bar and p from `in`,
+// writes them to `out`.
 void launch_tv_step(bool complex_, int W, int H, const ImgPtrs& in, const ImgPtrs& out, const void* f, float tau,
                     float sigma, float lambda, cudaStream_t st);
+// kTvStepsPerLaunch TvOptimizer iterations in one launch (temporal blocking in shared memory); same
+// arithmetic per pixel as launch_tv_step, state read from `in` and written to `out`.
+constexpr int kTvStepsPerLaunch = 4;
+void launch_tv_multi_step(bool complex_, int W, int H, const ImgPtrs& in, const ImgPtrs& out, const void* f,
+                          float tau, float sigma, float lambda, cudaStream_t st);
 
 // Fused TgvOptimizer iteration, primal first (tgvoptimizer.cu:117-137): every field ping-pongs.
 void launch_tgv_denoise_step(bool complex_, int W, int H, const ImgPtrs& in, const ImgPtrs& out, const void* f,
