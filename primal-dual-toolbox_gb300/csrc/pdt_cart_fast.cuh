@@ -174,6 +174,101 @@ __global__ void __launch_bounds__(32 * WPB) fl_cols(CartDev d, int mode, const f
   }
 }
 
+// Phase 2 over two warps per column (n = M * 64): the same steps as fl_cols with LaneFft64, for column
+// lengths whose 32-lane split would hold many values per lane; WPB / 2 columns per block. The compact
+// order is position k1 * 64 + t for spectrum index k1 + M brev_64(t).
+template <int M, int WPB>
+__global__ void __launch_bounds__(32 * WPB) fl_cols64(CartDev d, int mode, const float2* t_in, float2* t_out,
+                                                      float2* __restrict__ r, const float2* __restrict__ fc,
+                                                      const float2* __restrict__ kin, float2* __restrict__ kout,
+                                                      float sigma, float lambda) {
+  static_assert(WPB % 2 == 0, "two warps per column");
+  using F = LaneFft64<M>;
+  constexpr int Hf = F::n, L = 64;
+  extern __shared__ float2 sm[];
+  float2* tw = sm;
+  const int pair = threadIdx.x >> 6;
+  float2* xbuf = tw + Hf + (size_t)pair * M * 64;
+  const int bar = 1 + pair;  // named barrier of this column's two warps (0 is __syncthreads)
+  for (int i = threadIdx.x; i < Hf; i += blockDim.x) tw[i] = d.twH[i];
+  pdl_wait();  // t_in, r and fc come from earlier kernels
+  __syncthreads();
+  const int t = threadIdx.x & 63;
+  const int s0 = blockIdx.x * (WPB / 2) + pair;
+  const int c = blockIdx.y;
+  const bool ok = s0 < d.ns;
+  const int s = ok ? s0 : d.ns - 1;  // a pair past the last column reads column ns-1 and discards it
+  const size_t colc = (size_t)c * d.ns + s;
+  const int kb = M * (int)(__brev((unsigned)t) >> 26);
+  const float* mrow = d.maskc + (size_t)s * Hf;
+  float2 v[M];
+  if (mode == COL_SOLVE || mode == COL_FWD_DENSE) {
+#pragma unroll
+    for (int j = 0; j < M; ++j) {
+      int yf = t + L * j - d.mxH;
+      if (yf < 0) yf += Hf;
+      const int yi = yf - d.y0;
+      v[j] = (yi >= 0 && yi < d.Hi) ? t_in[colc * d.Hi + yi] : c2(0.f, 0.f);
+    }
+    F::fwd(v, t, tw, xbuf, bar);
+    if (mode == COL_FWD_DENSE) {
+      if (ok) {
+#pragma unroll
+        for (int k1 = 0; k1 < M; ++k1) {
+          int ypos = k1 + kb + d.oyH;
+          if (ypos >= Hf) ypos -= Hf;
+          kout[((size_t)c * Hf + ypos) * d.W + d.col_x[s]] = v[k1] * (d.scale * mrow[k1 * L + t]);
+        }
+      }
+      return;
+    }
+    const float2* fcol = fc + colc * Hf;
+    float2* rcol = r + colc * Hf;
+    float m[M];
+    float2 fv[M], rv[M];
+#pragma unroll
+    for (int k1 = 0; k1 < M; ++k1) {
+      const int P = k1 * L + t;
+      m[k1] = mrow[P];
+      fv[k1] = fcol[P];
+      rv[k1] = rcol[P];
+    }
+#pragma unroll
+    for (int k1 = 0; k1 < M; ++k1) {
+      const float2 kv = v[k1] * (d.scale * m[k1]);
+      rv[k1] = (rv[k1] + sigma * (kv - fv[k1])) / (1.0f + sigma * lambda);
+      v[k1] = rv[k1] * m[k1];
+    }
+    if (ok) {
+#pragma unroll
+      for (int k1 = 0; k1 < M; ++k1) rcol[k1 * L + t] = rv[k1];
+    }
+  } else {
+#pragma unroll
+    for (int k1 = 0; k1 < M; ++k1) {
+      float2 val;
+      if (mode == COL_ADJ_DENSE) {
+        int ypos = k1 + kb + d.oyH;
+        if (ypos >= Hf) ypos -= Hf;
+        val = kin[((size_t)c * Hf + ypos) * d.W + d.col_x[s]];
+      } else {
+        val = fc[colc * Hf + k1 * L + t];
+      }
+      v[k1] = val * mrow[k1 * L + t];
+    }
+  }
+  F::inv(v, t, tw, xbuf, bar);
+  if (ok) {
+#pragma unroll
+    for (int j = 0; j < M; ++j) {
+      int yf = t + L * j + d.oyH;
+      if (yf >= Hf) yf -= Hf;
+      const int yi = yf - d.y0;
+      if (yi >= 0 && yi < d.Hi) t_out[colc * d.Hi + yi] = v[j] * d.scale;
+    }
+  }
+}
+
 // Phase 3: per block of R image rows and coil group g, IFFT along W of the sampled columns, conj(sens_c)
 // multiply and the coil sum, accumulated in shared memory (each lane always owns the same pixels).
 // With use_cluster the G coil groups of a row block form a cluster (grid.y = G) and reduce their rows
@@ -295,7 +390,7 @@ struct FastColKernels {
   FrColsFn cols[3] = {nullptr, nullptr, nullptr};
   int M = 0, L = 0;
   bool ok() const { return cols[0] != nullptr; }
-  int cols_per_block(int wpb) const { return wpb * (32 / L); }
+  int cols_per_block(int wpb) const { return L == 64 ? wpb / 2 : wpb * (32 / L); }
 };
 
 template <int M, int L>
@@ -333,7 +428,25 @@ FastRowKernels find_row_kernels(int n) {
 #undef PDT_ROWCASE
   return FastRowKernels();
 }
+template <int M>
+FastColKernels col_kernels64() {
+  FastColKernels k;
+  k.cols[0] = fl_cols64<M, 2>;
+  k.cols[1] = fl_cols64<M, 4>;
+  k.cols[2] = fl_cols64<M, 8>;
+  k.M = M;
+  k.L = 64;
+  return k;
+}
+
+// Column lengths from 320 up run over two warps per column (M = n / 64 values per lane).
+#define PDT_COL64_SIZES(X) X(320, 5) X(384, 6) X(512, 8) X(640, 10) X(768, 12)
+
 FastColKernels find_col_kernels(int n) {
+#define PDT_COL64CASE(N, M) \
+  if (n == N) return col_kernels64<M>();
+  PDT_COL64_SIZES(PDT_COL64CASE)
+#undef PDT_COL64CASE
 #define PDT_COLCASE(N, M, L) \
   if (n == N) return col_kernels<M, L>();
   PDT_FAST_SIZES(PDT_COLCASE)
@@ -349,7 +462,10 @@ size_t fast_rows_adj_smem(const CartDev& d, const FastRowKernels& k, int wpb) {
   const size_t n = (size_t)k.M * k.L, R = (size_t)k.rows_per_block(wpb);
   return fast_rows_smem(d, k, wpb) + sizeof(float2) * R * n;
 }
-size_t fast_cols_smem(const FastColKernels& k) { return sizeof(float2) * (size_t)k.M * k.L; }
+size_t fast_cols_smem(const FastColKernels& k, int wpb) {
+  const size_t n = (size_t)k.M * k.L;
+  return sizeof(float2) * (n + (k.L == 64 ? (size_t)(wpb / 2) * n : 0));  // twiddles (+ exchange buffers)
+}
 
 // Host bit reversal over log2(L) bits (the order LaneFft leaves a spectrum in).
 inline int host_lane_brev(int t, int L) {

@@ -402,7 +402,7 @@ class CartesianOp : public OpImpl, public SolverHooks {
     if (fcol_.ok()) {
       const int wpb = kWpbChoices[tune_.wc];
       const int S = fcol_.cols_per_block(wpb);
-      LaunchEx lx(dim3((dev_.ns + S - 1) / S, dev_.C), dim3(32 * wpb), fast_cols_smem(fcol_), st);
+      LaunchEx lx(dim3((dev_.ns + S - 1) / S, dev_.C), dim3(32 * wpb), fast_cols_smem(fcol_, wpb), st);
       PDT_CUDA_CHECK(cudaLaunchKernelEx(&lx.cfg, fcol_.cols[tune_.wc], dev_, mode, tin, tout, r, fc, kin, kout, sigma,
                                         lambda));
       count_launch();
@@ -485,7 +485,7 @@ class CartesianOp : public OpImpl, public SolverHooks {
     frow_ = find_row_kernels(W);
     fcol_ = find_col_kernels(Hf);
     if (frow_.ok() && fast_rows_adj_smem(d, frow_, 8) > (size_t)g_max_smem) frow_ = FastRowKernels();
-    if (fcol_.ok() && fast_cols_smem(fcol_) > (size_t)g_max_smem) fcol_ = FastColKernels();
+    if (fcol_.ok() && fast_cols_smem(fcol_, 8) > (size_t)g_max_smem) fcol_ = FastColKernels();
     // compact position P -> output row: P = k1 L + t holds spectrum index k1 + M brev_L(t), which the
     // fftshift puts on row (k + Hf/2) mod Hf
     std::vector<int> kperm(Hf);

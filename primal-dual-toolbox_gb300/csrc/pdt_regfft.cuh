@@ -228,6 +228,91 @@ struct LaneFft {
   }
 };
 
+// The same transform over two warps (n = M * 64): lanes 0-31 of the first warp and 32-63 of the second
+// hold the sequence. The stage that pairs lane t with t ^ 32 goes through the shared-memory buffer xbuf
+// (M x 64 values) between two syncs of the named barrier bar_id (64 threads); the others are shuffles.
+// Both warps must call it.
+template <int M>
+struct LaneFft64 {
+  static constexpr int L = 64;
+  static constexpr int n = M * L;
+
+  static __device__ __forceinline__ void sync64(int bar_id) {
+    asm volatile("bar.sync %0, 64;" ::"r"(bar_id) : "memory");
+  }
+
+  static __device__ __forceinline__ void fwd(float2 (&v)[M], int t, const float2* __restrict__ tw, float2* xbuf,
+                                             int bar_id) {
+    reg_fft<M, L>(v, tw, -1.f);
+#pragma unroll
+    for (int k1 = 1; k1 < M; ++k1) v[k1] = cmul(v[k1], tw[t * k1]);
+    {  // h = 32: across the two warps
+      const bool up = (t & 32) != 0;
+      const float sg = up ? -1.f : 1.f;
+      const float2 w = up ? tw[(t & 31) * (n / 64)] : c2(1.f, 0.f);
+#pragma unroll
+      for (int k1 = 0; k1 < M; ++k1) xbuf[k1 * 64 + t] = v[k1];
+      sync64(bar_id);
+#pragma unroll
+      for (int k1 = 0; k1 < M; ++k1) {
+        const float2 p = xbuf[k1 * 64 + (t ^ 32)];
+        v[k1] = cmul(c2(fmaf(sg, v[k1].x, p.x), fmaf(sg, v[k1].y, p.y)), w);
+      }
+      sync64(bar_id);  // xbuf free again
+    }
+#pragma unroll
+    for (int h = 16; h >= 1; h >>= 1) {
+      const bool up = (t & h) != 0;
+      const float sg = up ? -1.f : 1.f;
+      float2 w = c2(1.f, 0.f);
+      if (h > 1 && up) w = tw[(t & (h - 1)) * (n / (2 * h))];
+#pragma unroll
+      for (int k1 = 0; k1 < M; ++k1) {
+        const float2 p = shfl_xor2(v[k1], h);
+        const float2 y = c2(fmaf(sg, v[k1].x, p.x), fmaf(sg, v[k1].y, p.y));
+        v[k1] = (h > 1) ? cmul(y, w) : y;
+      }
+    }
+  }
+
+  static __device__ __forceinline__ void inv(float2 (&v)[M], int t, const float2* __restrict__ tw, float2* xbuf,
+                                             int bar_id) {
+#pragma unroll
+    for (int h = 1; h < 32; h <<= 1) {
+      const bool up = (t & h) != 0;
+      const float sg = up ? -1.f : 1.f;
+      float2 w = c2(1.f, 0.f);
+      if (h > 1 && up) w = conjf2(tw[(t & (h - 1)) * (n / (2 * h))]);
+#pragma unroll
+      for (int k1 = 0; k1 < M; ++k1) {
+        const float2 m = (h > 1) ? cmul(v[k1], w) : v[k1];
+        const float2 p = shfl_xor2(m, h);
+        v[k1] = c2(fmaf(sg, m.x, p.x), fmaf(sg, m.y, p.y));
+      }
+    }
+    {  // h = 32: across the two warps
+      const bool up = (t & 32) != 0;
+      const float sg = up ? -1.f : 1.f;
+      const float2 w = up ? conjf2(tw[(t & 31) * (n / 64)]) : c2(1.f, 0.f);
+#pragma unroll
+      for (int k1 = 0; k1 < M; ++k1) {
+        v[k1] = cmul(v[k1], w);
+        xbuf[k1 * 64 + t] = v[k1];
+      }
+      sync64(bar_id);
+#pragma unroll
+      for (int k1 = 0; k1 < M; ++k1) {
+        const float2 p = xbuf[k1 * 64 + (t ^ 32)];
+        v[k1] = c2(fmaf(sg, v[k1].x, p.x), fmaf(sg, v[k1].y, p.y));
+      }
+      sync64(bar_id);
+    }
+#pragma unroll
+    for (int k1 = 1; k1 < M; ++k1) v[k1] = cmul(v[k1], conjf2(tw[t * k1]));
+    reg_fft<M, L>(v, tw, 1.f);
+  }
+};
+
 #endif  // PDT_HOST_EMULATION
 
 }  // namespace pdt
