@@ -56,6 +56,10 @@ struct CartDev {
   const float2* twW;
   const float2* twH;
   FftPlan planW, planH;
+  // Solver rounds with tensor-core adjoint rows: the column kernels write their image-row output as
+  // TF32 hi/lo operand tiles (tca, tc_nch K chunks per 128-row tile) instead of t[c][s][yi].
+  float* tca;
+  int tc_nch;
 };
 
 enum ColMode { COL_SOLVE = 0, COL_FWD_DENSE = 1, COL_ADJ_DENSE = 2, COL_ADJ_COMPACT = 3 };
@@ -240,6 +244,7 @@ void query_device() {
 }  // namespace pdt
 
 #include "pdt_cart_fast.cuh"
+#include "pdt_cart_tc.cuh"
 
 namespace pdt {
 
@@ -270,14 +275,28 @@ class CartesianOp : public OpImpl, public SolverHooks {
   SolverHooks* hooks() override { return this; }
   std::string tuning() override {
     prepare();
+    if (const int e = take_tc_error()) {
+      char code[16];
+      std::snprintf(code, sizeof code, "0x%x", e);
+      throw Error(PDT_ERR_TIMEOUT, name_ + ": a tensor-core row kernel gave up a bounded wait (code " + code +
+                                       "); results since the last check are not valid");
+    }
     std::ostringstream os;
     os << "W=" << dev_.W << " H=" << dev_.Hf << " C=" << dev_.C << " sampled_columns=" << dev_.ns;
-    if (frow_.ok())
-      os << " rows_fwd=lane_fft(" << frow_.M << "x" << frow_.L << ",warps=" << kWpbChoices[tune_.wf] << ")"
-         << " rows_adj=lane_fft(warps=" << kWpbChoices[tune_.wa] << ",coil_groups=" << G_
+    if (tune_.tcf)
+      os << " rows_fwd=tensor_dft(tf32x3,k_split=" << tune_.ks << ")";
+    else if (frow_.ok())
+      os << " rows_fwd=lane_fft(" << frow_.M << "x" << frow_.L << ",warps=" << kWpbChoices[tune_.wf] << ")";
+    else
+      os << " rows_fwd=stockham";
+    if (tune_.tca)
+      os << " rows_adj=tensor_dft(tf32x3,n_ranges=" << (2 * dev_.W + tc_adj_nb(tune_.nr) - 1) / tc_adj_nb(tune_.nr)
+         << ",stages=" << tc_adj_stages(tc_adj_nb(tune_.nr)) << ",coil_planes=" << dev_.C << ")";
+    else if (frow_.ok())
+      os << " rows_adj=lane_fft(warps=" << kWpbChoices[tune_.wa] << ",coil_groups=" << G_
          << (tune_.cluster ? ",cluster" : ",partials") << ")";
     else
-      os << " rows=stockham(coil_groups=" << G_ << ")";
+      os << " rows_adj=stockham(coil_groups=" << G_ << ")";
     if (fcol_.ok())
       os << " cols=lane_fft(" << fcol_.M << "x" << fcol_.L << ",warps=" << kWpbChoices[tune_.wc] << ")";
     else
@@ -306,6 +325,7 @@ class CartesianOp : public OpImpl, public SolverHooks {
   }
   int groups() override {
     prepare();
+    if (tune_.tca) return dev_.C;                    // one plane per coil (tensor-core adjoint rows)
     return (frow_.ok() && tune_.cluster) ? 1 : G_;  // a cluster reduces its coil groups on chip
   }
   long long group_stride() override { return (long long)dev_.Hi * dev_.W; }
@@ -320,9 +340,15 @@ class CartesianOp : public OpImpl, public SolverHooks {
     float2* t = scratch_.as<float2>();
     launch_rows_fwd(ubar, t, tick, st);
     if (mk) mk->mark("cart_rows_fwd", st);
-    launch_cols(COL_SOLVE, t, t, r, fc, nullptr, nullptr, sigma, lambda, st);
-    if (mk) mk->mark("cart_cols_prox", st);
-    launch_rows_adj(t, khr, G_, st);
+    if (tune_.tca) {  // column output as tensor-core operand tiles, one K^H r plane per coil
+      launch_cols(COL_SOLVE, t, t, r, fc, nullptr, nullptr, sigma, lambda, st, tca_.as<float>());
+      if (mk) mk->mark("cart_cols_prox", st);
+      launch_tc_rows_adj(khr, st);
+    } else {
+      launch_cols(COL_SOLVE, t, t, r, fc, nullptr, nullptr, sigma, lambda, st);
+      if (mk) mk->mark("cart_cols_prox", st);
+      launch_rows_adj(t, khr, G_, st);
+    }
     if (mk) mk->mark("cart_rows_adj", st);
   }
   void adjoint_compact(const float2* fc, float2* img, cudaStream_t st) override {
@@ -381,9 +407,93 @@ class CartesianOp : public OpImpl, public SolverHooks {
   struct Tune {
     int wf = 2, wc = 2, wa = 2;  // warps-per-block index (kWpbChoices) of rows_fwd, cols, rows_adj
     bool cluster = false;        // coil groups of a row block reduced in a cluster (else partial images)
+    int tcf = 0, tca = 0;        // 1: tensor-core DFT rows (forward / adjoint) instead of the FFT kernels
+    int ks = 4, nr = 4;          // tensor-core forward K split (cluster size), adjoint N ranges
   };
 
+  int tc_row_tiles() const { return (dev_.C * dev_.Hi + kTcRows - 1) / kTcRows; }
+  int tc_adj_nb(int nr) const { return std::min(kTcAdjMaxNB, ((2 * dev_.W + nr - 1) / nr + 15) & ~15); }
+
+  void launch_tc_rows_fwd(const float2* ubar, float2* t1, int* tick, cudaStream_t st) {
+    const int ks = tune_.ks, stiles = (dev_.ns + 127) / 128;
+    const int nb0 = (2 * std::min(128, dev_.ns) + 15) & ~15;
+    LaunchEx lx(dim3(tc_row_tiles(), ks, stiles), dim3(kTcThreads), tc_fwd_smem(dev_.W, nb0), st, ks > 1 ? ks : 0);
+    auto fn = dev_.sens ? tc_rows_fwd<true> : tc_rows_fwd<false>;
+    PDT_CUDA_CHECK(cudaLaunchKernelEx(&lx.cfg, fn, dev_, ubar, t1, tick, tc_err()));
+    count_launch();
+  }
+  int tc_adj_chunks() const { return (2 * dev_.ns + 31) / 32; }
+  int tc_adj_stages(int NB) const {
+    return std::min(kTcMaxStages, (int)(((size_t)g_max_smem - tc_adj_smem(NB, 0)) / tc_stage_bytes(NB)));
+  }
+  // The adjoint rows' DFT factor for output-column ranges of NB, as TF32 hi/lo operand tiles in the layout
+  // tc_rows_adj copies: [range][K chunk][hi rows | lo rows], row n = 2 x + o of the range (o = re/im
+  // output), K element k = 2 s + (re/im input), 128-byte swizzle. Values in double precision, then split.
+  void build_tc_adj_tiles(int NB) {
+    if (tcb_nb_ == NB) return;
+    const int W = dev_.W, ns = dev_.ns, nch = tc_adj_chunks(), nranges = (2 * W + NB - 1) / NB;
+    std::vector<float> h((size_t)nranges * nch * 2 * NB * 32, 0.f);
+    auto rna = [](float v) {  // round to TF32 (10 mantissa bits), ties away from zero
+      uint32_t u;
+      std::memcpy(&u, &v, 4);
+      u = (u + 0x1000u) & 0xFFFFE000u;
+      std::memcpy(&v, &u, 4);
+      return v;
+    };
+    const double two_pi = 6.283185307179586476925286766559;
+    for (int i = 0; i < nranges; ++i) {
+      const int n0 = i * NB, nb = std::min(NB, (2 * W - n0 + 15) & ~15);
+      for (int j = 0; j < nch; ++j) {
+        float* hi = &h[((size_t)i * nch + j) * 2 * NB * 32];
+        float* lo = hi + (size_t)nb * 32;
+        for (int n = 0; n < nb; ++n) {
+          const int x = (n0 + n) >> 1, o = (n0 + n) & 1;
+          if (x >= W) continue;
+          const int q = ((x - dev_.oxW) % W + W) % W;
+          for (int k = 0; k < 32; ++k) {
+            const int s = 16 * j + (k >> 1), ri = k & 1;
+            if (s >= ns) continue;
+            const int p = (col_x_h_[s] + dev_.mxW) % W;
+            const double a = two_pi * (double)(((long long)p * q) % W) / (double)W;
+            const float er = (float)std::cos(a), ei = (float)std::sin(a);  // exp(+i a) = conj(w^(p q))
+            const float v = o == 0 ? (ri == 0 ? er : -ei) : (ri == 0 ? ei : er);
+            const int pos = n * 32 + (((k >> 2) ^ (n & 7)) << 2) + (k & 3);
+            hi[pos] = rna(v);
+            lo[pos] = rna(v - hi[pos]);
+          }
+        }
+      }
+    }
+    tcb_.ensure(h.size() * sizeof(float));
+    PDT_CUDA_CHECK(cudaMemcpy(tcb_.p, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice));
+    tcb_nb_ = NB;
+  }
+  void launch_tc_rows_adj(float2* planes, cudaStream_t st) {
+    const int NB = tc_adj_nb(tune_.nr);
+    if (tcb_nb_ != NB) throw Error(PDT_ERR_STATE, name_ + ": tensor-core adjoint tiles not built for this range size");
+    const int nst = tc_adj_stages(NB);
+    LaunchEx lx(dim3((2 * dev_.W + NB - 1) / NB, tc_row_tiles()), dim3(kTcAdjThreads), tc_adj_smem(NB, nst), st);
+    auto fn = dev_.sens ? tc_rows_adj<true> : tc_rows_adj<false>;
+    PDT_CUDA_CHECK(cudaLaunchKernelEx(&lx.cfg, fn, dev_, (const float*)tca_.as<float>(),
+                                      (const unsigned char*)tcb_.p, planes, NB, nst, tc_err()));
+    count_launch();
+  }
+  int* tc_err() { return reinterpret_cast<int*>(tc_err_.p); }
+  // Reads (and clears) the tensor-core kernels' error word: non-zero when an MMA completion wait ran
+  // out of time, in which case that launch's output is not valid.
+  int take_tc_error() {
+    if (!tc_err_.p) return 0;
+    int e = 0;
+    PDT_CUDA_CHECK(cudaMemcpy(&e, tc_err_.p, sizeof(int), cudaMemcpyDeviceToHost));
+    if (e) PDT_CUDA_CHECK(cudaMemset(tc_err_.p, 0, sizeof(int)));
+    return e;
+  }
+
   void launch_rows_fwd(const float2* ubar, float2* t1, int* tick, cudaStream_t st) {
+    if (tune_.tcf) {
+      launch_tc_rows_fwd(ubar, t1, tick, st);
+      return;
+    }
     if (frow_.ok()) {
       const int wpb = kWpbChoices[tune_.wf];
       const int R = frow_.rows_per_block(wpb);
@@ -397,13 +507,19 @@ class CartesianOp : public OpImpl, public SolverHooks {
     PDT_LAUNCH_CHECK();
     count_launch();
   }
+  // `tiles`: COL_SOLVE writes its image-row output as the tensor-core adjoint's operand tiles
   void launch_cols(int mode, const float2* tin, float2* tout, float2* r, const float2* fc, const float2* kin,
-                   float2* kout, float sigma, float lambda, cudaStream_t st) {
+                   float2* kout, float sigma, float lambda, cudaStream_t st, float* tiles = nullptr) {
     if (fcol_.ok()) {
       const int wpb = kWpbChoices[tune_.wc];
       const int S = fcol_.cols_per_block(wpb);
+      CartDev dd = dev_;
+      if (tiles) {
+        dd.tca = tiles;
+        dd.tc_nch = tc_adj_chunks();
+      }
       LaunchEx lx(dim3((dev_.ns + S - 1) / S, dev_.C), dim3(32 * wpb), fast_cols_smem(fcol_, wpb), st);
-      PDT_CUDA_CHECK(cudaLaunchKernelEx(&lx.cfg, fcol_.cols[tune_.wc], dev_, mode, tin, tout, r, fc, kin, kout, sigma,
+      PDT_CUDA_CHECK(cudaLaunchKernelEx(&lx.cfg, fcol_.cols[tune_.wc], dd, mode, tin, tout, r, fc, kin, kout, sigma,
                                         lambda));
       count_launch();
       return;
@@ -485,6 +601,11 @@ class CartesianOp : public OpImpl, public SolverHooks {
     frow_ = find_row_kernels(W);
     fcol_ = find_col_kernels(Hf);
     if (frow_.ok() && fast_rows_adj_smem(d, frow_, 8) > (size_t)g_max_smem) frow_ = FastRowKernels();
+    // tensor-core DFT rows: even W (16-byte row vectors); the forward's twiddle table and index products
+    // are sized for W <= kTcMaxW; the adjoint's operand tiles come from the lane-FFT column kernels
+    const bool tc_any = W % 2 == 0 && d.ns > 0 && std::getenv("PDT_NO_TENSOR_ROWS") == nullptr;
+    tcf_ok_ = tc_any && W <= kTcMaxW && tc_fwd_smem(W, 256) <= (size_t)g_max_smem;
+    tca_ok_ = tc_any && fcol_.ok() && tc_adj_smem(kTcAdjMaxNB, 2) <= (size_t)g_max_smem;
     if (fcol_.ok() && fast_cols_smem(fcol_, 8) > (size_t)g_max_smem) fcol_ = FastColKernels();
     // compact position P -> output row: P = k1 L + t holds spectrum index k1 + M brev_L(t), which the
     // fftshift puts on row (k + Hf/2) mod Hf
@@ -548,6 +669,22 @@ class CartesianOp : public OpImpl, public SolverHooks {
       if (fcol_.ok())
         PDT_CUDA_CHECK(cudaFuncSetAttribute(fcol_.cols[w], cudaFuncAttributeMaxDynamicSharedMemorySize, g_max_smem));
     }
+    col_x_h_ = col_x;
+    tcb_nb_ = 0;
+    if (tcf_ok_ || tca_ok_) {
+      for (auto fn : {tc_rows_fwd<true>, tc_rows_fwd<false>})
+        PDT_CUDA_CHECK(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, g_max_smem));
+      for (auto fn : {tc_rows_adj<true>, tc_rows_adj<false>})
+        PDT_CUDA_CHECK(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, g_max_smem));
+      tc_err_.ensure(sizeof(int));
+      PDT_CUDA_CHECK(cudaMemset(tc_err_.p, 0, sizeof(int)));
+    }
+    if (tca_ok_) {  // operand tiles; entries past the last row or sampled column stay zero
+      const size_t bytes = (size_t)((C * d.Hi + kTcRows - 1) / kTcRows) * ((2 * d.ns + 31) / 32) * 2 * kTcTileA;
+      tca_.ensure(bytes);
+      PDT_CUDA_CHECK(cudaMemset(tca_.p, 0, bytes));
+    }
+    tune_ = Tune();
     const int row_blocks = (d.Hi + d.RB - 1) / d.RB;
     G_ = std::max(1, std::min(C, (2 * g_num_sms + row_blocks - 1) / row_blocks));
     dev_ = d;
@@ -561,7 +698,7 @@ class CartesianOp : public OpImpl, public SolverHooks {
   // the number of coil groups and cluster reduction versus partial images. Results are cached per
   // (W, H, coils, sampled columns).
   void autotune() {
-    if (!frow_.ok() && !fcol_.ok()) return;
+    if (!frow_.ok() && !fcol_.ok() && !tcf_ok_ && !tca_ok_) return;
     if (pinned_tune()) return;
     static std::mutex g_tune_mu;
     static std::map<std::array<int, 6>, std::pair<Tune, int>> g_tune_cache;
@@ -572,6 +709,7 @@ class CartesianOp : public OpImpl, public SolverHooks {
       if (it != g_tune_cache.end()) {
         tune_ = it->second.first;
         G_ = it->second.second;
+        if (tune_.tca) build_tc_adj_tiles(tc_adj_nb(tune_.nr));
         return;
       }
     }
@@ -614,15 +752,14 @@ class CartesianOp : public OpImpl, public SolverHooks {
     };
     const uint64_t launches0 = g_launches.load();
     Tune best = tune_;
+    float bt = 1e30f, ba = 1e30f;  // best forward / adjoint row times so far
     if (frow_.ok()) {
-      float bt = 1e30f;
       for (int w = 0; w < 3; ++w) {
         tune_.wf = w;
         const float ms = time([&] { launch_rows_fwd(ub.as<float2>(), t, nullptr, st); });
         if (ms < bt) bt = ms, best.wf = w;
       }
       tune_.wf = best.wf;
-      float ba = 1e30f;
       int bestG = G_;
       const int gmax = std::min(dev_.C, 16);
       for (int w = 0; w < 3; ++w)
@@ -635,6 +772,19 @@ class CartesianOp : public OpImpl, public SolverHooks {
             if (ms < ba) ba = ms, best.wa = w, best.cluster = cl != 0, bestG = g;
           }
       G_ = bestG;
+    } else if (tcf_ok_) {
+      bt = time([&] { launch_rows_fwd(ub.as<float2>(), t, nullptr, st); });
+    }
+    if (tcf_ok_) {  // tensor-core forward rows: K splits (cluster sizes)
+      const int nchT = (2 * dev_.W + 31) / 32;
+      for (int ks : {1, 2, 3, 4, 6, 8}) {
+        if (ks > nchT) continue;
+        tune_.tcf = 1;
+        tune_.ks = ks;
+        const float ms = time([&] { launch_rows_fwd(ub.as<float2>(), t, nullptr, st); });
+        if (ms < bt) bt = ms, best.tcf = 1, best.ks = ks;
+      }
+      tune_.tcf = 0;
     }
     if (fcol_.ok()) {
       float bc = 1e30f;
@@ -645,23 +795,52 @@ class CartesianOp : public OpImpl, public SolverHooks {
         });
         if (ms < bc) bc = ms, best.wc = w;
       }
+      tune_.wc = best.wc;
+    }
+    if (tca_ok_) {
+      // the column pass and the adjoint rows together: FFT rows (tuned above) against the tensor-core rows
+      // fed by the column kernel's operand tiles, for a few output-column range counts
+      tune_.wa = best.wa;
+      tune_.cluster = best.cluster;
+      float pair = time([&] {
+        launch_cols(COL_SOLVE, t, t, rr.as<float2>(), ff.as<float2>(), nullptr, nullptr, 0.125f, 1.f, st);
+        launch_rows_adj(t, kh.as<float2>(), G_, st);
+      });
+      for (int nr : {2, 3, 4, 5, 6, 8}) {
+        tune_.nr = nr;
+        build_tc_adj_tiles(tc_adj_nb(nr));
+        const float ms = time([&] {
+          launch_cols(COL_SOLVE, t, t, rr.as<float2>(), ff.as<float2>(), nullptr, nullptr, 0.125f, 1.f, st,
+                      tca_.as<float>());
+          launch_tc_rows_adj(kh.as<float2>(), st);
+        });
+        if (ms < pair) pair = ms, best.tca = 1, best.nr = nr;
+      }
+    }
+    if (const int e = take_tc_error()) {
+      std::fprintf(stderr, "pdt: tensor-core row kernels reported error %d while tuning; using the FFT rows\n", e);
+      best.tcf = best.tca = 0;
     }
     g_launches.fetch_sub(g_launches.load() - launches0);  // tuning launches are not solver work
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     tune_ = best;
+    if (tune_.tca) build_tc_adj_tiles(tc_adj_nb(tune_.nr));
     std::lock_guard<std::mutex> lock(g_tune_mu);
     g_tune_cache[key] = {tune_, G_};
   }
 
-  // PDT_CARTESIAN_TUNE="wf,wc,wa,groups,cluster" (warps per block of rows_fwd, cols, rows_adj; coil
-  // groups; 1 = cluster reduction) replaces the autotuner, e.g. to profile one fixed configuration.
+  // PDT_CARTESIAN_TUNE="wf,wc,wa,groups,cluster[,tcf,tca[,ks,nr]]" (warps per block of rows_fwd, cols,
+  // rows_adj; coil groups; 1 = cluster reduction; 1 = tensor-core DFT forward / adjoint rows; their K
+  // split and output-column ranges) replaces the autotuner, e.g. to profile one fixed configuration.
   bool pinned_tune() {
     const char* env = std::getenv("PDT_CARTESIAN_TUNE");
     if (!env || !*env) return false;
-    int v[5];
-    if (std::sscanf(env, "%d,%d,%d,%d,%d", &v[0], &v[1], &v[2], &v[3], &v[4]) != 5)
-      throw Error(PDT_ERR_INVALID_ARGUMENT, "PDT_CARTESIAN_TUNE: expected wf,wc,wa,groups,cluster");
+    int v[9];
+    const int n = std::sscanf(env, "%d,%d,%d,%d,%d,%d,%d,%d,%d", &v[0], &v[1], &v[2], &v[3], &v[4], &v[5], &v[6],
+                              &v[7], &v[8]);
+    if (n != 5 && n != 7 && n != 9)
+      throw Error(PDT_ERR_INVALID_ARGUMENT, "PDT_CARTESIAN_TUNE: expected wf,wc,wa,groups,cluster[,tcf,tca[,ks,nr]]");
     auto idx = [&](int w) {
       for (int i = 0; i < 3; ++i)
         if (kWpbChoices[i] == w) return i;
@@ -674,6 +853,17 @@ class CartesianOp : public OpImpl, public SolverHooks {
     if (v[3] < 1 || v[3] > std::min(dev_.C, 16) || (tune_.cluster && (v[3] < 2 || v[3] > 8)))
       throw Error(PDT_ERR_INVALID_ARGUMENT, "PDT_CARTESIAN_TUNE: coil groups out of range for this operator");
     G_ = v[3];
+    if (n >= 7) {  // where the tensor-core rows are not available (odd W, ...) the FFT rows run
+      tune_.tcf = v[5] != 0 && tcf_ok_;
+      tune_.tca = v[6] != 0 && tca_ok_;
+    }
+    if (n == 9) {
+      if (v[7] < 1 || v[7] > 8 || v[8] < 1 || v[8] > 64)
+        throw Error(PDT_ERR_INVALID_ARGUMENT, "PDT_CARTESIAN_TUNE: K split must be 1..8 and ranges 1..64");
+      tune_.ks = std::min(v[7], (2 * dev_.W + 31) / 32);
+      tune_.nr = v[8];
+    }
+    if (tune_.tca) build_tc_adj_tiles(tc_adj_nb(tune_.nr));
     return true;
   }
 
@@ -682,8 +872,11 @@ class CartesianOp : public OpImpl, public SolverHooks {
   CartDev dev_{};
   FastRowKernels frow_;
   FastColKernels fcol_;
+  bool tcf_ok_ = false, tca_ok_ = false;
+  std::vector<int> col_x_h_;
+  int tcb_nb_ = 0;  // range size the adjoint DFT tiles in tcb_ were built for
   int G_ = 1;
-  DevBuf tables_, scratch_;
+  DevBuf tables_, scratch_, tc_err_, tca_, tcb_;
 };
 
 std::shared_ptr<OpImpl> make_cartesian_operator(pdt_op_kind kind) { return std::make_shared<CartesianOp>(kind); }
