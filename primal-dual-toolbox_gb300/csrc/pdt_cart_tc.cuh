@@ -16,8 +16,8 @@
 //
 //   tc_rows_adj  grid (N ranges, row tiles). Both operands arrive by bulk copy (cp.async.bulk): the data
 //                tiles as the column kernel wrote them, the DFT factor from tiles precomputed per operator.
-//                Each CTA writes conj(sens_c) . g_c for its rows and output columns into the per-coil
-//                plane c; the primal kernel sums the C planes in coil order (deterministic).
+//                A row tile holds a few image rows of every coil, and each CTA writes the coil sum
+//                sum_c conj(sens_c) . g_c of its rows and output columns (coil order: deterministic).
 //   tc_rows_fwd  grid (row tiles, KS, s tiles), clusters of (1, KS, 1). The threads stage the data operand
 //                (ubar . sens_c, split) and generate the DFT factor from the twiddle table; the KS CTAs of
 //                a cluster take disjoint K (x) ranges and reduce their accumulators through distributed
@@ -82,25 +82,27 @@ __device__ __forceinline__ void tc_issue_chunk(uint32_t tmem, uint32_t a_hi, uin
 }
 
 // ------------------------------------------------------------------------------------------------
-// Adjoint rows: planes[c][y][x] = conj(sens_c[y0 + y][x]) sum_s t2[c][s][y] w^(-p_s q'(x)).
-// K = 2 ns (s, re/im); N = 2 W (x, re/im) cut into ranges of NB; M = C Hi in tiles of 128.
+// Adjoint rows and coil combination: out[y][x] = sum_c conj(sens_c[y0 + y][x]) sum_s t2[c][s][y] w^(-p_s q'(x)).
+// K = 2 ns (s, re/im); N = 2 W (x, re/im) cut into ranges of NB; M: a tile holds yb image rows of all
+// C coils (row m = c yb + yl), so that the coil sum stays inside the CTA and one image is written.
 // Both operands arrive by bulk copy: the data tiles as the column kernel wrote them (tc_put_a), the DFT
-// factor from the operator's precomputed tiles. Thread 0 copies, thread 32 issues the MMAs, all sixteen
-// warps run the epilogue. `nst` stages of [A hi | A lo | B hi | B lo].
+// factor from the operator's precomputed tiles. Thread 0 copies, thread 32 issues the MMAs; the
+// epilogue (1) moves TMEM lanes 32 q .. + 31 (warps q, q + 4, ...: one row per thread, column groups of
+// 8) to shared memory, (2) sums the coils: item (yl, four real columns) per thread, coalesced along x.
+// `nst` stages of [A hi | A lo | B hi | B lo].
 // ------------------------------------------------------------------------------------------------
-constexpr int kTcAdjThreads = 512;  // 16 warps: four per tensor-memory lane quarter in the epilogue
-constexpr int kTcAdjMaxNB = 192;    // output columns per CTA of the adjoint rows
-constexpr int kTcAdjOutThreads = kTcAdjThreads - 64;  // warps 2.. write the output tile
-constexpr int kTcAdjItems = (kTcRows * kTcAdjMaxNB / 4 + kTcAdjOutThreads - 1) / kTcAdjOutThreads;
+constexpr int kTcAdjThreads = 512;  // 16 warps
+constexpr int kTcAdjMaxNB = 256;    // output columns (re/im) per CTA
+constexpr int kTcCoilUnroll = 16;   // coil-sum loads issued together
 
 template <bool SENS>
 __global__ void __launch_bounds__(kTcAdjThreads, 1) tc_rows_adj(CartDev d, const float* __restrict__ atiles,
                                                              const unsigned char* __restrict__ btiles,
-                                                             float2* __restrict__ planes, int NB, int nst,
+                                                             float2* __restrict__ out, int NB, int nst,
                                                              int* __restrict__ err) {
   extern __shared__ unsigned char tc_smem_raw[];
   unsigned char* sm = tc_align1024(tc_smem_raw);
-  const int W = d.W, ns = d.ns, Hi = d.Hi;
+  const int W = d.W, ns = d.ns, Hi = d.Hi, C = d.C, yb = d.tc_yb;
   const uint32_t stage_bytes = tc_stage_bytes(NB);
   uint64_t* full = reinterpret_cast<uint64_t*>(sm + nst * stage_bytes);  // copies of a stage landed
   uint64_t* empty = full + kTcMaxStages;                                  // MMAs of a stage done
@@ -108,39 +110,12 @@ __global__ void __launch_bounds__(kTcAdjThreads, 1) tc_rows_adj(CartDev d, const
   uint32_t* tslot = reinterpret_cast<uint32_t*>(accb + 1);
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int R = d.C * Hi;
   const int n0 = blockIdx.x * NB;
   const int nb = min(NB, (2 * W - n0 + 15) & ~15);
-  const int T = blockIdx.y, r0 = T * kTcRows;
+  const int T = blockIdx.y, ybase = T * yb;
   const int K = 2 * ns;
   const int nch = (K + 31) >> 5;
-
-  // Roles: thread 0 copies, thread 32 issues the MMAs; warps 2..15 load the coil-map values of their
-  // output items now (they arrive while the MMAs run). Epilogue: (1) warp (q, h) moves TMEM lanes
-  // 32 q .. + 31 (one row per thread), column groups [gb, ge) of 8, to shared memory; (2) warps 2..15
-  // write the tile row by row, four real columns (two outputs) per item, coalesced, times the coil map.
-  const int q = warp & 3, h = warp >> 2;
-  const int G8 = nb >> 3, gb = h * G8 / 4, ge = (h + 1) * G8 / 4;
-  const int F4 = nb >> 2;  // float4 groups per row
-  const bool out_warp = warp >= 2;
-  const int ot = tid - 64;  // output thread index (warps 2..15)
-  const int drow = kTcAdjOutThreads / F4, dcol = kTcAdjOutThreads - drow * F4;
-  float4 sv[kTcAdjItems];
-  if (SENS && out_warp) {
-    int row = ot / F4, f = ot - row * F4;
-#pragma unroll
-    for (int k = 0; k < kTcAdjItems; ++k) {
-      const int r = r0 + row, x = (n0 >> 1) + 2 * f;  // even; W even, so x + 1 < W as well
-      sv[k] = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (row < kTcRows && r < R && x < W) {
-        const int c = r / Hi, y = r - c * Hi;
-        sv[k] = *reinterpret_cast<const float4*>(d.sens + ((size_t)c * d.Hf + y + d.y0) * W + x);
-      }
-      row += drow;
-      f += dcol;
-      if (f >= F4) f -= F4, ++row;
-    }
-  }
+  const int F4 = nb >> 2;  // float4 groups (two outputs) per row
 
   if (tid == 0) {
     for (int i = 0; i < nst; ++i) {
@@ -157,24 +132,20 @@ __global__ void __launch_bounds__(kTcAdjThreads, 1) tc_rows_adj(CartDev d, const
   const uint32_t tmem = *tslot;
 
   const uint32_t base = tc::smem_addr(sm);
-  bool ok = true;
-  if (tid == 0) {
-    const unsigned char* bsrc = btiles + (size_t)blockIdx.x * nch * 2 * NB * 128;
-    const uint32_t bbytes = 2u * (uint32_t)nb * 128u;
-    // the DFT-factor tiles are constants: the first stages' copies start before the column kernel ends
-    const int pre = min(nst, nch);
+  const uint32_t bbytes = 2u * (uint32_t)nb * 128u;
+  const unsigned char* bsrc = btiles + (size_t)blockIdx.x * nch * 2 * NB * 128;
+  const int pre = min(nst, nch);
+  if (tid == 0) {  // the DFT-factor tiles are constants: their first copies start before the column kernel ends
     for (int j = 0; j < pre; ++j) {
-      const uint32_t dst = base + j * stage_bytes;
       tc::mbar_arrive_expect_tx(&full[j], 2 * kTcTileA + bbytes);
-      tc::bulk_g2s(dst + 2 * kTcTileA, bsrc + (size_t)j * 2 * NB * 128, bbytes, &full[j]);
+      tc::bulk_g2s(base + j * stage_bytes + 2 * kTcTileA, bsrc + (size_t)j * 2 * NB * 128, bbytes, &full[j]);
     }
   }
   pdl_wait();  // every thread: the data tiles come from the column kernel
+
+  bool ok = true;
   if (tid == 0) {
     const float* asrc = atiles + (size_t)T * nch * (2 * 128 * 32);
-    const unsigned char* bsrc = btiles + (size_t)blockIdx.x * nch * 2 * NB * 128;
-    const uint32_t bbytes = 2u * (uint32_t)nb * 128u;
-    const int pre = min(nst, nch);
     tc::fence_async_global();
     for (int j = 0; j < pre; ++j)
       tc::bulk_g2s(base + j * stage_bytes, asrc + (size_t)j * (2 * 128 * 32), 2 * kTcTileA, &full[j]);
@@ -213,11 +184,29 @@ __global__ void __launch_bounds__(kTcAdjThreads, 1) tc_rows_adj(CartDev d, const
     }
     tc::fence_before_sync();
   }
+
+  // coil-map values of this thread's first output item: the other threads load them while the MMAs run
+  const int yrows = min(yb, Hi - ybase);  // image rows of this tile
+  const int nitems = yrows * F4;
+  float4 sv[kTcCoilUnroll];
+  {
+    const int yl = tid / F4, f = tid - yl * F4;
+    const int x = (n0 >> 1) + 2 * f;  // even; W even, so x + 1 < W as well
+    const bool iv = tid < nitems && x < W;
+#pragma unroll
+    for (int c = 0; c < kTcCoilUnroll; ++c) {
+      sv[c] = make_float4(1.f, 0.f, 1.f, 0.f);
+      if (SENS && iv && c < C)
+        sv[c] = *reinterpret_cast<const float4*>(d.sens + ((size_t)c * d.Hf + ybase + yl + d.y0) * W + x);
+    }
+  }
   const bool done = __syncthreads_and(ok);
   tc::fence_after_sync();
   float* dt = reinterpret_cast<float*>(sm);  // the stage buffers are free: every MMA has completed
   const int ld = nb + 4;                      // row stride: 16-byte row-per-thread stores conflict-free
   if (done) {
+    const int q = warp & 3, h = warp >> 2;
+    const int G8 = nb >> 3, gb = h * G8 / 4, ge = (h + 1) * G8 / 4;
     const uint32_t taddr = tmem + ((uint32_t)(32 * q) << 16);
     float* drow = dt + (size_t)(32 * q + lane) * ld;
     for (int g = gb; g < ge; ++g) {  // warp-uniform bounds
@@ -228,20 +217,40 @@ __global__ void __launch_bounds__(kTcAdjThreads, 1) tc_rows_adj(CartDev d, const
     }
   }
   __syncthreads();
-  if (done && out_warp) {
-    int row = ot / F4, f = ot - row * F4;
+  if (done) {
+    for (int i = tid; i < nitems; i += kTcAdjThreads) {
+      const int yl = i / F4, f = i - yl * F4;
+      const int x = (n0 >> 1) + 2 * f;
+      if (x >= W) continue;
+      const int y = ybase + yl;
+      const float* drow = dt + (size_t)yl * ld + 4 * f;  // row c yb + yl of coil c
+      const float2* srow = d.sens + ((size_t)y + d.y0) * W + x;  // coil c at + c Hf W
+      const size_t sstride = (size_t)d.Hf * W;
+      float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+      auto add = [&](int c, float4 sc) {
+        const float4 v = *reinterpret_cast<const float4*>(drow + (size_t)c * yb * ld);
+        const float4 p = SENS ? tc_cmulc2(v, sc) : v;  // D . conj(sens_c) for two outputs
+        acc.x += p.x;
+        acc.y += p.y;
+        acc.z += p.z;
+        acc.w += p.w;
+      };
+      if (i == tid) {  // this thread's first item: the coil-map values of the first coils are loaded
 #pragma unroll
-    for (int k = 0; k < kTcAdjItems; ++k) {
-      const int r = r0 + row, x = (n0 >> 1) + 2 * f;
-      if (row < kTcRows && r < R && x < W) {
-        const int c = r / Hi, y = r - c * Hi;
-        float4 o = *reinterpret_cast<const float4*>(dt + (size_t)row * ld + 4 * f);
-        if (SENS) o = tc_cmulc2(o, sv[k]);
-        *reinterpret_cast<float4*>(planes + ((size_t)c * Hi + y) * W + x) = o;
+        for (int c = 0; c < kTcCoilUnroll; ++c)
+          if (c < C) add(c, sv[c]);
+      } else {
+        float4 s4[kTcCoilUnroll];
+#pragma unroll
+        for (int c = 0; c < kTcCoilUnroll; ++c)
+          s4[c] = (SENS && c < C) ? *reinterpret_cast<const float4*>(srow + c * sstride) : make_float4(1.f, 0.f, 1.f, 0.f);
+#pragma unroll
+        for (int c = 0; c < kTcCoilUnroll; ++c)
+          if (c < C) add(c, s4[c]);
       }
-      row += drow;
-      f += dcol;
-      if (f >= F4) f -= F4, ++row;
+      for (int c = kTcCoilUnroll; c < C; ++c)
+        add(c, SENS ? *reinterpret_cast<const float4*>(srow + c * sstride) : make_float4(1.f, 0.f, 1.f, 0.f));
+      *reinterpret_cast<float4*>(out + (size_t)y * W + x) = acc;  // coils summed in coil order
     }
   }
   tc::fence_before_sync();

@@ -59,7 +59,7 @@ struct CartDev {
   // Solver rounds with tensor-core adjoint rows: the column kernels write their image-row output as
   // TF32 hi/lo operand tiles (tca, tc_nch K chunks per 128-row tile) instead of t[c][s][yi].
   float* tca;
-  int tc_nch;
+  int tc_nch, tc_yb;
 };
 
 enum ColMode { COL_SOLVE = 0, COL_FWD_DENSE = 1, COL_ADJ_DENSE = 2, COL_ADJ_COMPACT = 3 };
@@ -291,7 +291,8 @@ class CartesianOp : public OpImpl, public SolverHooks {
       os << " rows_fwd=stockham";
     if (tune_.tca)
       os << " rows_adj=tensor_dft(tf32x3,n_ranges=" << (2 * dev_.W + tc_adj_nb(tune_.nr) - 1) / tc_adj_nb(tune_.nr)
-         << ",stages=" << tc_adj_stages(tc_adj_nb(tune_.nr)) << ",coil_planes=" << dev_.C << ")";
+         << ",row_tiles=" << tc_adj_tiles() << "x" << tc_adj_yb() << "rows,stages=" << tc_adj_stages(tc_adj_nb(tune_.nr))
+         << ",coil_sum_on_chip)";
     else if (frow_.ok())
       os << " rows_adj=lane_fft(warps=" << kWpbChoices[tune_.wa] << ",coil_groups=" << G_
          << (tune_.cluster ? ",cluster" : ",partials") << ")";
@@ -325,7 +326,7 @@ class CartesianOp : public OpImpl, public SolverHooks {
   }
   int groups() override {
     prepare();
-    if (tune_.tca) return dev_.C;                    // one plane per coil (tensor-core adjoint rows)
+    if (tune_.tca) return 1;                         // the tensor-core adjoint rows sum the coils on chip
     return (frow_.ok() && tune_.cluster) ? 1 : G_;  // a cluster reduces its coil groups on chip
   }
   long long group_stride() override { return (long long)dev_.Hi * dev_.W; }
@@ -358,6 +359,11 @@ class CartesianOp : public OpImpl, public SolverHooks {
       return;
     }
     float2* t = scratch_.as<float2>();
+    if (tune_.tca) {
+      launch_cols(COL_ADJ_COMPACT, nullptr, t, nullptr, fc, nullptr, nullptr, 0.f, 0.f, st, tca_.as<float>());
+      launch_tc_rows_adj(img, st);
+      return;
+    }
     launch_cols(COL_ADJ_COMPACT, nullptr, t, nullptr, fc, nullptr, nullptr, 0.f, 0.f, st);
     launch_rows_adj(t, img, 1, st);
   }
@@ -397,6 +403,11 @@ class CartesianOp : public OpImpl, public SolverHooks {
       return;
     }
     float2* t = scratch_.as<float2>();
+    if (tune_.tca) {
+      launch_cols(COL_ADJ_DENSE, nullptr, t, nullptr, nullptr, src, nullptr, 0.f, 0.f, st, tca_.as<float>());
+      launch_tc_rows_adj(dst, st);
+      return;
+    }
     launch_cols(COL_ADJ_DENSE, nullptr, t, nullptr, nullptr, src, nullptr, 0.f, 0.f, st);
     launch_rows_adj(t, dst, 1, st);
   }
@@ -423,6 +434,9 @@ class CartesianOp : public OpImpl, public SolverHooks {
     count_launch();
   }
   int tc_adj_chunks() const { return (2 * dev_.ns + 31) / 32; }
+  // image rows per adjoint row tile: the tile's 128 rows hold them for every coil
+  int tc_adj_yb() const { return kTcRows / dev_.C; }
+  int tc_adj_tiles() const { return (dev_.Hi + tc_adj_yb() - 1) / tc_adj_yb(); }
   int tc_adj_stages(int NB) const {
     return std::min(kTcMaxStages, (int)(((size_t)g_max_smem - tc_adj_smem(NB, 0)) / tc_stage_bytes(NB)));
   }
@@ -472,9 +486,11 @@ class CartesianOp : public OpImpl, public SolverHooks {
     const int NB = tc_adj_nb(tune_.nr);
     if (tcb_nb_ != NB) throw Error(PDT_ERR_STATE, name_ + ": tensor-core adjoint tiles not built for this range size");
     const int nst = tc_adj_stages(NB);
-    LaunchEx lx(dim3((2 * dev_.W + NB - 1) / NB, tc_row_tiles()), dim3(kTcAdjThreads), tc_adj_smem(NB, nst), st);
+    CartDev dd = dev_;
+    dd.tc_yb = tc_adj_yb();
+    LaunchEx lx(dim3((2 * dev_.W + NB - 1) / NB, tc_adj_tiles()), dim3(kTcAdjThreads), tc_adj_smem(NB, nst), st);
     auto fn = dev_.sens ? tc_rows_adj<true> : tc_rows_adj<false>;
-    PDT_CUDA_CHECK(cudaLaunchKernelEx(&lx.cfg, fn, dev_, (const float*)tca_.as<float>(),
+    PDT_CUDA_CHECK(cudaLaunchKernelEx(&lx.cfg, fn, dd, (const float*)tca_.as<float>(),
                                       (const unsigned char*)tcb_.p, planes, NB, nst, tc_err()));
     count_launch();
   }
@@ -517,6 +533,7 @@ class CartesianOp : public OpImpl, public SolverHooks {
       if (tiles) {
         dd.tca = tiles;
         dd.tc_nch = tc_adj_chunks();
+        dd.tc_yb = tc_adj_yb();
       }
       LaunchEx lx(dim3((dev_.ns + S - 1) / S, dev_.C), dim3(32 * wpb), fast_cols_smem(fcol_, wpb), st);
       PDT_CUDA_CHECK(cudaLaunchKernelEx(&lx.cfg, fcol_.cols[tune_.wc], dd, mode, tin, tout, r, fc, kin, kout, sigma,
@@ -605,7 +622,7 @@ class CartesianOp : public OpImpl, public SolverHooks {
     // are sized for W <= kTcMaxW; the adjoint's operand tiles come from the lane-FFT column kernels
     const bool tc_any = W % 2 == 0 && d.ns > 0 && std::getenv("PDT_NO_TENSOR_ROWS") == nullptr;
     tcf_ok_ = tc_any && W <= kTcMaxW && tc_fwd_smem(W, 256) <= (size_t)g_max_smem;
-    tca_ok_ = tc_any && fcol_.ok() && tc_adj_smem(kTcAdjMaxNB, 2) <= (size_t)g_max_smem;
+    tca_ok_ = tc_any && fcol_.ok() && C <= kTcRows && tc_adj_smem(kTcAdjMaxNB, 2) <= (size_t)g_max_smem;
     if (fcol_.ok() && fast_cols_smem(fcol_, 8) > (size_t)g_max_smem) fcol_ = FastColKernels();
     // compact position P -> output row: P = k1 L + t holds spectrum index k1 + M brev_L(t), which the
     // fftshift puts on row (k + Hf/2) mod Hf
@@ -680,7 +697,8 @@ class CartesianOp : public OpImpl, public SolverHooks {
       PDT_CUDA_CHECK(cudaMemset(tc_err_.p, 0, sizeof(int)));
     }
     if (tca_ok_) {  // operand tiles; entries past the last row or sampled column stay zero
-      const size_t bytes = (size_t)((C * d.Hi + kTcRows - 1) / kTcRows) * ((2 * d.ns + 31) / 32) * 2 * kTcTileA;
+      const int yb = kTcRows / C;
+      const size_t bytes = (size_t)((d.Hi + yb - 1) / yb) * ((2 * d.ns + 31) / 32) * 2 * kTcTileA;
       tca_.ensure(bytes);
       PDT_CUDA_CHECK(cudaMemset(tca_.p, 0, bytes));
     }
