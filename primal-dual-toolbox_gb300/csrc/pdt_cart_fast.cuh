@@ -17,28 +17,11 @@
 #include <cooperative_groups.h>
 
 #include "pdt_regfft.cuh"
-#include "pdt_tc.cuh"
 
 namespace cg = cooperative_groups;
 
 namespace pdt {
 namespace {
-
-// One value of the adjoint rows' data operand: image row yi of coil c, sampled column s. A tile holds
-// yb image rows of every coil (tile row m = c yb + yi mod yb, tile yi / yb), 32 FP32 along K (16
-// sampled columns re/im), as TF32 hi/lo parts in 128-byte-swizzled K-major layout; tiles run
-// [row tile][K chunk][hi | lo] (tc_rows_adj copies one (row tile, chunk) pair of 32 KB per stage).
-__device__ __forceinline__ void tc_put_a(float* __restrict__ tiles, int nch, int yb, int c, int yi, int s,
-                                         float2 v) {
-  const int T = yi / yb, m = c * yb + (yi - T * yb), u = (s & 15) >> 1;
-  float* tile = tiles + ((size_t)T * nch + (s >> 4)) * (2 * 128 * 32);
-  const int off = m * 32 + ((u ^ (m & 7)) << 2) + ((s & 1) << 1);
-  float2 hi, lo;
-  tc::split_tf32(v.x, hi.x, lo.x);
-  tc::split_tf32(v.y, hi.y, lo.y);
-  *reinterpret_cast<float2*>(tile + off) = hi;
-  *reinterpret_cast<float2*>(tile + 128 * 32 + off) = lo;
-}
 
 // Phase 1: rows of ubar . sens_c -> FFT along W -> sampled columns t1[c][s][yi]. A block takes
 // R = WPB * 32 / L consecutive rows of one coil and writes each sampled column's R rows as one run.
@@ -186,10 +169,7 @@ __global__ void __launch_bounds__(32 * WPB) fl_cols(CartDev d, int mode, const f
       int yf = t + L * j + d.oyH;
       if (yf >= Hf) yf -= Hf;
       const int yi = yf - d.y0;
-      if (yi >= 0 && yi < d.Hi) {
-        if (d.tca) tc_put_a(d.tca, d.tc_nch, d.tc_yb, c, yi, s, v[j] * d.scale);
-        else t_out[colc * d.Hi + yi] = v[j] * d.scale;
-      }
+      if (yi >= 0 && yi < d.Hi) t_out[colc * d.Hi + yi] = v[j] * d.scale;
     }
   }
 }
@@ -284,10 +264,7 @@ __global__ void __launch_bounds__(32 * WPB) fl_cols64(CartDev d, int mode, const
       int yf = t + L * j + d.oyH;
       if (yf >= Hf) yf -= Hf;
       const int yi = yf - d.y0;
-      if (yi >= 0 && yi < d.Hi) {
-        if (d.tca) tc_put_a(d.tca, d.tc_nch, d.tc_yb, c, yi, s, v[j] * d.scale);
-        else t_out[colc * d.Hi + yi] = v[j] * d.scale;
-      }
+      if (yi >= 0 && yi < d.Hi) t_out[colc * d.Hi + yi] = v[j] * d.scale;
     }
   }
 }

@@ -14,14 +14,14 @@
 // MMAs per K step (hi.hi + hi.lo + lo.hi, FP32 accumulate in tensor memory) and commits them to the
 // stage's mbarrier.
 //
-//   tc_rows_adj  grid (N ranges, row tiles). Both operands arrive by bulk copy (cp.async.bulk): the data
-//                tiles as the column kernel wrote them, the DFT factor from tiles precomputed per operator.
-//                A row tile holds a few image rows of every coil, and each CTA writes the coil sum
+//   tc_rows_adj  grid (N ranges, row tiles). The DFT factor arrives by bulk copy (cp.async.bulk) from
+//                tiles precomputed per operator; the threads stage the data operand from t2. A row tile
+//                holds a few image rows of every coil, and each CTA writes the coil sum
 //                sum_c conj(sens_c) . g_c of its rows and output columns (coil order: deterministic).
-//   tc_rows_fwd  grid (row tiles, KS, s tiles), clusters of (1, KS, 1). The threads stage the data operand
-//                (ubar . sens_c, split) and generate the DFT factor from the twiddle table; the KS CTAs of
-//                a cluster take disjoint K (x) ranges and reduce their accumulators through distributed
-//                shared memory in rank order (deterministic) before writing t1.
+//   tc_rows_fwd  grid (row tiles, KS, s tiles), clusters of (1, KS, 1). The DFT factor arrives by bulk
+//                copy, the threads form the data operand (ubar . sens_c, split); the KS CTAs of a cluster
+//                take disjoint K (x) ranges and reduce their accumulators through distributed shared
+//                memory in rank order (deterministic) before writing t1.
 #pragma once
 
 #include <cooperative_groups.h>
@@ -31,27 +31,14 @@
 namespace pdt {
 namespace {
 
-constexpr int kTcThreads = 256;
 constexpr int kTcRows = 128;
 constexpr uint32_t kTcTmemCols = 256;
 constexpr uint32_t kTcTileA = 128 * 128;  // bytes of one 128-row x 32-element FP32 tile
-constexpr int kTcMaxW = 1024;             // twiddle table and index products (< 2^20) sized for this
 constexpr int kTcMaxStages = 4;
 
 __device__ __forceinline__ unsigned char* tc_align1024(unsigned char* raw) {
   const uint32_t off = tc::smem_addr(raw);
   return raw + ((1024u - (off & 1023u)) & 1023u);
-}
-
-// (a b) mod W for 0 <= a, b < W <= 1024: the product is exact in FP32, the quotient estimate is off by
-// at most one and corrected.
-__device__ __forceinline__ int tc_mod_mul(int a, int b, int W, float invW) {
-  const int p = a * b;
-  const int q = __float2int_rz(__int2float_rn(p) * invW);
-  int m = p - q * W;
-  if (m < 0) m += W;
-  if (m >= W) m -= W;
-  return m;
 }
 
 __device__ __forceinline__ float4 tc_cmul2(float4 a, float4 b) {
@@ -65,7 +52,7 @@ __device__ __forceinline__ float4 tc_cmulc2(float4 a, float4 b) {  // a . conj(b
 // stage, two stages, then the kernel's tables.
 __host__ __device__ inline uint32_t tc_stage_bytes(int nbmax) { return 2 * kTcTileA + 2u * (uint32_t)nbmax * 128u; }
 inline size_t tc_adj_smem(int NB, int nst) { return 1024 + (size_t)nst * tc_stage_bytes(NB) + 16 * kTcMaxStages + 32; }
-inline size_t tc_fwd_smem(int W, int nb) { return 1024 + 2 * (size_t)tc_stage_bytes(nb) + 8 * (size_t)W + 4 * 128 + 64; }
+inline size_t tc_fwd_smem(int nb, int nst) { return 1024 + (size_t)nst * tc_stage_bytes(nb) + 16 * kTcMaxStages + 32; }
 
 // Issues the MMAs of one staged K chunk (ksteps <= 4 steps of K = 8) and commits them to `bar`.
 __device__ __forceinline__ void tc_issue_chunk(uint32_t tmem, uint32_t a_hi, uint32_t a_lo, uint32_t b_hi,
@@ -85,18 +72,20 @@ __device__ __forceinline__ void tc_issue_chunk(uint32_t tmem, uint32_t a_hi, uin
 // Adjoint rows and coil combination: out[y][x] = sum_c conj(sens_c[y0 + y][x]) sum_s t2[c][s][y] w^(-p_s q'(x)).
 // K = 2 ns (s, re/im); N = 2 W (x, re/im) cut into ranges of NB; M: a tile holds yb image rows of all
 // C coils (row m = c yb + yl), so that the coil sum stays inside the CTA and one image is written.
-// Both operands arrive by bulk copy: the data tiles as the column kernel wrote them (tc_put_a), the DFT
-// factor from the operator's precomputed tiles. Thread 0 copies, thread 32 issues the MMAs; the
-// epilogue (1) moves TMEM lanes 32 q .. + 31 (warps q, q + 4, ...: one row per thread, column groups of
-// 8) to shared memory, (2) sums the coils: item (yl, four real columns) per thread, coalesced along x.
-// `nst` stages of [A hi | A lo | B hi | B lo].
+// Thread 0 bulk-copies the DFT factor from the operator's precomputed tiles; warps 2..15 stage the data
+// operand from t2 (split into TF32 hi/lo) and arrive on the stage's barrier; thread 32 issues the MMAs.
+// The epilogue (1) moves TMEM lanes 32 q .. + 31 (warps q, q + 4, ...: one row per thread, column
+// groups of 8) to shared memory, (2) sums the coils: item (yl, four real columns) per thread, coalesced
+// along x. `nst` stages of [A hi | A lo | B hi | B lo].
 // ------------------------------------------------------------------------------------------------
-constexpr int kTcAdjThreads = 512;  // 16 warps
+constexpr int kTcAdjThreads = 512;  // 16 warps: copy thread (warp 0), MMA thread (warp 1), 14 staging warps
+constexpr int kTcStagers = kTcAdjThreads - 64;
+constexpr int kTcStageItems = (kTcRows * 8 + kTcStagers - 1) / kTcStagers;  // staging items per thread
 constexpr int kTcAdjMaxNB = 256;    // output columns (re/im) per CTA
 constexpr int kTcCoilUnroll = 16;   // coil-sum loads issued together
 
 template <bool SENS>
-__global__ void __launch_bounds__(kTcAdjThreads, 1) tc_rows_adj(CartDev d, const float* __restrict__ atiles,
+__global__ void __launch_bounds__(kTcAdjThreads, 1) tc_rows_adj(CartDev d, const float2* __restrict__ t2,
                                                              const unsigned char* __restrict__ btiles,
                                                              float2* __restrict__ out, int NB, int nst,
                                                              int* __restrict__ err) {
@@ -104,7 +93,7 @@ __global__ void __launch_bounds__(kTcAdjThreads, 1) tc_rows_adj(CartDev d, const
   unsigned char* sm = tc_align1024(tc_smem_raw);
   const int W = d.W, ns = d.ns, Hi = d.Hi, C = d.C, yb = d.tc_yb;
   const uint32_t stage_bytes = tc_stage_bytes(NB);
-  uint64_t* full = reinterpret_cast<uint64_t*>(sm + nst * stage_bytes);  // copies of a stage landed
+  uint64_t* full = reinterpret_cast<uint64_t*>(sm + nst * stage_bytes);  // B copies + A stores landed
   uint64_t* empty = full + kTcMaxStages;                                  // MMAs of a stage done
   uint64_t* accb = empty + kTcMaxStages;                                  // every MMA done (one phase)
   uint32_t* tslot = reinterpret_cast<uint32_t*>(accb + 1);
@@ -119,7 +108,7 @@ __global__ void __launch_bounds__(kTcAdjThreads, 1) tc_rows_adj(CartDev d, const
 
   if (tid == 0) {
     for (int i = 0; i < nst; ++i) {
-      tc::mbar_init(&full[i], 1);
+      tc::mbar_init(&full[i], 1 + kTcStagers / 32);
       tc::mbar_init(&empty[i], 1);
     }
     tc::mbar_init(accb, 1);
@@ -134,40 +123,27 @@ __global__ void __launch_bounds__(kTcAdjThreads, 1) tc_rows_adj(CartDev d, const
   const uint32_t base = tc::smem_addr(sm);
   const uint32_t bbytes = 2u * (uint32_t)nb * 128u;
   const unsigned char* bsrc = btiles + (size_t)blockIdx.x * nch * 2 * NB * 128;
-  const int pre = min(nst, nch);
-  if (tid == 0) {  // the DFT-factor tiles are constants: their first copies start before the column kernel ends
-    for (int j = 0; j < pre; ++j) {
-      tc::mbar_arrive_expect_tx(&full[j], 2 * kTcTileA + bbytes);
-      tc::bulk_g2s(base + j * stage_bytes + 2 * kTcTileA, bsrc + (size_t)j * 2 * NB * 128, bbytes, &full[j]);
-    }
-  }
-  pdl_wait();  // every thread: the data tiles come from the column kernel
-
   bool ok = true;
-  if (tid == 0) {
-    const float* asrc = atiles + (size_t)T * nch * (2 * 128 * 32);
-    tc::fence_async_global();
-    for (int j = 0; j < pre; ++j)
-      tc::bulk_g2s(base + j * stage_bytes, asrc + (size_t)j * (2 * 128 * 32), 2 * kTcTileA, &full[j]);
-    for (int j = pre; j < nch && ok; ++j) {
+  if (tid == 0) {  // DFT-factor tiles (constants: the first copies may start before the column kernel ends)
+    for (int j = 0; j < nch && ok; ++j) {
       const int b = j % nst;
-      ok = tc::mbar_wait(&empty[b], ((j / nst) - 1) & 1);  // the MMAs of chunk j - nst are done
+      if (j >= nst) ok = tc::mbar_wait(&empty[b], ((j / nst) - 1) & 1);  // the MMAs of chunk j - nst are done
       if (!ok) {
-        atomicCAS(err, 0, 0x100 | j);  // the copy thread gave up at chunk j
+        atomicCAS(err, 0, 0x100 | j);
         break;
       }
-      const uint32_t dst = base + b * stage_bytes;
-      tc::mbar_arrive_expect_tx(&full[b], 2 * kTcTileA + bbytes);
-      tc::bulk_g2s(dst, asrc + (size_t)j * (2 * 128 * 32), 2 * kTcTileA, &full[b]);
-      tc::bulk_g2s(dst + 2 * kTcTileA, bsrc + (size_t)j * 2 * NB * 128, bbytes, &full[b]);
+      tc::mbar_arrive_expect_tx(&full[b], bbytes);
+      tc::bulk_g2s(base + b * stage_bytes + 2 * kTcTileA, bsrc + (size_t)j * 2 * NB * 128, bbytes, &full[b]);
     }
-  } else if (tid == 32) {
+  }
+  pdl_wait();  // every thread: t2 comes from the column kernel
+  if (tid == 32) {
     const uint32_t idesc = tc::idesc_tf32(kTcRows, nb);
     for (int j = 0; j < nch && ok; ++j) {
       const int b = j % nst;
       ok = tc::mbar_wait(&full[b], (j / nst) & 1);
       if (!ok) {
-        atomicCAS(err, 0, 0x200 | j);  // the MMA thread gave up waiting for chunk j's copies
+        atomicCAS(err, 0, 0x200 | j);  // the MMA thread gave up waiting for chunk j's operands
         break;
       }
       const uint32_t a_hi = base + b * stage_bytes, a_lo = a_hi + kTcTileA;
@@ -183,6 +159,64 @@ __global__ void __launch_bounds__(kTcAdjThreads, 1) tc_rows_adj(CartDev d, const
       ok = false;
     }
     tc::fence_before_sync();
+  } else if (warp >= 2) {
+    // data operand: tile row m = c yb + yl, 16-byte chunk p = sampled columns 16 j + 2p, + 1 (re/im
+    // each), split into TF32 hi/lo. Item it = ot + kTcStagers k, yl fastest (consecutive image rows of
+    // t2 for consecutive threads); the next chunk's values are loaded before the wait for its stage.
+    const int ot = tid - 64;
+    const int nit = C * yb * 8;  // items of the C yb tile rows in use (<= 128 x 8); later rows stay unused
+    int im[kTcStageItems], ioff[kTcStageItems];
+#pragma unroll
+    for (int k = 0; k < kTcStageItems; ++k) {
+      const int it = ot + kTcStagers * k;
+      const int yl = it % yb, rest = it / yb, p = rest & 7, c = rest >> 3;
+      const int y = ybase + yl;
+      const bool valid = it < nit && y < Hi;
+      im[k] = valid ? ((c * yb + yl) << 3 | p) : -1;  // tile row and chunk
+      ioff[k] = (c * ns + 2 * p) * Hi + y;             // t2 offset of column 2p of chunk 0
+    }
+    float2 va[kTcStageItems], vb[kTcStageItems];
+    auto load = [&](int j) {
+#pragma unroll
+      for (int k = 0; k < kTcStageItems; ++k) {
+        const int s = 16 * j + 2 * ((im[k] >= 0 ? im[k] : 0) & 7);
+        va[k] = vb[k] = c2(0.f, 0.f);
+        if (im[k] >= 0 && s < ns) va[k] = t2[(size_t)ioff[k] + (size_t)16 * j * Hi];
+        if (im[k] >= 0 && s + 1 < ns) vb[k] = t2[(size_t)ioff[k] + (size_t)(16 * j + 1) * Hi];
+      }
+    };
+    if (nch > 0) load(0);
+    for (int j = 0; j < nch && ok; ++j) {
+      const int b = j % nst;
+      float4 cur[kTcStageItems];
+#pragma unroll
+      for (int k = 0; k < kTcStageItems; ++k) cur[k] = make_float4(va[k].x, va[k].y, vb[k].x, vb[k].y);
+      if (j + 1 < nch) load(j + 1);
+      if (j >= nst) {  // one lane polls; the others wait in the warp barrier without taking issue slots
+        if (lane == 0) ok = tc::mbar_wait(&empty[b], ((j / nst) - 1) & 1);
+        ok = __shfl_sync(0xffffffffu, ok, 0);
+      }
+      if (!ok) {
+        if (lane == 0) atomicCAS(err, 0, 0x400 | j);
+        break;
+      }
+      const uint32_t a_hi = base + b * stage_bytes, a_lo = a_hi + kTcTileA;
+#pragma unroll
+      for (int k = 0; k < kTcStageItems; ++k) {
+        const int it = ot + kTcStagers * k;
+        if (it < nit) {  // tile row m = c yb + yl < C yb <= 128 (a D row depends on its own A row only)
+          const int yl = it % yb, rest = it / yb, p = rest & 7, m = (rest >> 3) * yb + yl;
+          float4 hi, lo;
+          tc::split4(cur[k], hi, lo);  // zero for image rows past the last one
+          const uint32_t o = tc::sw128(m, p);
+          tc::st_shared4(a_hi + o, hi);
+          tc::st_shared4(a_lo + o, lo);
+        }
+      }
+      tc::fence_async_smem();
+      __syncwarp();
+      if (lane == 0) tc::mbar_arrive(&full[b]);  // one arrival per staging warp
+    }
   }
 
   // coil-map values of this thread's first output item: the other threads load them while the MMAs run
@@ -262,161 +296,212 @@ __global__ void __launch_bounds__(kTcAdjThreads, 1) tc_rows_adj(CartDev d, const
 }
 
 // ------------------------------------------------------------------------------------------------
-// Forward rows: t1[c][s][y] = sum_x (ubar . sens_c)[y][x] w^(q(x) f_s) for the 128 sampled columns of
-// s tile blockIdx.z. K = 2 W (x, re/im) split over the KS CTAs of a cluster; N = 2 (s, re/im) <= 256.
+// Forward rows: t1[c][s][y] = sum_x (ubar . sens_c)[y][x] w^(q(x) f_s) for the 128 sampled columns of s
+// tile blockIdx.z. K = 2 W (x, re/im), split over the KS CTAs of a cluster (grid.y); N = 2 (s, re/im)
+// <= 256; M: the adjoint's row tiles (yb image rows of every coil). The DFT factor arrives by bulk copy
+// (thread 0); warps 2..15 form the data operand ubar . sens_c on chip, split it into TF32 hi/lo parts
+// and arrive on the stage's barrier; thread 32 issues the MMAs. The KS partial accumulators are summed
+// through distributed shared memory in rank order (deterministic).
 // ------------------------------------------------------------------------------------------------
+constexpr int kTcFwdThreads = 512;
+constexpr int kTcFwdStagers = kTcFwdThreads - 64;
+constexpr int kTcFwdItems = (kTcRows * 8 + kTcFwdStagers - 1) / kTcFwdStagers;  // staging items per thread
+constexpr int kTcFwdBatch = 4;  // reduction items per thread whose remote loads are in flight together
+
 template <bool SENS>
-__global__ void __launch_bounds__(kTcThreads, 1) tc_rows_fwd(CartDev d, const float2* __restrict__ ubar,
+__global__ void __launch_bounds__(kTcFwdThreads, 1) tc_rows_fwd(CartDev d, const float2* __restrict__ ubar,
+                                                             const unsigned char* __restrict__ btiles,
                                                              float2* __restrict__ t1, int* __restrict__ tick,
-                                                             int* __restrict__ err) {
+                                                             int nst, int* __restrict__ err) {
   namespace cg = cooperative_groups;
   extern __shared__ unsigned char tc_smem_raw[];
   unsigned char* sm = tc_align1024(tc_smem_raw);
-  const int W = d.W, ns = d.ns, Hi = d.Hi;
+  const int W = d.W, ns = d.ns, Hi = d.Hi, C = d.C, yb = d.tc_yb;
   const int s0 = blockIdx.z * 128, nsl = min(128, ns - s0);
   const int nb = (2 * nsl + 15) & ~15;
+  const int nbmax = (2 * min(128, ns) + 15) & ~15;  // B tile stride of the precomputed tiles
   const uint32_t stage_bytes = tc_stage_bytes(nb);
-  float2* tw = reinterpret_cast<float2*>(sm + 2 * stage_bytes);
-  int* fs = reinterpret_cast<int*>(tw + W);
-  uint64_t* bars = reinterpret_cast<uint64_t*>((reinterpret_cast<uintptr_t>(fs + 128) + 15) & ~(uintptr_t)15);
-  uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 2);
+  uint64_t* full = reinterpret_cast<uint64_t*>(sm + nst * stage_bytes);  // B copies + A stores landed
+  uint64_t* empty = full + kTcMaxStages;                                  // MMAs of a stage done
+  uint64_t* accb = empty + kTcMaxStages;                                  // every MMA done (one phase)
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(accb + 1);
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int R = d.C * Hi;
-  const int r0 = blockIdx.x * kTcRows;
+  const int T = blockIdx.x, ybase = T * yb;
   const int KS = gridDim.y, ks = blockIdx.y;
-  const int K = 2 * W;
-  const int nchT = (K + 31) >> 5;
-  const int jb = ks * nchT / KS, je = (ks + 1) * nchT / KS;
-  const float invW = 1.0f / (float)W;
+  const int nchT = (2 * W + 31) >> 5;
+  const int jb = ks * nchT / KS, je = (ks + 1) * nchT / KS, nch = je - jb;
 
   if (tid == 0) {
-    tc::mbar_init(&bars[0], 1);
-    tc::mbar_init(&bars[1], 1);
+    for (int i = 0; i < nst; ++i) {
+      tc::mbar_init(&full[i], 1 + kTcFwdStagers / 32);
+      tc::mbar_init(&empty[i], 1);
+    }
+    tc::mbar_init(accb, 1);
     tc::fence_mbar_init();
   }
   if (warp == 0) tc::tmem_alloc(tslot, kTcTmemCols);
-  for (int i = tid; i < W; i += kTcThreads) tw[i] = d.twW[i];
-  for (int i = tid; i < nsl; i += kTcThreads) fs[i] = d.fwd_slot[s0 + i];
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t tmem = *tslot;
-  pdl_wait();  // ubar comes from the previous kernel; t1 may still be read by it
-  if (tick && blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && tid == 0) atomicAdd(tick, 1);
-
   const uint32_t base = tc::smem_addr(sm);
-  const uint32_t idesc = tc::idesc_tf32(kTcRows, nb);
-  int issued = 0;
-  bool good = true;
-  for (int j = jb; j < je; ++j) {
-    const int jl = j - jb, b = jl & 1;
-    const uint32_t a_hi = base + b * stage_bytes, a_lo = a_hi + kTcTileA;
-    const uint32_t b_hi = a_lo + kTcTileA, b_lo = b_hi + (uint32_t)nb * 128u;
-    bool ok = jl < 2 || tc::mbar_wait(&bars[b], ((jl >> 1) - 1) & 1);
-    const int x0 = 16 * j;
-    // A: rows (c, y) x 16 image columns (re, im) of ubar . sens_c; 8 threads cover one row's 128 bytes
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      const int it = tid + kTcThreads * i;
-      const int p = it & 7, row = it >> 3;
-      const int r = r0 + row, x = x0 + 2 * p;
-      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (r < R && x < W) {  // x even and W even: x + 1 < W
-        const int c = r / Hi, y = r - c * Hi;
-        v = *reinterpret_cast<const float4*>(ubar + (size_t)y * W + x);
-        if (SENS) v = tc_cmul2(v, *reinterpret_cast<const float4*>(d.sens + ((size_t)c * d.Hf + y + d.y0) * W + x));
+  const uint32_t bbytes = 2u * (uint32_t)nb * 128u;
+  const unsigned char* bsrc = btiles + ((size_t)blockIdx.z * nchT + jb) * 2 * nbmax * 128;
+
+  bool ok = true;
+  if (tid == 0) {  // DFT-factor tiles (constants, may start before the previous kernel ends)
+    for (int jl = 0; jl < nch && ok; ++jl) {
+      const int b = jl % nst;
+      if (jl >= nst) ok = tc::mbar_wait(&empty[b], ((jl / nst) - 1) & 1);
+      if (!ok) {
+        atomicCAS(err, 0, 0x1100 | jl);
+        break;
       }
-      float4 hi, lo;
-      tc::split4(v, hi, lo);
-      const uint32_t o = tc::sw128(row, p);
-      tc::st_shared4(a_hi + o, hi);
-      tc::st_shared4(a_lo + o, lo);
+      tc::mbar_arrive_expect_tx(&full[b], bbytes);
+      tc::bulk_g2s(base + b * stage_bytes + 2 * kTcTileA, bsrc + (size_t)jl * 2 * nbmax * 128, bbytes, &full[b]);
     }
-    // B: output columns (s, re/im) x the same 16 image columns, from the twiddles
-    const int nitems = (nb >> 1) * 8;
-    for (int it = tid; it < nitems; it += kTcThreads) {
-      const int p = it & 7, sl = it >> 3;
-      const int x = x0 + 2 * p;
-      float2 e0 = c2(0.f, 0.f), e1 = c2(0.f, 0.f);
-      if (sl < nsl && x < W) {
-        const int f = fs[sl];
-        int q = x + d.mxW;
-        if (q >= W) q -= W;
-        e0 = tw[tc_mod_mul(q, f, W, invW)];
-        if (++q == W) q = 0;
-        e1 = tw[tc_mod_mul(q, f, W, invW)];
-      }
-      float4 hi, lo;
-      tc::split4(make_float4(e0.x, -e0.y, e1.x, -e1.y), hi, lo);
-      uint32_t o = tc::sw128(2 * sl, p);
-      tc::st_shared4(b_hi + o, hi);
-      tc::st_shared4(b_lo + o, lo);
-      tc::split4(make_float4(e0.y, e0.x, e1.y, e1.x), hi, lo);
-      o = tc::sw128(2 * sl + 1, p);
-      tc::st_shared4(b_hi + o, hi);
-      tc::st_shared4(b_lo + o, lo);
-    }
-    tc::fence_async_smem();
-    if (!__syncthreads_and(ok)) {
-      good = false;
-      break;
-    }
-    if (tid == 0) tc_issue_chunk(tmem, a_hi, a_lo, b_hi, b_lo, min(4, (K - 32 * j + 7) >> 3), idesc, jl == 0, &bars[b]);
-    ++issued;
   }
-  bool done = issued > 0 && tc::mbar_wait(&bars[(issued - 1) & 1], ((issued - 1) >> 1) & 1);
-  done = __syncthreads_and(done) && good;
+  pdl_wait();  // every thread: ubar comes from the previous kernel; t1 may still be read by it
+  if (tick && blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && tid == 0) atomicAdd(tick, 1);
+  if (tid == 32) {
+    const uint32_t idesc = tc::idesc_tf32(kTcRows, nb);
+    for (int jl = 0; jl < nch && ok; ++jl) {
+      const int b = jl % nst;
+      ok = tc::mbar_wait(&full[b], (jl / nst) & 1);
+      if (!ok) {
+        atomicCAS(err, 0, 0x1200 | jl);
+        break;
+      }
+      const uint32_t a_hi = base + b * stage_bytes, a_lo = a_hi + kTcTileA;
+      const uint32_t b_hi = a_lo + kTcTileA, b_lo = b_hi + (uint32_t)nb * 128u;
+      tc_issue_chunk(tmem, a_hi, a_lo, b_hi, b_lo, min(4, (2 * W - 32 * (jb + jl) + 7) >> 3), idesc, jl == 0,
+                     &empty[b]);
+    }
+    tc::mma_commit(accb);
+    if (!tc::mbar_wait(accb, 0)) {
+      atomicCAS(err, 0, 0x1300);
+      ok = false;
+    }
+    tc::fence_before_sync();
+  } else if (warp >= 2) {
+    // data operand: tile row m = c yb + yl, 16-byte chunk p = image columns x0 + 2p, x0 + 2p + 1. Item
+    // it = ot + kTcFwdStagers k; the next chunk's ubar and coil-map values are loaded into registers
+    // before the wait for its stage, so that their latency overlaps the MMAs.
+    const int ot = tid - 64;
+    int im[kTcFwdItems];   // tile row of item k (or -1)
+    int ioff[kTcFwdItems];  // ubar offset y W + 2 p of item k (add the chunk's first column)
+    int isoff[kTcFwdItems];
+#pragma unroll
+    for (int k = 0; k < kTcFwdItems; ++k) {
+      const int it = ot + kTcFwdStagers * k;
+      const int p = it & 7, m = it >> 3;
+      const int c = m / yb, yl = m - c * yb, y = ybase + yl;
+      const bool valid = it < kTcRows * 8 && c < C && y < Hi;
+      im[k] = valid ? m : -1;
+      ioff[k] = y * W + 2 * p;
+      isoff[k] = (c * d.Hf + y + d.y0) * W + 2 * p;
+    }
+    float4 uv[kTcFwdItems], sv[kTcFwdItems];
+    auto load = [&](int jl) {
+      const int x0 = 16 * (jb + jl);
+#pragma unroll
+      for (int k = 0; k < kTcFwdItems; ++k) {
+        const int it = ot + kTcFwdStagers * k;
+        const int x = x0 + 2 * (it & 7);
+        uv[k] = sv[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (im[k] >= 0 && x < W) {  // x even and W even: x + 1 < W
+          uv[k] = *reinterpret_cast<const float4*>(ubar + (size_t)ioff[k] + x0);
+          if (SENS) sv[k] = *reinterpret_cast<const float4*>(d.sens + (size_t)isoff[k] + x0);
+        }
+      }
+    };
+    if (nch > 0) load(0);
+    for (int jl = 0; jl < nch && ok; ++jl) {
+      const int b = jl % nst;
+      float4 cur[kTcFwdItems];
+#pragma unroll
+      for (int k = 0; k < kTcFwdItems; ++k) cur[k] = SENS ? tc_cmul2(uv[k], sv[k]) : uv[k];
+      if (jl + 1 < nch) load(jl + 1);
+      if (jl >= nst) {  // one lane polls; the others wait in the warp barrier without taking issue slots
+        if (lane == 0) ok = tc::mbar_wait(&empty[b], ((jl / nst) - 1) & 1);
+        ok = __shfl_sync(0xffffffffu, ok, 0);
+      }
+      if (!ok) {
+        if (lane == 0) atomicCAS(err, 0, 0x1400 | jl);
+        break;
+      }
+      const uint32_t a_hi = base + b * stage_bytes, a_lo = a_hi + kTcTileA;
+#pragma unroll
+      for (int k = 0; k < kTcFwdItems; ++k) {
+        const int it = ot + kTcFwdStagers * k;
+        if (it < kTcRows * 8) {
+          float4 hi, lo;
+          tc::split4(cur[k], hi, lo);
+          const uint32_t o = tc::sw128(it >> 3, it & 7);
+          tc::st_shared4(a_hi + o, hi);
+          tc::st_shared4(a_lo + o, lo);
+        }
+      }
+      tc::fence_async_smem();
+      __syncwarp();
+      if (lane == 0) tc::mbar_arrive(&full[b]);  // one arrival per staging warp
+    }
+  }
+  const bool done = __syncthreads_and(ok);
   tc::fence_after_sync();
-  const int q = warp & 3, h = warp >> 2;
-  const int half = nb >> 1;  // a multiple of 8
-  const int row = 32 * q + lane, r = r0 + row;
-  const bool rv = r < R;
-  const uint32_t taddr = tmem + ((uint32_t)(32 * q) << 16);
-  if (KS == 1) {
-    if (done) {
-      const int c = rv ? r / Hi : 0, y = rv ? r - c * Hi : 0;
-      float2* out = t1 + ((size_t)c * ns + s0) * Hi + y;
-      for (int col = h * half; col < (h + 1) * half; col += 8) {
-        float v[8];
-        tc::tmem_ld8(taddr + (uint32_t)col, v);
+  // accumulator -> shared memory as complex values [sl][tile row] (a warp's rows are consecutive); the
+  // stage buffers are free
+  float2* dt = reinterpret_cast<float2*>(sm);
+  if (done) {
+    const int q = warp & 3, h = warp >> 2;
+    const int G8 = nb >> 3, gb = h * G8 / 4, ge = (h + 1) * G8 / 4;
+    const uint32_t taddr = tmem + ((uint32_t)(32 * q) << 16);
+    const int row = 32 * q + lane;
+    for (int g = gb; g < ge; ++g) {
+      float v[8];
+      tc::tmem_ld8(taddr + (uint32_t)(8 * g), v);
 #pragma unroll
-        for (int i = 0; i < 4; ++i) {
-          const int sl = (col >> 1) + i;
-          if (rv && sl < nsl) out[(size_t)sl * Hi] = c2(v[2 * i], v[2 * i + 1]);
-        }
-      }
+      for (int i = 0; i < 4; ++i) dt[(size_t)(4 * g + i) * kTcRows + row] = c2(v[2 * i], v[2 * i + 1]);
     }
-  } else {
-    // accumulator -> shared memory red[sl][row] (the stage buffers are free: every MMA has completed)
-    float2* red = reinterpret_cast<float2*>(sm);
-    if (done) {
-      for (int col = h * half; col < (h + 1) * half; col += 8) {
-        float v[8];
-        tc::tmem_ld8(taddr + (uint32_t)col, v);
-#pragma unroll
-        for (int i = 0; i < 4; ++i) red[((col >> 1) + i) * kTcRows + row] = c2(v[2 * i], v[2 * i + 1]);
-      }
-    }
-    cg::cluster_group cluster = cg::this_cluster();
-    const int anybad = __syncthreads_or(!done);
-    cluster.sync();  // every CTA's partial sums are in its shared memory (executed by all CTAs)
-    const int sb = ks * nsl / KS, se = (ks + 1) * nsl / KS;
-    if (!anybad) {
-      for (int i = tid; i < (se - sb) * kTcRows; i += kTcThreads) {
-        const int rr = i & (kTcRows - 1), sl = sb + (i >> 7);
-        float2 acc = c2(0.f, 0.f);
-        for (int qq = 0; qq < KS; ++qq) acc += cluster.map_shared_rank(red, qq)[sl * kTcRows + rr];  // rank order
-        const int rg = r0 + rr;
-        if (rg < R) {
-          const int c = rg / Hi, y = rg - c * Hi;
-          t1[((size_t)c * ns + s0 + sl) * Hi + y] = acc;
-        }
-      }
-    }
-    cluster.sync();  // keep this CTA's shared memory alive until the other CTAs have read it
   }
-  if (!done && tid == 0) atomicExch(err, 2);
+  cg::cluster_group cluster = cg::this_cluster();
+  const int anybad = __syncthreads_or(!done);
+  cluster.sync();  // every CTA's partial accumulator is in its shared memory (all CTAs reach this)
+  if (!anybad) {
+    // rank ks writes sampled columns [sb, se) of this s tile: items (c, s, yl), yl fastest, so that a
+    // warp's remote loads and t1 stores cover consecutive tile rows / image rows
+    const int sb = ks * nsl / KS, se = (ks + 1) * nsl / KS, nsr = se - sb, n = C * nsr * yb;
+    for (int i0 = tid; i0 < n; i0 += kTcFwdThreads * kTcFwdBatch) {
+      float2 acc[kTcFwdBatch];
+      int src[kTcFwdBatch], dst[kTcFwdBatch];
+#pragma unroll
+      for (int u = 0; u < kTcFwdBatch; ++u) {
+        const int i = i0 + u * kTcFwdThreads;
+        acc[u] = c2(0.f, 0.f);
+        dst[u] = -1;
+        src[u] = 0;
+        if (i < n) {
+          const int yl = i % yb, rest = i / yb, sl = sb + rest % nsr, c = rest / nsr;
+          if (ybase + yl < Hi) {
+            dst[u] = (c * ns + s0 + sl) * Hi + ybase + yl;
+            src[u] = sl * kTcRows + c * yb + yl;
+          }
+        }
+      }
+      for (int qq = 0; qq < KS; ++qq) {  // rank order
+        const float2* rem = cluster.map_shared_rank(dt, qq);
+#pragma unroll
+        for (int u = 0; u < kTcFwdBatch; ++u)
+          if (dst[u] >= 0) acc[u] += rem[src[u]];
+      }
+#pragma unroll
+      for (int u = 0; u < kTcFwdBatch; ++u)
+        if (dst[u] >= 0) t1[(size_t)dst[u]] = acc[u];
+    }
+  }
+  cluster.sync();  // keep this CTA's shared memory alive until the other CTAs have read it
+  if (!done && tid == 0) atomicCAS(err, 0, 0x1500);
   tc::fence_before_sync();
   __syncthreads();
   if (warp == 0) {

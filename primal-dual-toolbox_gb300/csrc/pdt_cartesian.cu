@@ -56,10 +56,7 @@ struct CartDev {
   const float2* twW;
   const float2* twH;
   FftPlan planW, planH;
-  // Solver rounds with tensor-core adjoint rows: the column kernels write their image-row output as
-  // TF32 hi/lo operand tiles (tca, tc_nch K chunks per 128-row tile) instead of t[c][s][yi].
-  float* tca;
-  int tc_nch, tc_yb;
+  int tc_yb;  // tensor-core row passes: image rows per 128-row tile (the tile holds them for every coil)
 };
 
 enum ColMode { COL_SOLVE = 0, COL_FWD_DENSE = 1, COL_ADJ_DENSE = 2, COL_ADJ_COMPACT = 3 };
@@ -227,6 +224,15 @@ size_t rows_smem(const CartDev& d, bool with_acc) {
 }
 size_t cols_smem(const CartDev& d) { return sizeof(float2) * ((size_t)d.Hf + 2 * (size_t)d.CB * d.ldH); }
 
+// v rounded to TF32 (10 explicit mantissa bits, ties away from zero): the host side of split_tf32
+float tc_host_tf32(float v) {
+  uint32_t u;
+  std::memcpy(&u, &v, 4);
+  u = (u + 0x1000u) & 0xFFFFE000u;
+  std::memcpy(&v, &u, 4);
+  return v;
+}
+
 int g_num_sms = 0;
 int g_max_smem = 0;
 void query_device() {
@@ -284,7 +290,7 @@ class CartesianOp : public OpImpl, public SolverHooks {
     std::ostringstream os;
     os << "W=" << dev_.W << " H=" << dev_.Hf << " C=" << dev_.C << " sampled_columns=" << dev_.ns;
     if (tune_.tcf)
-      os << " rows_fwd=tensor_dft(tf32x3,k_split=" << tune_.ks << ")";
+      os << " rows_fwd=tensor_dft(tf32x3,k_split=" << tune_.ks << ",stages=" << tc_fwd_stages() << ")";
     else if (frow_.ok())
       os << " rows_fwd=lane_fft(" << frow_.M << "x" << frow_.L << ",warps=" << kWpbChoices[tune_.wf] << ")";
     else
@@ -341,15 +347,12 @@ class CartesianOp : public OpImpl, public SolverHooks {
     float2* t = scratch_.as<float2>();
     launch_rows_fwd(ubar, t, tick, st);
     if (mk) mk->mark("cart_rows_fwd", st);
-    if (tune_.tca) {  // column output as tensor-core operand tiles, one K^H r plane per coil
-      launch_cols(COL_SOLVE, t, t, r, fc, nullptr, nullptr, sigma, lambda, st, tca_.as<float>());
-      if (mk) mk->mark("cart_cols_prox", st);
-      launch_tc_rows_adj(khr, st);
-    } else {
-      launch_cols(COL_SOLVE, t, t, r, fc, nullptr, nullptr, sigma, lambda, st);
-      if (mk) mk->mark("cart_cols_prox", st);
+    launch_cols(COL_SOLVE, t, t, r, fc, nullptr, nullptr, sigma, lambda, st);
+    if (mk) mk->mark("cart_cols_prox", st);
+    if (tune_.tca)
+      launch_tc_rows_adj(t, khr, st);  // the coil sum on chip: one K^H r plane
+    else
       launch_rows_adj(t, khr, G_, st);
-    }
     if (mk) mk->mark("cart_rows_adj", st);
   }
   void adjoint_compact(const float2* fc, float2* img, cudaStream_t st) override {
@@ -359,13 +362,11 @@ class CartesianOp : public OpImpl, public SolverHooks {
       return;
     }
     float2* t = scratch_.as<float2>();
-    if (tune_.tca) {
-      launch_cols(COL_ADJ_COMPACT, nullptr, t, nullptr, fc, nullptr, nullptr, 0.f, 0.f, st, tca_.as<float>());
-      launch_tc_rows_adj(img, st);
-      return;
-    }
     launch_cols(COL_ADJ_COMPACT, nullptr, t, nullptr, fc, nullptr, nullptr, 0.f, 0.f, st);
-    launch_rows_adj(t, img, 1, st);
+    if (tune_.tca)
+      launch_tc_rows_adj(t, img, st);
+    else
+      launch_rows_adj(t, img, 1, st);
   }
 
  protected:
@@ -403,13 +404,11 @@ class CartesianOp : public OpImpl, public SolverHooks {
       return;
     }
     float2* t = scratch_.as<float2>();
-    if (tune_.tca) {
-      launch_cols(COL_ADJ_DENSE, nullptr, t, nullptr, nullptr, src, nullptr, 0.f, 0.f, st, tca_.as<float>());
-      launch_tc_rows_adj(dst, st);
-      return;
-    }
     launch_cols(COL_ADJ_DENSE, nullptr, t, nullptr, nullptr, src, nullptr, 0.f, 0.f, st);
-    launch_rows_adj(t, dst, 1, st);
+    if (tune_.tca)
+      launch_tc_rows_adj(t, dst, st);
+    else
+      launch_rows_adj(t, dst, 1, st);
   }
   void invalidate() override { prepared_ = false; }
 
@@ -422,15 +421,58 @@ class CartesianOp : public OpImpl, public SolverHooks {
     int ks = 4, nr = 4;          // tensor-core forward K split (cluster size), adjoint N ranges
   };
 
-  int tc_row_tiles() const { return (dev_.C * dev_.Hi + kTcRows - 1) / kTcRows; }
   int tc_adj_nb(int nr) const { return std::min(kTcAdjMaxNB, ((2 * dev_.W + nr - 1) / nr + 15) & ~15); }
-
+  int tc_fwd_nb() const { return (2 * std::min(128, dev_.ns) + 15) & ~15; }
+  int tc_fwd_stages() const {
+    return std::min(kTcMaxStages,
+                    (int)(((size_t)g_max_smem - tc_fwd_smem(tc_fwd_nb(), 0)) / tc_stage_bytes(tc_fwd_nb())));
+  }
+  // The forward rows' DFT factor as TF32 hi/lo operand tiles in the layout tc_rows_fwd copies:
+  // [s tile][K chunk][hi rows | lo rows] (chunk stride 2 nbmax 128 bytes), row n = 2 sl + o (output s =
+  // 128 z + sl, re/im o), K element k = 2 (x - 16 j) + (re/im input), 128-byte swizzle; E'[x][s] =
+  // w^(q(x) f_s), values in double precision, then split.
+  void build_tc_fwd_tiles() {
+    if (tcf_built_) return;
+    const int W = dev_.W, ns = dev_.ns, nchT = (2 * W + 31) / 32, stiles = (ns + 127) / 128;
+    const int nbmax = tc_fwd_nb();
+    std::vector<float> h((size_t)stiles * nchT * 2 * nbmax * 32, 0.f);
+    const double two_pi = 6.283185307179586476925286766559;
+    for (int z = 0; z < stiles; ++z) {
+      const int nsl = std::min(128, ns - 128 * z), nb = (2 * nsl + 15) & ~15;
+      for (int j = 0; j < nchT; ++j) {
+        float* hi = &h[((size_t)z * nchT + j) * 2 * nbmax * 32];
+        float* lo = hi + (size_t)nb * 32;
+        for (int n = 0; n < 2 * nsl; ++n) {
+          const int s = 128 * z + (n >> 1), o = n & 1;
+          const int f = ((col_x_h_[s] - dev_.oxW) % W + W) % W;  // forward-FFT output slot of s
+          for (int k = 0; k < 32; ++k) {
+            const int x = 16 * j + (k >> 1), ri = k & 1;
+            if (x >= W) continue;
+            const int q = (x + dev_.mxW) % W;  // ifftshift slot of image column x
+            const double a = -two_pi * (double)(((long long)q * f) % W) / (double)W;
+            const float er = (float)std::cos(a), ei = (float)std::sin(a);  // w^(q f)
+            const float v = o == 0 ? (ri == 0 ? er : -ei) : (ri == 0 ? ei : er);
+            const int pos = n * 32 + (((k >> 2) ^ (n & 7)) << 2) + (k & 3);
+            hi[pos] = tc_host_tf32(v);
+            lo[pos] = tc_host_tf32(v - hi[pos]);
+          }
+        }
+      }
+    }
+    tcf_tiles_.ensure(h.size() * sizeof(float));
+    PDT_CUDA_CHECK(cudaMemcpy(tcf_tiles_.p, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice));
+    tcf_built_ = true;
+  }
   void launch_tc_rows_fwd(const float2* ubar, float2* t1, int* tick, cudaStream_t st) {
-    const int ks = tune_.ks, stiles = (dev_.ns + 127) / 128;
-    const int nb0 = (2 * std::min(128, dev_.ns) + 15) & ~15;
-    LaunchEx lx(dim3(tc_row_tiles(), ks, stiles), dim3(kTcThreads), tc_fwd_smem(dev_.W, nb0), st, ks > 1 ? ks : 0);
+    const int ks = tune_.ks, stiles = (dev_.ns + 127) / 128, nst = tc_fwd_stages();
+    if (!tcf_built_) throw Error(PDT_ERR_STATE, name_ + ": tensor-core forward tiles not built");
+    CartDev dd = dev_;
+    dd.tc_yb = tc_adj_yb();
+    LaunchEx lx(dim3(tc_adj_tiles(), ks, stiles), dim3(kTcFwdThreads), tc_fwd_smem(tc_fwd_nb(), nst), st,
+                ks > 1 ? ks : 0);
     auto fn = dev_.sens ? tc_rows_fwd<true> : tc_rows_fwd<false>;
-    PDT_CUDA_CHECK(cudaLaunchKernelEx(&lx.cfg, fn, dev_, ubar, t1, tick, tc_err()));
+    PDT_CUDA_CHECK(cudaLaunchKernelEx(&lx.cfg, fn, dd, ubar, (const unsigned char*)tcf_tiles_.p, t1, tick, nst,
+                                      tc_err()));
     count_launch();
   }
   int tc_adj_chunks() const { return (2 * dev_.ns + 31) / 32; }
@@ -447,13 +489,6 @@ class CartesianOp : public OpImpl, public SolverHooks {
     if (tcb_nb_ == NB) return;
     const int W = dev_.W, ns = dev_.ns, nch = tc_adj_chunks(), nranges = (2 * W + NB - 1) / NB;
     std::vector<float> h((size_t)nranges * nch * 2 * NB * 32, 0.f);
-    auto rna = [](float v) {  // round to TF32 (10 mantissa bits), ties away from zero
-      uint32_t u;
-      std::memcpy(&u, &v, 4);
-      u = (u + 0x1000u) & 0xFFFFE000u;
-      std::memcpy(&v, &u, 4);
-      return v;
-    };
     const double two_pi = 6.283185307179586476925286766559;
     for (int i = 0; i < nranges; ++i) {
       const int n0 = i * NB, nb = std::min(NB, (2 * W - n0 + 15) & ~15);
@@ -472,8 +507,8 @@ class CartesianOp : public OpImpl, public SolverHooks {
             const float er = (float)std::cos(a), ei = (float)std::sin(a);  // exp(+i a) = conj(w^(p q))
             const float v = o == 0 ? (ri == 0 ? er : -ei) : (ri == 0 ? ei : er);
             const int pos = n * 32 + (((k >> 2) ^ (n & 7)) << 2) + (k & 3);
-            hi[pos] = rna(v);
-            lo[pos] = rna(v - hi[pos]);
+            hi[pos] = tc_host_tf32(v);
+            lo[pos] = tc_host_tf32(v - hi[pos]);
           }
         }
       }
@@ -482,7 +517,7 @@ class CartesianOp : public OpImpl, public SolverHooks {
     PDT_CUDA_CHECK(cudaMemcpy(tcb_.p, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice));
     tcb_nb_ = NB;
   }
-  void launch_tc_rows_adj(float2* planes, cudaStream_t st) {
+  void launch_tc_rows_adj(const float2* t2, float2* out, cudaStream_t st) {
     const int NB = tc_adj_nb(tune_.nr);
     if (tcb_nb_ != NB) throw Error(PDT_ERR_STATE, name_ + ": tensor-core adjoint tiles not built for this range size");
     const int nst = tc_adj_stages(NB);
@@ -490,8 +525,7 @@ class CartesianOp : public OpImpl, public SolverHooks {
     dd.tc_yb = tc_adj_yb();
     LaunchEx lx(dim3((2 * dev_.W + NB - 1) / NB, tc_adj_tiles()), dim3(kTcAdjThreads), tc_adj_smem(NB, nst), st);
     auto fn = dev_.sens ? tc_rows_adj<true> : tc_rows_adj<false>;
-    PDT_CUDA_CHECK(cudaLaunchKernelEx(&lx.cfg, fn, dd, (const float*)tca_.as<float>(),
-                                      (const unsigned char*)tcb_.p, planes, NB, nst, tc_err()));
+    PDT_CUDA_CHECK(cudaLaunchKernelEx(&lx.cfg, fn, dd, t2, (const unsigned char*)tcb_.p, out, NB, nst, tc_err()));
     count_launch();
   }
   int* tc_err() { return reinterpret_cast<int*>(tc_err_.p); }
@@ -523,20 +557,13 @@ class CartesianOp : public OpImpl, public SolverHooks {
     PDT_LAUNCH_CHECK();
     count_launch();
   }
-  // `tiles`: COL_SOLVE writes its image-row output as the tensor-core adjoint's operand tiles
   void launch_cols(int mode, const float2* tin, float2* tout, float2* r, const float2* fc, const float2* kin,
-                   float2* kout, float sigma, float lambda, cudaStream_t st, float* tiles = nullptr) {
+                   float2* kout, float sigma, float lambda, cudaStream_t st) {
     if (fcol_.ok()) {
       const int wpb = kWpbChoices[tune_.wc];
       const int S = fcol_.cols_per_block(wpb);
-      CartDev dd = dev_;
-      if (tiles) {
-        dd.tca = tiles;
-        dd.tc_nch = tc_adj_chunks();
-        dd.tc_yb = tc_adj_yb();
-      }
       LaunchEx lx(dim3((dev_.ns + S - 1) / S, dev_.C), dim3(32 * wpb), fast_cols_smem(fcol_, wpb), st);
-      PDT_CUDA_CHECK(cudaLaunchKernelEx(&lx.cfg, fcol_.cols[tune_.wc], dd, mode, tin, tout, r, fc, kin, kout, sigma,
+      PDT_CUDA_CHECK(cudaLaunchKernelEx(&lx.cfg, fcol_.cols[tune_.wc], dev_, mode, tin, tout, r, fc, kin, kout, sigma,
                                         lambda));
       count_launch();
       return;
@@ -618,11 +645,11 @@ class CartesianOp : public OpImpl, public SolverHooks {
     frow_ = find_row_kernels(W);
     fcol_ = find_col_kernels(Hf);
     if (frow_.ok() && fast_rows_adj_smem(d, frow_, 8) > (size_t)g_max_smem) frow_ = FastRowKernels();
-    // tensor-core DFT rows: even W (16-byte row vectors); the forward's twiddle table and index products
-    // are sized for W <= kTcMaxW; the adjoint's operand tiles come from the lane-FFT column kernels
+    // tensor-core DFT rows: even W (16-byte row vectors), at most 128 coils (a row tile holds one image row
+    // of every coil)
     const bool tc_any = W % 2 == 0 && d.ns > 0 && std::getenv("PDT_NO_TENSOR_ROWS") == nullptr;
-    tcf_ok_ = tc_any && W <= kTcMaxW && tc_fwd_smem(W, 256) <= (size_t)g_max_smem;
-    tca_ok_ = tc_any && fcol_.ok() && C <= kTcRows && tc_adj_smem(kTcAdjMaxNB, 2) <= (size_t)g_max_smem;
+    tcf_ok_ = tc_any && C <= kTcRows && tc_fwd_smem(256, 2) <= (size_t)g_max_smem;
+    tca_ok_ = tc_any && C <= kTcRows && tc_adj_smem(kTcAdjMaxNB, 2) <= (size_t)g_max_smem;
     if (fcol_.ok() && fast_cols_smem(fcol_, 8) > (size_t)g_max_smem) fcol_ = FastColKernels();
     // compact position P -> output row: P = k1 L + t holds spectrum index k1 + M brev_L(t), which the
     // fftshift puts on row (k + Hf/2) mod Hf
@@ -688,6 +715,7 @@ class CartesianOp : public OpImpl, public SolverHooks {
     }
     col_x_h_ = col_x;
     tcb_nb_ = 0;
+    tcf_built_ = false;
     if (tcf_ok_ || tca_ok_) {
       for (auto fn : {tc_rows_fwd<true>, tc_rows_fwd<false>})
         PDT_CUDA_CHECK(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, g_max_smem));
@@ -695,12 +723,6 @@ class CartesianOp : public OpImpl, public SolverHooks {
         PDT_CUDA_CHECK(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, g_max_smem));
       tc_err_.ensure(sizeof(int));
       PDT_CUDA_CHECK(cudaMemset(tc_err_.p, 0, sizeof(int)));
-    }
-    if (tca_ok_) {  // operand tiles; entries past the last row or sampled column stay zero
-      const int yb = kTcRows / C;
-      const size_t bytes = (size_t)((d.Hi + yb - 1) / yb) * ((2 * d.ns + 31) / 32) * 2 * kTcTileA;
-      tca_.ensure(bytes);
-      PDT_CUDA_CHECK(cudaMemset(tca_.p, 0, bytes));
     }
     tune_ = Tune();
     const int row_blocks = (d.Hi + d.RB - 1) / d.RB;
@@ -728,6 +750,7 @@ class CartesianOp : public OpImpl, public SolverHooks {
         tune_ = it->second.first;
         G_ = it->second.second;
         if (tune_.tca) build_tc_adj_tiles(tc_adj_nb(tune_.nr));
+        if (tune_.tcf) build_tc_fwd_tiles();
         return;
       }
     }
@@ -794,8 +817,9 @@ class CartesianOp : public OpImpl, public SolverHooks {
       bt = time([&] { launch_rows_fwd(ub.as<float2>(), t, nullptr, st); });
     }
     if (tcf_ok_) {  // tensor-core forward rows: K splits (cluster sizes)
+      build_tc_fwd_tiles();
       const int nchT = (2 * dev_.W + 31) / 32;
-      for (int ks : {1, 2, 3, 4, 6, 8}) {
+      for (int ks : {2, 3, 4}) {
         if (ks > nchT) continue;
         tune_.tcf = 1;
         tune_.ks = ks;
@@ -816,22 +840,15 @@ class CartesianOp : public OpImpl, public SolverHooks {
       tune_.wc = best.wc;
     }
     if (tca_ok_) {
-      // the column pass and the adjoint rows together: FFT rows (tuned above) against the tensor-core rows
-      // fed by the column kernel's operand tiles, for a few output-column range counts
+      // the adjoint rows: FFT rows (tuned above, with their coil-group partial images) against the
+      // tensor-core rows (coil sum on chip), for a few output-column range counts
       tune_.wa = best.wa;
       tune_.cluster = best.cluster;
-      float pair = time([&] {
-        launch_cols(COL_SOLVE, t, t, rr.as<float2>(), ff.as<float2>(), nullptr, nullptr, 0.125f, 1.f, st);
-        launch_rows_adj(t, kh.as<float2>(), G_, st);
-      });
+      float pair = time([&] { launch_rows_adj(t, kh.as<float2>(), G_, st); });
       for (int nr : {2, 3, 4, 5, 6, 8}) {
         tune_.nr = nr;
         build_tc_adj_tiles(tc_adj_nb(nr));
-        const float ms = time([&] {
-          launch_cols(COL_SOLVE, t, t, rr.as<float2>(), ff.as<float2>(), nullptr, nullptr, 0.125f, 1.f, st,
-                      tca_.as<float>());
-          launch_tc_rows_adj(kh.as<float2>(), st);
-        });
+        const float ms = time([&] { launch_tc_rows_adj(t, kh.as<float2>(), st); });
         if (ms < pair) pair = ms, best.tca = 1, best.nr = nr;
       }
     }
@@ -844,6 +861,7 @@ class CartesianOp : public OpImpl, public SolverHooks {
     cudaEventDestroy(e1);
     tune_ = best;
     if (tune_.tca) build_tc_adj_tiles(tc_adj_nb(tune_.nr));
+    if (tune_.tcf) build_tc_fwd_tiles();
     std::lock_guard<std::mutex> lock(g_tune_mu);
     g_tune_cache[key] = {tune_, G_};
   }
@@ -882,6 +900,7 @@ class CartesianOp : public OpImpl, public SolverHooks {
       tune_.nr = v[8];
     }
     if (tune_.tca) build_tc_adj_tiles(tc_adj_nb(tune_.nr));
+    if (tune_.tcf) build_tc_fwd_tiles();
     return true;
   }
 
@@ -892,9 +911,10 @@ class CartesianOp : public OpImpl, public SolverHooks {
   FastColKernels fcol_;
   bool tcf_ok_ = false, tca_ok_ = false;
   std::vector<int> col_x_h_;
-  int tcb_nb_ = 0;  // range size the adjoint DFT tiles in tcb_ were built for
+  int tcb_nb_ = 0;         // range size the adjoint DFT tiles in tcb_ were built for
+  bool tcf_built_ = false;  // forward DFT tiles in tcf_tiles_
   int G_ = 1;
-  DevBuf tables_, scratch_, tc_err_, tca_, tcb_;
+  DevBuf tables_, scratch_, tc_err_, tcb_, tcf_tiles_;
 };
 
 std::shared_ptr<OpImpl> make_cartesian_operator(pdt_op_kind kind) { return std::make_shared<CartesianOp>(kind); }
