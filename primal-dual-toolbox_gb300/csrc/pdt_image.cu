@@ -19,6 +19,7 @@
 //   over-relaxation theta = 1: bar = 2 new - old.
 #include "pdt_device.cuh"
 #include "pdt_internal.h"
+#include "pdt_primal.cuh"
 
 namespace pdt {
 namespace {
@@ -326,11 +327,6 @@ __global__ void __launch_bounds__(NT) mri_dual_kernel(int W, int H, ImgPtrs in, 
   }
 }
 
-// div- of a component at (x, y) along x (dir 0) or y (dir 1) with the reference's boundary rows.
-__device__ __forceinline__ float2 bdiff(const float2* __restrict__ f, size_t idx, int pos, int n, size_t step) {
-  return (pos > 0) ? ((pos < n - 1) ? f[idx] - f[idx - step] : -f[idx - step]) : f[idx];
-}
-
 template <bool TGV>
 __global__ void __launch_bounds__(NT) mri_primal_kernel(int W, int H, ImgPtrs out, const float2* __restrict__ khr,
                                                         int G, long long gstride, float tau, int* __restrict__ iter) {
@@ -339,34 +335,9 @@ __global__ void __launch_bounds__(NT) mri_primal_kernel(int W, int H, ImgPtrs ou
   const int x = blockIdx.x * TX + threadIdx.x % TX, y = blockIdx.y * TY + threadIdx.x / TX;
   if (x >= W || y >= H) return;
   const size_t idx = (size_t)y * W + x;
-  const float2* px = static_cast<const float2*>(out.px);
-  const float2* py = static_cast<const float2*>(out.py);
   float2 kh = khr[idx];
   for (int g = 1; g < G; ++g) kh += khr[idx + (size_t)g * gstride];
-  float2* u = static_cast<float2*>(out.u);
-  const float2 ou = u[idx];
-  // TGV_primal_u_noprox_kernel (tgv_kernels.cuh:432-467)
-  const float2 d = bdiff(px, idx, x, W, 1) + bdiff(py, idx, y, H, (size_t)W);
-  const float2 un = ou + tau * (d - kh);
-  u[idx] = un;
-  static_cast<float2*>(out.ub)[idx] = 2.0f * un - ou;
-  if constexpr (TGV) {
-    // TGV_primal_v_kernel (tgv_kernels.cuh:647-686)
-    const float2* qxx = static_cast<const float2*>(out.qxx);
-    const float2* qyy = static_cast<const float2*>(out.qyy);
-    const float2* qxy = static_cast<const float2*>(out.qxy);
-    float2* vx = static_cast<float2*>(out.vx);
-    float2* vy = static_cast<float2*>(out.vy);
-    const float2 ovx = vx[idx], ovy = vy[idx];
-    const float2 dqxx = bdiff(qxx, idx, x, W, 1), dqyy = bdiff(qyy, idx, y, H, (size_t)W);
-    const float2 dqxyx = bdiff(qxy, idx, x, W, 1), dqxyy = bdiff(qxy, idx, y, H, (size_t)W);
-    const float2 vxn = ovx + tau * ((dqxx + dqxyy) + px[idx]);
-    const float2 vyn = ovy + tau * ((dqyy + dqxyx) + py[idx]);
-    vx[idx] = vxn;
-    vy[idx] = vyn;
-    static_cast<float2*>(out.vbx)[idx] = 2.0f * vxn - ovx;
-    static_cast<float2*>(out.vby)[idx] = 2.0f * vyn - ovy;
-  }
+  mri_primal_pixel<TGV>(W, H, out, x, y, kh, tau);
 }
 
 __global__ void tick_kernel(int* tick) { atomicAdd(tick, 1); }
