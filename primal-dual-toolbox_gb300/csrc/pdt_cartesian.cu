@@ -233,6 +233,14 @@ float tc_host_tf32(float v) {
   return v;
 }
 
+// cos (which = 0) or sin (which = 1) of 2 pi m / n for m < n, in double precision
+std::vector<double> host_roots(int n, int which) {
+  const double two_pi = 6.283185307179586476925286766559;
+  std::vector<double> r(n);
+  for (int m = 0; m < n; ++m) r[m] = which ? std::sin(two_pi * m / n) : std::cos(two_pi * m / n);
+  return r;
+}
+
 int g_num_sms = 0;
 int g_max_smem = 0;
 void query_device() {
@@ -436,7 +444,7 @@ class CartesianOp : public OpImpl, public SolverHooks {
     const int W = dev_.W, ns = dev_.ns, nchT = (2 * W + 31) / 32, stiles = (ns + 127) / 128;
     const int nbmax = tc_fwd_nb();
     std::vector<float> h((size_t)stiles * nchT * 2 * nbmax * 32, 0.f);
-    const double two_pi = 6.283185307179586476925286766559;
+    const std::vector<double> wc = host_roots(W, 0), ws = host_roots(W, 1);  // cos, sin of 2 pi m / W
     for (int z = 0; z < stiles; ++z) {
       const int nsl = std::min(128, ns - 128 * z), nb = (2 * nsl + 15) & ~15;
       for (int j = 0; j < nchT; ++j) {
@@ -449,8 +457,8 @@ class CartesianOp : public OpImpl, public SolverHooks {
             const int x = 16 * j + (k >> 1), ri = k & 1;
             if (x >= W) continue;
             const int q = (x + dev_.mxW) % W;  // ifftshift slot of image column x
-            const double a = -two_pi * (double)(((long long)q * f) % W) / (double)W;
-            const float er = (float)std::cos(a), ei = (float)std::sin(a);  // w^(q f)
+            const int m = (int)(((long long)q * f) % W);
+            const float er = (float)wc[m], ei = -(float)ws[m];  // w^(q f) = exp(-2 pi i m / W)
             const float v = o == 0 ? (ri == 0 ? er : -ei) : (ri == 0 ? ei : er);
             const int pos = n * 32 + (((k >> 2) ^ (n & 7)) << 2) + (k & 3);
             hi[pos] = tc_host_tf32(v);
@@ -489,7 +497,7 @@ class CartesianOp : public OpImpl, public SolverHooks {
     if (tcb_nb_ == NB) return;
     const int W = dev_.W, ns = dev_.ns, nch = tc_adj_chunks(), nranges = (2 * W + NB - 1) / NB;
     std::vector<float> h((size_t)nranges * nch * 2 * NB * 32, 0.f);
-    const double two_pi = 6.283185307179586476925286766559;
+    const std::vector<double> wc = host_roots(W, 0), ws = host_roots(W, 1);  // cos, sin of 2 pi m / W
     for (int i = 0; i < nranges; ++i) {
       const int n0 = i * NB, nb = std::min(NB, (2 * W - n0 + 15) & ~15);
       for (int j = 0; j < nch; ++j) {
@@ -503,8 +511,8 @@ class CartesianOp : public OpImpl, public SolverHooks {
             const int s = 16 * j + (k >> 1), ri = k & 1;
             if (s >= ns) continue;
             const int p = (col_x_h_[s] + dev_.mxW) % W;
-            const double a = two_pi * (double)(((long long)p * q) % W) / (double)W;
-            const float er = (float)std::cos(a), ei = (float)std::sin(a);  // exp(+i a) = conj(w^(p q))
+            const int m = (int)(((long long)p * q) % W);
+            const float er = (float)wc[m], ei = (float)ws[m];  // exp(+2 pi i m / W) = conj(w^(p q))
             const float v = o == 0 ? (ri == 0 ? er : -ei) : (ri == 0 ? ei : er);
             const int pos = n * 32 + (((k >> 2) ^ (n & 7)) << 2) + (k & 3);
             hi[pos] = tc_host_tf32(v);
