@@ -21,6 +21,7 @@
 
 #include "pdt_device.cuh"
 #include "pdt_internal.h"
+#include "pdt_tc.cuh"
 
 namespace pdt {
 namespace {
@@ -51,6 +52,137 @@ enum Epi {
   EPI_RELU_RES = 2,  // zsave = z, out = in + relu(z)   (CIN == COUT)
   EPI_F32 = 3        // out32 = z (FP32)
 };
+
+// 32 -> 32 channel 3 x 3 convolution on the fifth-generation tensor cores (tcgen05 kind::f16, BF16
+// operands, FP32 accumulator in tensor memory), as an implicit GEMM without an im2col copy. One CTA computes
+// a tile of 8 x 16 pixels (x, y) = the 128 rows of one MMA tile, rows ordered y-major. The input tile with
+// its one-pixel zero halo (10 x 18 pixels) sits in shared memory in the no-swizzle K-major layout: channel
+// group g (8 channels, 16 bytes) of pixel p at byte g 2880 + 16 p, so eight consecutive pixels form a core
+// matrix; the 8-pixel groups of the M tile are one halo row (160 bytes) apart, and tap (ky, kx) is the
+// same layout started 16 (10 ky + kx) bytes in. The weights sit the same way ([tap][g][co] x 16 bytes).
+// K = (tap, channel) = 288 in 18 MMAs of K = 16 (two channel groups), N = 32 output channels. One thread
+// issues the MMAs and commits them to an mbarrier; the epilogue reads pixel rows from tensor memory
+// (warps q and q + 4 share lane quarter q, 16 output channels each).
+constexpr int kConvTcThreads = 256;
+constexpr int kConvTcTW = 8, kConvTcTH = 16;                      // tile: 8 pixels wide, 16 rows
+constexpr int kConvTcHaloPix = (kConvTcTW + 2) * (kConvTcTH + 2);  // 180
+constexpr uint32_t kConvTcGroup = 16 * kConvTcHaloPix;             // 2880: one channel group of the tile
+constexpr uint32_t kConvTcIn = 4 * kConvTcGroup;                   // 11,520 bytes
+constexpr uint32_t kConvTcW = NTAP * 4 * 32 * 16;                   // 18,432 bytes
+// the allocation also covers reads with the two descriptor strides exchanged (2880 x 15 + 160 x 1 + 128
+// past a tap start below 11,520 + 18,432), so no operand read can leave it
+constexpr size_t kConvTcSmem = 1024 + 65536 + 64;
+
+// Persistent: a CTA loads the weights once and walks tiles t = blockIdx.x, + gridDim.x, ... of the
+// (x tiles) x (y tiles) x B grid; the completion barrier's phase alternates per tile.
+template <int EPI>
+__global__ void __launch_bounds__(kConvTcThreads) conv3x3_tc(const bf16* __restrict__ in, const bf16* __restrict__ w,
+                                                            const float* __restrict__ bias, int B, int H, int W,
+                                                            bf16* __restrict__ out, bf16* __restrict__ zsave,
+                                                            int* __restrict__ err) {
+  static_assert(EPI == EPI_LINEAR || EPI == EPI_RELU_RES, "epilogues of the 32 -> 32 layers");
+  extern __shared__ unsigned char conv_smem_raw[];
+  const uint32_t off = tc::smem_addr(conv_smem_raw);
+  unsigned char* sm = conv_smem_raw + ((1024u - (off & 1023u)) & 1023u);
+  const uint32_t in_base = tc::smem_addr(sm), w_base = in_base + kConvTcIn;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(sm + 65536);
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(bar + 1);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int ntx = (W + kConvTcTW - 1) / kConvTcTW, nty = (H + kConvTcTH - 1) / kConvTcTH;
+  const int ntiles = ntx * nty * B;
+  if (tid == 0) {
+    tc::mbar_init(bar, 1);
+    tc::fence_mbar_init();
+  }
+  if (warp == 0) tc::tmem_alloc(tslot, 32);
+  // weights: item (tap, group, co) at byte ((tap 4 + g) 32 + co) 16
+  for (int i = tid; i < NTAP * 4 * 32; i += kConvTcThreads) {
+    const int co = i & 31, g = (i >> 5) & 3, tap = i >> 7;
+    const uint4 v = __ldg(reinterpret_cast<const uint4*>(w + ((size_t)tap * CH + co) * CH) + g);
+    asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(w_base + 16 * i), "r"(v.x), "r"(v.y), "r"(v.z),
+                 "r"(v.w)
+                 : "memory");
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = *tslot;
+  const int q = warp & 3, h = warp >> 2;
+  bool ok = true;
+  int it = 0;
+  for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x, ++it) {
+    const int bx = t % ntx, by = (t / ntx) % nty, b = t / (ntx * nty);
+    const int x0 = bx * kConvTcTW, y0 = by * kConvTcTH;
+    const bf16* inb = in + (size_t)b * H * W * CH;
+    // input tile with halo: item (pixel, channel group), 16 bytes each (the previous tile's MMAs are done)
+    for (int i = tid; i < kConvTcHaloPix * 4; i += kConvTcThreads) {
+      const int g = i & 3, pix = i >> 2;
+      const int hy = pix / (kConvTcTW + 2), hx = pix - hy * (kConvTcTW + 2);
+      const int gy = y0 + hy - 1, gx = x0 + hx - 1;
+      uint4 v = make_uint4(0u, 0u, 0u, 0u);
+      if (gy >= 0 && gy < H && gx >= 0 && gx < W)
+        v = __ldg(reinterpret_cast<const uint4*>(inb + ((size_t)gy * W + gx) * CH) + g);
+      asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(in_base + g * kConvTcGroup + 16 * pix), "r"(v.x),
+                   "r"(v.y), "r"(v.z), "r"(v.w)
+                   : "memory");
+    }
+    tc::fence_async_smem();
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    if (tid == 0) {
+      const uint32_t idesc = tc::idesc_bf16(128, CH);
+      for (int tap = 0; tap < NTAP; ++tap) {
+        const uint32_t a0 = in_base + 16 * ((tap / 3) * (kConvTcTW + 2) + tap % 3);
+        for (int k = 0; k < 2; ++k)  // channel groups 2k, 2k + 1
+          tc::mma_bf16(tmem, tc::desc_interleave(a0 + 2 * k * kConvTcGroup, kConvTcGroup, 16 * (kConvTcTW + 2)),
+                       tc::desc_interleave(w_base + (tap * 4 + 2 * k) * 512, 512, 128), idesc, (tap | k) ? 1u : 0u);
+      }
+      tc::mma_commit(bar);
+    }
+    ok = tc::mbar_wait(bar, it & 1);  // every thread waits each phase in turn
+    tc::fence_after_sync();
+    float v[16];
+    tc::tmem_ld16(tmem + ((uint32_t)(32 * q) << 16) + 16 * h, v);
+    const int m = 32 * q + lane, gy = y0 + (m >> 3), gx = x0 + (m & 7);  // row m = pixel (m % 8, m / 8)
+    if (ok && gy < H && gx < W) {
+      const size_t pix = ((size_t)b * H + gy) * W + gx;
+      uint32_t o[8], zz[8];
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        const int co = 16 * h + 2 * j;
+        float z0 = v[2 * j], z1 = v[2 * j + 1];
+        if (bias) {
+          z0 += bias[co];
+          z1 += bias[co + 1];
+        }
+        if constexpr (EPI == EPI_LINEAR) {
+          o[j] = pack_bf16(z0, z1);
+        } else {
+          zz[j] = pack_bf16(z0, z1);
+          const __nv_bfloat162 hv = reinterpret_cast<const __nv_bfloat162*>(in + pix * CH)[co / 2];
+          o[j] = pack_bf16(__bfloat162float(hv.x) + fmaxf(z0, 0.f), __bfloat162float(hv.y) + fmaxf(z1, 0.f));
+        }
+      }
+      uint4* op = reinterpret_cast<uint4*>(out + pix * CH + 16 * h);
+      op[0] = make_uint4(o[0], o[1], o[2], o[3]);
+      op[1] = make_uint4(o[4], o[5], o[6], o[7]);
+      if constexpr (EPI == EPI_RELU_RES) {
+        uint4* zp = reinterpret_cast<uint4*>(zsave + pix * CH + 16 * h);
+        zp[0] = make_uint4(zz[0], zz[1], zz[2], zz[3]);
+        zp[1] = make_uint4(zz[4], zz[5], zz[6], zz[7]);
+      }
+    }
+    ok = __syncthreads_and(ok);  // the tile buffer and the accumulator are free for the next tile
+  }
+  if (!ok && tid == 0) atomicExch(err, 0x2000);
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) {
+    tc::fence_after_sync();
+    tc::tmem_dealloc(tmem, 32);
+  }
+}
 
 // 3 x 3 convolution as an implicit GEMM. in: [B][H][W][CIN] BF16; w: [9][COUT][CIN] BF16; bias: [COUT] FP32
 // (may be null). Each block computes a 16 x 8 pixel tile; warp w owns tile row w (16 pixels = one M tile).
@@ -480,6 +612,24 @@ class WarmStartCnn {
       init_param(W_[l], w, l >= 1);
       init_param(B_[l], std::vector<float>(nb[l], 0.f), false);
     }
+    for (auto fn : {conv3x3_tc<EPI_LINEAR>, conv3x3_tc<EPI_RELU_RES>})
+      PDT_CUDA_CHECK(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kConvTcSmem));
+    err_.ensure(sizeof(int));
+    PDT_CUDA_CHECK(cudaMemset(err_.p, 0, sizeof(int)));
+    int dev = 0;
+    PDT_CUDA_CHECK(cudaGetDevice(&dev));
+    PDT_CUDA_CHECK(cudaDeviceGetAttribute(&sms_, cudaDevAttrMultiProcessorCount, dev));
+  }
+
+  // Raises (and clears) the error word of the tensor-core convolutions: set when an MMA completion wait
+  // gave up, after which that launch's output is not valid.
+  void check_error() {
+    int e = 0;
+    PDT_CUDA_CHECK(cudaMemcpy(&e, err_.p, sizeof(int), cudaMemcpyDeviceToHost));
+    if (e) {
+      PDT_CUDA_CHECK(cudaMemset(err_.p, 0, sizeof(int)));
+      throw Error(PDT_ERR_TIMEOUT, "warm-start network: a tensor-core convolution gave up waiting for its MMAs");
+    }
   }
 
   // Parameters as one flat FP32 vector (weights then biases per layer) for saving / loading.
@@ -522,10 +672,11 @@ class WarmStartCnn {
     PDT_LAUNCH_CHECK();
     count_launch(2);
     const dim3 grid((W + TW - 1) / TW, (H + TH - 1) / TH, B);
+    const int tgrid = conv_tc_grid(B, H, W);
     for (int l = 1; l <= 6; ++l) {
-      conv3x3_mma<CH, CH, EPI_RELU_RES><<<grid, 32 * TH, 0, st>>>(h_[l - 1].as<bf16>(), W_[l].wb.as<bf16>(),
-                                                                  B_[l].w.as<float>(), H, W, h_[l].as<bf16>(),
-                                                                  z_[l].as<bf16>(), nullptr);
+      conv3x3_tc<EPI_RELU_RES><<<tgrid, kConvTcThreads, kConvTcSmem, st>>>(h_[l - 1].as<bf16>(), W_[l].wb.as<bf16>(),
+                                                                         B_[l].w.as<float>(), B, H, W, h_[l].as<bf16>(),
+                                                                         z_[l].as<bf16>(), err_.as<int>());
       PDT_LAUNCH_CHECK();
       count_launch();
     }
@@ -545,6 +696,7 @@ class WarmStartCnn {
     PDT_LAUNCH_CHECK();
     count_launch();
     const dim3 grid((W + TW - 1) / TW, (H + TH - 1) / TH, B);
+    const int tgrid = conv_tc_grid(B, H, W);
     // conv_out: dW, db, and dh6 = conv(go, W7') (8 -> 32 channels, padded to 16 input channels)
     wgrad(8, h_[6].as<bf16>(), go_.as<bf16>(), B, H, W, W_[7].g.as<float>(), st);
     bias_grad<<<8, 256, 0, st>>>(go_.as<bf16>(), npix, 8, B_[7].g.as<float>());
@@ -569,8 +721,8 @@ class WarmStartCnn {
       wgrad(CH, h_[l - 1].as<bf16>(), gz_.as<bf16>(), B, H, W, W_[l].g.as<float>(), st);
       bias_grad<<<CH, 256, 0, st>>>(gz_.as<bf16>(), npix, CH, B_[l].g.as<float>());
       flip_transpose<<<64, 256, 0, st>>>(W_[l].wb.as<bf16>(), CH, CH, CH, CH, wt_.as<bf16>());
-      conv3x3_mma<CH, CH, EPI_LINEAR><<<grid, 32 * TH, 0, st>>>(gz_.as<bf16>(), wt_.as<bf16>(), nullptr, H, W,
-                                                                gtmp_.as<bf16>(), nullptr, nullptr);
+      conv3x3_tc<EPI_LINEAR><<<tgrid, kConvTcThreads, kConvTcSmem, st>>>(gz_.as<bf16>(), wt_.as<bf16>(), nullptr, B, H, W,
+                                                                       gtmp_.as<bf16>(), nullptr, err_.as<int>());
       add_into<<<grid_for(npix * CH), 256, 0, st>>>(gacc_.as<float>(), gtmp_.as<bf16>(), npix * CH);
       PDT_LAUNCH_CHECK();
       count_launch(6);
@@ -585,6 +737,7 @@ class WarmStartCnn {
     std::vector<double> h(lb);
     PDT_CUDA_CHECK(cudaMemcpyAsync(h.data(), part_.p, sizeof(double) * lb, cudaMemcpyDeviceToHost, st));
     PDT_CUDA_CHECK(cudaStreamSynchronize(st));
+    check_error();
     double loss = 0;
     for (double v : h) loss += v;
     return loss / (double)npix;
@@ -658,6 +811,11 @@ class WarmStartCnn {
       refresh_bf16(p, 0);
     }
   }
+  // persistent tensor-core convolutions: three CTAs per SM (66 KB of shared memory each), at most one tile each
+  int conv_tc_grid(int B, int H, int W) const {
+    const long long tiles = (long long)((W + kConvTcTW - 1) / kConvTcTW) * ((H + kConvTcTH - 1) / kConvTcTH) * B;
+    return (int)std::min<long long>(tiles, 3LL * sms_);
+  }
   void refresh_bf16(CnnParam& p, cudaStream_t st) {
     to_bf16<<<grid_for(p.n), 256, 0, st>>>(p.w.as<float>(), p.n, p.wb.as<bf16>());
     PDT_LAUNCH_CHECK();
@@ -707,7 +865,8 @@ class WarmStartCnn {
   }
 
   CnnParam W_[kLayers], B_[kLayers];
-  DevBuf x_, h_[7], z_[7], o_, go_, go16_, gtmp_, gbf_, gz_, gacc_, wt_, wpart_, part_, t_, sc_;
+  DevBuf x_, h_[7], z_[7], o_, go_, go16_, gtmp_, gbf_, gz_, gacc_, wt_, wpart_, part_, t_, sc_, err_;
+  int sms_ = 1;
   int B_n_ = 0, H_n_ = 0, W_n_ = 0;
   long step_ = 0;
 };
@@ -815,7 +974,10 @@ pdt_status pdt_cnn_predict(pdt_cnn* c, const void* u0, int B, int H, int W, void
     n.forward(static_cast<const float2*>(u0), n.inv_scale_ptr(B), B, H, W, st);
     n.assemble(static_cast<const float2*>(u0), n.scale_ptr(), B, np, static_cast<float2*>(u), static_cast<float2*>(v),
                st);
-    if (!stream) PDT_CUDA_CHECK(cudaStreamSynchronize(st));
+    if (!stream) {
+      PDT_CUDA_CHECK(cudaStreamSynchronize(st));
+      n.check_error();
+    }
   });
 }
 

@@ -34,6 +34,14 @@ __device__ __forceinline__ uint64_t desc_sw128(uint32_t saddr) {
          ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
 }
 
+// Shared-memory matrix descriptor, no swizzle, K-major: core matrices of 8 rows x 16 bytes stored
+// contiguously (row r at byte 16 r); `kstride` bytes between core matrices adjacent along K (leading byte
+// offset), `mnstride` bytes between core matrices adjacent along M / N (stride byte offset).
+__device__ __forceinline__ uint64_t desc_interleave(uint32_t saddr, uint32_t kstride, uint32_t mnstride) {
+  return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)((kstride >> 4) & 0x3FFFu) << 16) |
+         ((uint64_t)((mnstride >> 4) & 0x3FFFu) << 32) | ((uint64_t)1 << 46);
+}
+
 // Instruction descriptor of kind::tf32: FP32 accumulator (bits 4-5 = 1), A and B TF32 (bits 7-9 and
 // 10-12 = 2), both K-major (bits 15, 16 = 0), N >> 3 in bits 17-22, M >> 4 in bits 24-28.
 __host__ __device__ constexpr uint32_t idesc_tf32(int M, int N) {
@@ -46,6 +54,20 @@ __device__ __forceinline__ void mma_tf32(uint32_t d_tmem, uint64_t adesc, uint64
   asm volatile(
       "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
       "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate));
+}
+
+// Instruction descriptor of kind::f16 with BF16 A and B (bits 7-9, 10-12 = 1) and an FP32 accumulator.
+__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+// D[tmem] (+)= A * B^T for one K = 16 step of BF16 operands; issued by a single thread.
+__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                         uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
       "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate));
 }
 
