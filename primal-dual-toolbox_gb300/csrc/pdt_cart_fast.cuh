@@ -177,7 +177,10 @@ __global__ void __launch_bounds__(32 * WPB) fl_cols(CartDev d, int mode, const f
 // Phase 2 over two warps per column (n = M * 64): the same steps as fl_cols with LaneFft64, for column
 // lengths whose 32-lane split would hold many values per lane; WPB / 2 columns per block. The compact
 // order is position k1 * 64 + t for spectrum index k1 + M brev_64(t).
-template <int M, int WPB>
+// ZM: register slots j (bit j) that are known at compile time to hold only rows outside the image, for
+// every lane: their forward-transform inputs are zero and their inverse-transform outputs are not
+// stored, so the register DFTs fold them away (the host selects it when the geometry matches).
+template <int M, int WPB, int ZM = 0>
 __global__ void __launch_bounds__(32 * WPB) fl_cols64(CartDev d, int mode, const float2* t_in, float2* t_out,
                                                       float2* __restrict__ r, const float2* __restrict__ fc,
                                                       const float2* __restrict__ kin, float2* __restrict__ kout,
@@ -205,6 +208,10 @@ __global__ void __launch_bounds__(32 * WPB) fl_cols64(CartDev d, int mode, const
   if (mode == COL_SOLVE || mode == COL_FWD_DENSE) {
 #pragma unroll
     for (int j = 0; j < M; ++j) {
+      if ((ZM >> j) & 1) {
+        v[j] = c2(0.f, 0.f);
+        continue;
+      }
       int yf = t + L * j - d.mxH;
       if (yf < 0) yf += Hf;
       const int yi = yf - d.y0;
@@ -261,6 +268,7 @@ __global__ void __launch_bounds__(32 * WPB) fl_cols64(CartDev d, int mode, const
   if (ok) {
 #pragma unroll
     for (int j = 0; j < M; ++j) {
+      if ((ZM >> j) & 1) continue;
       int yf = t + L * j + d.oyH;
       if (yf >= Hf) yf -= Hf;
       const int yi = yf - d.y0;
@@ -388,7 +396,8 @@ struct FastRowKernels {
 };
 struct FastColKernels {
   FrColsFn cols[3] = {nullptr, nullptr, nullptr};
-  int M = 0, L = 0;
+  FrColsFn cols_z[3] = {nullptr, nullptr, nullptr};  // specialisation for the zero-slot mask zmask
+  int M = 0, L = 0, zmask = 0;
   bool ok() const { return cols[0] != nullptr; }
   int cols_per_block(int wpb) const { return L == 64 ? wpb / 2 : wpb * (32 / L); }
 };
@@ -434,6 +443,12 @@ FastColKernels col_kernels64() {
   k.cols[0] = fl_cols64<M, 2>;
   k.cols[1] = fl_cols64<M, 4>;
   k.cols[2] = fl_cols64<M, 8>;
+  if constexpr (M == 10) {  // 640 rows with readout-oversampling removal: slots 3..6 lie outside the image
+    k.cols_z[0] = fl_cols64<M, 2, 0x78>;
+    k.cols_z[1] = fl_cols64<M, 4, 0x78>;
+    k.cols_z[2] = fl_cols64<M, 8, 0x78>;
+    k.zmask = 0x78;
+  }
   k.M = M;
   k.L = 64;
   return k;

@@ -313,7 +313,8 @@ class CartesianOp : public OpImpl, public SolverHooks {
     else
       os << " rows_adj=stockham(coil_groups=" << G_ << ")";
     if (fcol_.ok())
-      os << " cols=lane_fft(" << fcol_.M << "x" << fcol_.L << ",warps=" << kWpbChoices[tune_.wc] << ")";
+      os << " cols=lane_fft(" << fcol_.M << "x" << fcol_.L << ",warps=" << kWpbChoices[tune_.wc]
+         << (colz_ ? ",image_rows_only" : "") << ")";
     else
       os << " cols=stockham";
     return os.str();
@@ -571,8 +572,8 @@ class CartesianOp : public OpImpl, public SolverHooks {
       const int wpb = kWpbChoices[tune_.wc];
       const int S = fcol_.cols_per_block(wpb);
       LaunchEx lx(dim3((dev_.ns + S - 1) / S, dev_.C), dim3(32 * wpb), fast_cols_smem(fcol_, wpb), st);
-      PDT_CUDA_CHECK(cudaLaunchKernelEx(&lx.cfg, fcol_.cols[tune_.wc], dev_, mode, tin, tout, r, fc, kin, kout, sigma,
-                                        lambda));
+      const FrColsFn fn = colz_ ? fcol_.cols_z[tune_.wc] : fcol_.cols[tune_.wc];
+      PDT_CUDA_CHECK(cudaLaunchKernelEx(&lx.cfg, fn, dev_, mode, tin, tout, r, fc, kin, kout, sigma, lambda));
       count_launch();
       return;
     }
@@ -659,6 +660,21 @@ class CartesianOp : public OpImpl, public SolverHooks {
     tcf_ok_ = tc_any && C <= kTcRows && tc_fwd_smem(256, 2) <= (size_t)g_max_smem;
     tca_ok_ = tc_any && C <= kTcRows && tc_adj_smem(kTcAdjMaxNB, 2) <= (size_t)g_max_smem;
     if (fcol_.ok() && fast_cols_smem(fcol_, 8) > (size_t)g_max_smem) fcol_ = FastColKernels();
+    // register slots of the 64-lane column kernel that hold only rows outside the image for every lane
+    // (forward input zero, inverse output unused): the specialised kernel folds them away
+    colz_ = false;
+    if (fcol_.ok() && fcol_.zmask && fcol_.L == 64) {
+      int zm = 0;
+      for (int j = 0; j < fcol_.M; ++j) {
+        bool outside = true;
+        for (int t = 0; t < 64 && outside; ++t) {
+          const int yin = ((t + 64 * j - d.mxH) % Hf + Hf) % Hf - d.y0, yout = (t + 64 * j + d.oyH) % Hf - d.y0;
+          outside = (yin < 0 || yin >= d.Hi) && (yout < 0 || yout >= d.Hi);
+        }
+        if (outside) zm |= 1 << j;
+      }
+      colz_ = (zm & fcol_.zmask) == fcol_.zmask;  // every slot the specialisation skips is outside
+    }
     // compact position P -> output row: P = k1 L + t holds spectrum index k1 + M brev_L(t), which the
     // fftshift puts on row (k + Hf/2) mod Hf
     std::vector<int> kperm(Hf);
@@ -720,6 +736,8 @@ class CartesianOp : public OpImpl, public SolverHooks {
       }
       if (fcol_.ok())
         PDT_CUDA_CHECK(cudaFuncSetAttribute(fcol_.cols[w], cudaFuncAttributeMaxDynamicSharedMemorySize, g_max_smem));
+      if (fcol_.ok() && fcol_.cols_z[w])
+        PDT_CUDA_CHECK(cudaFuncSetAttribute(fcol_.cols_z[w], cudaFuncAttributeMaxDynamicSharedMemorySize, g_max_smem));
     }
     col_x_h_ = col_x;
     tcb_nb_ = 0;
@@ -918,6 +936,7 @@ class CartesianOp : public OpImpl, public SolverHooks {
   FastRowKernels frow_;
   FastColKernels fcol_;
   bool tcf_ok_ = false, tca_ok_ = false;
+  bool colz_ = false;  // the column kernel's zero-slot specialisation applies
   std::vector<int> col_x_h_;
   int tcb_nb_ = 0;         // range size the adjoint DFT tiles in tcb_ were built for
   bool tcf_built_ = false;  // forward DFT tiles in tcf_tiles_
