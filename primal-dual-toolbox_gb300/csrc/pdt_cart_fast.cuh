@@ -428,7 +428,7 @@ FastColKernels col_kernels() {
 
 // Lengths with a compiled split n = M * L.
 #define PDT_FAST_SIZES(X) X(32, 4, 8) X(48, 6, 8) X(64, 8, 8) X(96, 6, 16) X(128, 8, 16) X(192, 12, 16) \
-  X(256, 16, 16) X(320, 10, 32) X(368, 23, 16) X(384, 12, 32) X(512, 16, 32) X(640, 20, 32) X(768, 24, 32)
+  X(256, 16, 16) X(320, 10, 32) X(368, 46, 8) X(384, 12, 32) X(512, 16, 32) X(640, 20, 32) X(768, 24, 32)
 
 FastRowKernels find_row_kernels(int n) {
 #define PDT_ROWCASE(N, M, L) \
