@@ -18,6 +18,8 @@
 //                tiles precomputed per operator; the threads stage the data operand from t2. A row tile
 //                holds a few image rows of every coil, and each CTA writes the coil sum
 //                sum_c conj(sens_c) . g_c of its rows and output columns (coil order: deterministic).
+//                Rows of blocks past the row tiles, when the launch has them, run the solver's dual
+//                update on the SMs the row tiles leave free.
 //   tc_rows_fwd  grid (row tiles, KS, s tiles), clusters of (1, KS, 1). The DFT factor arrives by bulk
 //                copy, the threads form the data operand (ubar . sens_c, split); the KS CTAs of a cluster
 //                take disjoint K (x) ranges and reduce their accumulators through distributed shared
@@ -26,6 +28,7 @@
 
 #include <cooperative_groups.h>
 
+#include "pdt_primal.cuh"
 #include "pdt_tc.cuh"
 
 namespace pdt {
@@ -88,7 +91,18 @@ template <bool SENS>
 __global__ void __launch_bounds__(kTcAdjThreads, 1) tc_rows_adj(CartDev d, const float2* __restrict__ t2,
                                                              const unsigned char* __restrict__ btiles,
                                                              float2* __restrict__ out, int NB, int nst,
-                                                             int* __restrict__ err) {
+                                                             int* __restrict__ err, int ntiles, DualStep ds) {
+  if ((int)blockIdx.y >= ntiles) {
+    // rows of blocks past the row tiles run the solver's dual update (no TMEM, no barriers); its inputs
+    // come from before the previous launch, its outputs are read only after this launch completes
+    pdl_wait();
+    const int db = (blockIdx.y - ntiles) * gridDim.x + blockIdx.x, nd = (gridDim.y - ntiles) * gridDim.x;
+    if (ds.tgv)
+      mri_dual_blocks<true>(ds, db, nd);
+    else
+      mri_dual_blocks<false>(ds, db, nd);
+    return;
+  }
   extern __shared__ unsigned char tc_smem_raw[];
   unsigned char* sm = tc_align1024(tc_smem_raw);
   const int W = d.W, ns = d.ns, Hi = d.Hi, C = d.C, yb = d.tc_yb;

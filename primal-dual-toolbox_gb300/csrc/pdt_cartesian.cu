@@ -317,6 +317,9 @@ class CartesianOp : public OpImpl, public SolverHooks {
          << (colz_ ? ",image_rows_only" : "") << ")";
     else
       os << " cols=stockham";
+    if (tune_.tca && dev_.ns > 0 && fuse_dual_ && dual_rows() > 0)
+      os << " solver_dual=adjoint_launch(" << dual_rows() * ((2 * dev_.W + tc_adj_nb(tune_.nr) - 1) / tc_adj_nb(tune_.nr))
+         << "_blocks)";
     return os.str();
   }
   Dims natural_input_size() override {
@@ -345,9 +348,23 @@ class CartesianOp : public OpImpl, public SolverHooks {
     return (frow_.ok() && tune_.cluster) ? 1 : G_;  // a cluster reduces its coil groups on chip
   }
   long long group_stride() override { return (long long)dev_.Hi * dev_.W; }
-  void round(const float2* ubar, float2* r, const float2* fc, float sigma, float lambda, float2* khr, int* tick,
-             cudaStream_t st, PhaseMarker* mk) override {
+  // The dual update rides in the tensor-core adjoint launch when its row tiles leave at least
+  // kMinDualBlocks SMs free (one CTA per SM), one row of dual blocks per N range.
+  static constexpr int kMinDualBlocks = 8;
+  int dual_rows() {
+    const int gx = (2 * dev_.W + tc_adj_nb(tune_.nr) - 1) / tc_adj_nb(tune_.nr);
+    const int idle = g_num_sms - gx * tc_adj_tiles();
+    return idle >= kMinDualBlocks ? idle / gx : 0;
+  }
+  bool can_fuse_dual(int W, int H) override {
     prepare();
+    return tune_.tca && dev_.ns > 0 && fuse_dual_ && W == dev_.W && H == dev_.Hi && dual_rows() > 0;
+  }
+  void round(const float2* ubar, float2* r, const float2* fc, float sigma, float lambda, float2* khr, int* tick,
+             cudaStream_t st, PhaseMarker* mk, const DualStep* dual) override {
+    prepare();
+    if (dual && !can_fuse_dual(dual->W, dual->H))
+      throw Error(PDT_ERR_STATE, name_ + ": round() given a dual update it cannot run");
     if (dev_.ns == 0) {
       launch_fill_zero(khr, sizeof(float2) * (size_t)G_ * dev_.Hi * dev_.W, st);
       if (tick) launch_tick(tick, st);
@@ -359,7 +376,7 @@ class CartesianOp : public OpImpl, public SolverHooks {
     launch_cols(COL_SOLVE, t, t, r, fc, nullptr, nullptr, sigma, lambda, st);
     if (mk) mk->mark("cart_cols_prox", st);
     if (tune_.tca)
-      launch_tc_rows_adj(t, khr, st);  // the coil sum on chip: one K^H r plane
+      launch_tc_rows_adj(t, khr, st, dual);  // the coil sum on chip: one K^H r plane
     else
       launch_rows_adj(t, khr, G_, st);
     if (mk) mk->mark("cart_rows_adj", st);
@@ -526,15 +543,19 @@ class CartesianOp : public OpImpl, public SolverHooks {
     PDT_CUDA_CHECK(cudaMemcpy(tcb_.p, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice));
     tcb_nb_ = NB;
   }
-  void launch_tc_rows_adj(const float2* t2, float2* out, cudaStream_t st) {
+  void launch_tc_rows_adj(const float2* t2, float2* out, cudaStream_t st, const DualStep* dual = nullptr) {
     const int NB = tc_adj_nb(tune_.nr);
     if (tcb_nb_ != NB) throw Error(PDT_ERR_STATE, name_ + ": tensor-core adjoint tiles not built for this range size");
     const int nst = tc_adj_stages(NB);
     CartDev dd = dev_;
     dd.tc_yb = tc_adj_yb();
-    LaunchEx lx(dim3((2 * dev_.W + NB - 1) / NB, tc_adj_tiles()), dim3(kTcAdjThreads), tc_adj_smem(NB, nst), st);
+    const int ntiles = tc_adj_tiles();
+    const DualStep ds = dual ? *dual : DualStep{};
+    LaunchEx lx(dim3((2 * dev_.W + NB - 1) / NB, ntiles + (dual ? dual_rows() : 0)), dim3(kTcAdjThreads),
+                tc_adj_smem(NB, nst), st);
     auto fn = dev_.sens ? tc_rows_adj<true> : tc_rows_adj<false>;
-    PDT_CUDA_CHECK(cudaLaunchKernelEx(&lx.cfg, fn, dd, t2, (const unsigned char*)tcb_.p, out, NB, nst, tc_err()));
+    PDT_CUDA_CHECK(cudaLaunchKernelEx(&lx.cfg, fn, dd, t2, (const unsigned char*)tcb_.p, out, NB, nst, tc_err(),
+                                      ntiles, ds));
     count_launch();
   }
   int* tc_err() { return reinterpret_cast<int*>(tc_err_.p); }
@@ -659,6 +680,7 @@ class CartesianOp : public OpImpl, public SolverHooks {
     const bool tc_any = W % 2 == 0 && d.ns > 0 && std::getenv("PDT_NO_TENSOR_ROWS") == nullptr;
     tcf_ok_ = tc_any && C <= kTcRows && tc_fwd_smem(256, 2) <= (size_t)g_max_smem;
     tca_ok_ = tc_any && C <= kTcRows && tc_adj_smem(kTcAdjMaxNB, 2) <= (size_t)g_max_smem;
+    fuse_dual_ = std::getenv("PDT_NO_FUSED_DUAL") == nullptr;
     if (fcol_.ok() && fast_cols_smem(fcol_, 8) > (size_t)g_max_smem) fcol_ = FastColKernels();
     // register slots of the 64-lane column kernel that hold only rows outside the image for every lane
     // (forward input zero, inverse output unused): the specialised kernel folds them away
@@ -936,6 +958,7 @@ class CartesianOp : public OpImpl, public SolverHooks {
   FastRowKernels frow_;
   FastColKernels fcol_;
   bool tcf_ok_ = false, tca_ok_ = false;
+  bool fuse_dual_ = true;  // PDT_NO_FUSED_DUAL: the solvers' dual update always in its own kernel
   bool colz_ = false;  // the column kernel's zero-slot specialisation applies
   std::vector<int> col_x_h_;
   int tcb_nb_ = 0;         // range size the adjoint DFT tiles in tcb_ were built for

@@ -281,50 +281,9 @@ __global__ void __launch_bounds__(NT) mri_dual_kernel(int W, int H, ImgPtrs in, 
                                                       const int* __restrict__ iter) {
   const int x = blockIdx.x * TX + threadIdx.x % TX, y = blockIdx.y * TY + threadIdx.x / TX;
   if (x >= W || y >= H) return;
-  const size_t idx = (size_t)y * W + x;
-  const bool xn = x < W - 1, yn = y < H - 1;
-  const float2* ub = static_cast<const float2*>(in.ub);
-  float alpha0 = 1.f, alpha1 = 1.f;
-  if constexpr (TGV) {
-    const int k = min(max(iter[0], 0), iter[1] - 1);
-    alpha0 = alpha_tab[2 * k];
-    alpha1 = alpha_tab[2 * k + 1];
-  }
-  const float2 c = ub[idx];
-  const float2 ux = xn ? ub[idx + 1] : c, uy = yn ? ub[idx + W] : c;
-  const float2 pxo = static_cast<const float2*>(in.px)[idx], pyo = static_cast<const float2*>(in.py)[idx];
-  float2 a, b;
-  float2 vx, vy, vxx, vxy, vyx, vyy;
-  if constexpr (TGV) {
-    const float2* vbx = static_cast<const float2*>(in.vbx);
-    const float2* vby = static_cast<const float2*>(in.vby);
-    vx = vbx[idx];
-    vy = vby[idx];
-    vxx = xn ? vbx[idx + 1] : vx;
-    vxy = yn ? vbx[idx + W] : vx;
-    vyx = xn ? vby[idx + 1] : vy;
-    vyy = yn ? vby[idx + W] : vy;
-    a = pxo + sigma * ((ux - c) - vx);
-    b = pyo + sigma * ((uy - c) - vy);
-  } else {
-    a = pxo + sigma * (ux - c);
-    b = pyo + sigma * (uy - c);
-  }
-  const float sp = proj_scale(sqrtf(abs2(a) + abs2(b)), alpha1);
-  static_cast<float2*>(out.px)[idx] = a * sp;
-  static_cast<float2*>(out.py)[idx] = b * sp;
-  if constexpr (TGV) {
-    const float2 gxx = vxx - vx;
-    const float2 gxy = 0.5f * (vxy - vx + vyx - vy);
-    const float2 gyy = vyy - vy;
-    const float2 qa = static_cast<const float2*>(in.qxx)[idx] + sigma * gxx;
-    const float2 qb = static_cast<const float2*>(in.qyy)[idx] + sigma * gyy;
-    const float2 qc = static_cast<const float2*>(in.qxy)[idx] + sigma * gxy;
-    const float sq = proj_scale(sqrtf(abs2(qa) + abs2(qb) + 2.0f * abs2(qc)), alpha0);
-    static_cast<float2*>(out.qxx)[idx] = qa * sq;
-    static_cast<float2*>(out.qyy)[idx] = qb * sq;
-    static_cast<float2*>(out.qxy)[idx] = qc * sq;
-  }
+  float alpha0, alpha1;
+  dual_alphas<TGV>(alpha_tab, iter, alpha0, alpha1);
+  mri_dual_pixel<TGV>(W, H, in, out, sigma, alpha0, alpha1, x, y);
 }
 
 template <bool TGV>

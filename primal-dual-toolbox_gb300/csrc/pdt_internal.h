@@ -73,6 +73,18 @@ struct ImgPtrs {
   void *u, *ub, *vx, *vy, *vbx, *vby, *px, *py, *qxx, *qyy, *qxy;
 };
 
+// One dual update of the with-operator solvers (p, q ascent and projections, state `in` -> `out`, the
+// TGV weights from alpha_tab at the iteration counter iter[0]) handed to an operator round that runs it
+// in otherwise idle blocks of one of its launches (SolverHooks::can_fuse_dual).
+struct DualStep {
+  ImgPtrs in, out;
+  float sigma;
+  const float* alpha_tab;
+  const int* iter;
+  int W, H;
+  int tgv;  // 1: TGV (p and q), 0: TV (p only)
+};
+
 // Fused TvOptimizer iteration (tgv_kernels.cuh:294-324 then 568-605): reads u, u-bar and p from `in`,
 // writes them to `out`.
 void launch_tv_step(bool complex_, int W, int H, const ImgPtrs& in, const ImgPtrs& out, const void* f, float tau,

@@ -37,8 +37,12 @@ struct SolverHooks {
   // khr receives `groups()` partial sums spaced `group_stride()` elements apart.
   // `tick`, when non-null, is incremented once by the round's first kernel (the solvers' device-side
   // iteration counter).
+  // `dual`, when non-null, is a dual update the round runs inside one of its launches, after that
+  // launch's programmatic wait (only where can_fuse_dual says so).
   virtual void round(const float2* ubar, float2* r, const float2* fc, float sigma, float lambda, float2* khr,
-                     int* tick, cudaStream_t st, PhaseMarker* mk = nullptr) = 0;
+                     int* tick, cudaStream_t st, PhaseMarker* mk = nullptr, const DualStep* dual = nullptr) = 0;
+  // Whether round() can run a W x H dual update in blocks its launches leave idle.
+  virtual bool can_fuse_dual(int W, int H) { return false; }
   virtual int groups() = 0;
   virtual long long group_stride() = 0;
   // img <- K^H f from the compact layout (the solver's initial u0 = A^T f).

@@ -382,7 +382,7 @@ class RadialOp : public OpImpl, public SolverHooks {
   }
   long long group_stride() override { return (long long)dev_.N * dev_.N; }
   void round(const float2* ubar, float2* r, const float2* fc, float sigma, float lambda, float2* khr, int* tick,
-             cudaStream_t st, PhaseMarker* mk) override {
+             cudaStream_t st, PhaseMarker* mk, const DualStep*) override {
     prepare();
     if (tick) launch_tick(tick, st);
     forward_grid(ubar, st, mk);
