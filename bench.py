@@ -530,7 +530,7 @@ def run_batched(pdt, torch, n_cases, iters, steps, warmup):
                                                 mp_context=multiprocessing.get_context("spawn")) as pool:
         cases = list(pool.map(warmstart._case, specs, chunksize=1))
     t_gen = time.perf_counter() - t0
-    opts, ops, nbytes, pix = [], [], 0, 0
+    opts, ops, nbytes, pix, adj_rows = [], [], 0, 0, {}
     for spec, case in zip(specs, cases):
         op = pdt.mri.MriCartesianOperator()
         op.setCoilSens(case["sens"])
@@ -542,7 +542,10 @@ def run_batched(pdt, torch, n_cases, iters, steps, warmup):
         opt.setOperator(op)
         opt.setNoisyData(case["rawdata"])
         ns = int((case["mask"] != 0).any(axis=0).sum())
-        G = _khr_planes(op.tuning())
+        tuning = op.tuning()
+        G = _khr_planes(tuning)
+        adj = "tensor_dft" if "rows_adj=tensor_dft" in tuning else "lane_fft"
+        adj_rows[adj] = adj_rows.get(adj, 0) + 1
         nbytes += sum(_phase_bytes_case(spec["C"], spec["H"], spec["W"], ns, G, False).values())
         pix += spec["H"] * spec["W"]
         opts.append(opt)
@@ -570,7 +573,7 @@ def run_batched(pdt, torch, n_cases, iters, steps, warmup):
             "roofline": {"bound": "hbm", "kernel": "whole iteration (all phases)", "achieved": round(achieved, 1),
                          "peak": hbm, "peak_source": src, "unit": "GB/s", "frac": round(achieved / hbm, 4),
                          "algorithmic_bytes_per_iteration_all_cases": int(nbytes)},
-            "case_generation_s": round(t_gen, 1)}
+            "adjoint_rows_chosen": adj_rows, "case_generation_s": round(t_gen, 1)}
 
 
 RAD_N, RAD_C, RAD_SPOKES, RAD_RO, RAD_OSF, RAD_KW = 256, 12, 64, 512, 1.5, 3

@@ -447,6 +447,11 @@ class OptImpl {
     finish(p);
   }
   const OpImpl* op_ptr() const { return op_.get(); }
+  // Tells the operator that its rounds launch beside other problems' kernels (SolverHooks::set_concurrent).
+  void set_concurrent(bool on) {
+    if (op_)
+      if (SolverHooks* hk = op_->hooks()) hk->set_concurrent(on);
+  }
 
   Dims result_size() const {
     if (!has_state_) throw Error(PDT_ERR_STATE, "There is no result yet!");
@@ -852,6 +857,16 @@ class BatchImpl {
 
   void solve(bool verbose, cudaStream_t st) {
     if (opts_.empty()) return;
+    // every round of the batch runs beside the other problems' launches
+    struct Concurrent {
+      std::vector<OptImpl*>& opts;
+      explicit Concurrent(std::vector<OptImpl*>& o) : opts(o) {
+        for (OptImpl* q : opts) q->set_concurrent(true);
+      }
+      ~Concurrent() {
+        for (OptImpl* q : opts) q->set_concurrent(false);
+      }
+    } concurrent(opts_);
     std::vector<OptImpl::Plan> plans;
     plans.reserve(opts_.size());
     for (OptImpl* o : opts_) plans.push_back(o->plan(verbose, st));

@@ -437,6 +437,20 @@ FastRowKernels find_row_kernels(int n) {
 #undef PDT_ROWCASE
   return FastRowKernels();
 }
+
+// Row splits for launches that share the SMs with other problems' kernels (batched solves): the 46
+// values per lane of 368 = 46 x 8 hold about 200 registers, one 256-thread block per SM, which is fastest
+// alone but crowds out the concurrent kernels; 23 x 16 needs about 70. Twiddles and slot maps are indexed
+// by the natural spectrum index, so both splits read and write the same arrays from the same tables.
+#define PDT_CONCURRENT_ROW_SIZES(X) X(368, 23, 16)
+
+FastRowKernels find_concurrent_row_kernels(int n) {
+#define PDT_ROWCASE(N, M, L) \
+  if (n == N) return row_kernels<M, L>();
+  PDT_CONCURRENT_ROW_SIZES(PDT_ROWCASE)
+#undef PDT_ROWCASE
+  return FastRowKernels();
+}
 template <int M>
 FastColKernels col_kernels64() {
   FastColKernels k;

@@ -300,7 +300,11 @@ class CartesianOp : public OpImpl, public SolverHooks {
     if (tune_.tcf)
       os << " rows_fwd=tensor_dft(tf32x3,k_split=" << tune_.ks << ",stages=" << tc_fwd_stages() << ")";
     else if (frow_.ok())
-      os << " rows_fwd=lane_fft(" << frow_.M << "x" << frow_.L << ",warps=" << kWpbChoices[tune_.wf] << ")";
+      os << " rows_fwd=lane_fft(" << frow_.M << "x" << frow_.L << ",warps=" << kWpbChoices[tune_.wf]
+         << (frow_cc_.ok() ? ",batched:" + std::to_string(frow_cc_.M) + "x" + std::to_string(frow_cc_.L) +
+                                 ",warps=" + std::to_string(kWpbChoices[tune_.wfc])
+                           : std::string())
+         << ")";
     else
       os << " rows_fwd=stockham";
     if (tune_.tca)
@@ -356,6 +360,7 @@ class CartesianOp : public OpImpl, public SolverHooks {
     const int idle = g_num_sms - gx * tc_adj_tiles();
     return idle >= kMinDualBlocks ? idle / gx : 0;
   }
+  void set_concurrent(bool on) override { concurrent_ = on; }
   bool can_fuse_dual(int W, int H) override {
     prepare();
     return tune_.tca && dev_.ns > 0 && fuse_dual_ && W == dev_.W && H == dev_.Hi && dual_rows() > 0;
@@ -445,6 +450,7 @@ class CartesianOp : public OpImpl, public SolverHooks {
     bool cluster = false;        // coil groups of a row block reduced in a cluster (else partial images)
     int tcf = 0, tca = 0;        // 1: tensor-core DFT rows (forward / adjoint) instead of the FFT kernels
     int ks = 4, nr = 4;          // tensor-core forward K split (cluster size), adjoint N ranges
+    int wfc = 1;  // warps-per-block index of the concurrent forward-row split (4 warps; 2 and 4 measured alike)
   };
 
   int tc_adj_nb(int nr) const { return std::min(kTcAdjMaxNB, ((2 * dev_.W + nr - 1) / nr + 15) & ~15); }
@@ -575,10 +581,13 @@ class CartesianOp : public OpImpl, public SolverHooks {
       return;
     }
     if (frow_.ok()) {
-      const int wpb = kWpbChoices[tune_.wf];
-      const int R = frow_.rows_per_block(wpb);
-      LaunchEx lx(dim3((dev_.Hi + R - 1) / R, dev_.C), dim3(32 * wpb), fast_rows_smem(dev_, frow_, wpb), st);
-      PDT_CUDA_CHECK(cudaLaunchKernelEx(&lx.cfg, frow_.fwd[tune_.wf], dev_, ubar, t1, tick));
+      const bool cc = concurrent_ && frow_cc_.ok();
+      const FastRowKernels& k = cc ? frow_cc_ : frow_;
+      const int wf = cc ? tune_.wfc : tune_.wf;
+      const int wpb = kWpbChoices[wf];
+      const int R = k.rows_per_block(wpb);
+      LaunchEx lx(dim3((dev_.Hi + R - 1) / R, dev_.C), dim3(32 * wpb), fast_rows_smem(dev_, k, wpb), st);
+      PDT_CUDA_CHECK(cudaLaunchKernelEx(&lx.cfg, k.fwd[wf], dev_, ubar, t1, tick));
       count_launch();
       return;
     }
@@ -606,12 +615,12 @@ class CartesianOp : public OpImpl, public SolverHooks {
   // K^H: G coil-group partial images (or, with a cluster, one reduced image) into out.
   void launch_rows_adj(const float2* t2, float2* out, int G, cudaStream_t st) {
     if (frow_.ok()) {
+      const FastRowKernels& k = (concurrent_ && frow_cc_.ok()) ? frow_cc_ : frow_;
       const int wpb = kWpbChoices[tune_.wa];
       const bool cl = tune_.cluster && G > 1;
-      const int R = frow_.rows_per_block(wpb);
-      LaunchEx lx(dim3((dev_.Hi + R - 1) / R, G), dim3(32 * wpb), fast_rows_adj_smem(dev_, frow_, wpb), st,
-                  cl ? G : 0);
-      PDT_CUDA_CHECK(cudaLaunchKernelEx(&lx.cfg, frow_.adj[tune_.wa], dev_, t2, out, cl ? 1 : 0, G,
+      const int R = k.rows_per_block(wpb);
+      LaunchEx lx(dim3((dev_.Hi + R - 1) / R, G), dim3(32 * wpb), fast_rows_adj_smem(dev_, k, wpb), st, cl ? G : 0);
+      PDT_CUDA_CHECK(cudaLaunchKernelEx(&lx.cfg, k.adj[tune_.wa], dev_, t2, out, cl ? 1 : 0, G,
                                         (long long)dev_.Hi * dev_.W));
       count_launch();
       return;
@@ -673,8 +682,9 @@ class CartesianOp : public OpImpl, public SolverHooks {
     d.ns = (int)col_x.size();
     // lane-FFT kernels where the length has a compiled split (they fix the compact k-space order)
     frow_ = find_row_kernels(W);
+    frow_cc_ = frow_.ok() ? find_concurrent_row_kernels(W) : FastRowKernels();  // forward and adjoint rows
     fcol_ = find_col_kernels(Hf);
-    if (frow_.ok() && fast_rows_adj_smem(d, frow_, 8) > (size_t)g_max_smem) frow_ = FastRowKernels();
+    if (frow_.ok() && fast_rows_adj_smem(d, frow_, 8) > (size_t)g_max_smem) frow_ = frow_cc_ = FastRowKernels();
     // tensor-core DFT rows: even W (16-byte row vectors), at most 128 coils (a row tile holds one image row
     // of every coil)
     const bool tc_any = W % 2 == 0 && d.ns > 0 && std::getenv("PDT_NO_TENSOR_ROWS") == nullptr;
@@ -755,6 +765,10 @@ class CartesianOp : public OpImpl, public SolverHooks {
       if (frow_.ok()) {
         PDT_CUDA_CHECK(cudaFuncSetAttribute(frow_.fwd[w], cudaFuncAttributeMaxDynamicSharedMemorySize, g_max_smem));
         PDT_CUDA_CHECK(cudaFuncSetAttribute(frow_.adj[w], cudaFuncAttributeMaxDynamicSharedMemorySize, g_max_smem));
+      }
+      if (frow_cc_.ok()) {
+        PDT_CUDA_CHECK(cudaFuncSetAttribute(frow_cc_.fwd[w], cudaFuncAttributeMaxDynamicSharedMemorySize, g_max_smem));
+        PDT_CUDA_CHECK(cudaFuncSetAttribute(frow_cc_.adj[w], cudaFuncAttributeMaxDynamicSharedMemorySize, g_max_smem));
       }
       if (fcol_.ok())
         PDT_CUDA_CHECK(cudaFuncSetAttribute(fcol_.cols[w], cudaFuncAttributeMaxDynamicSharedMemorySize, g_max_smem));
@@ -958,6 +972,8 @@ class CartesianOp : public OpImpl, public SolverHooks {
   FastRowKernels frow_;
   FastColKernels fcol_;
   bool tcf_ok_ = false, tca_ok_ = false;
+  FastRowKernels frow_cc_;  // forward-row split for concurrent rounds (set_concurrent)
+  bool concurrent_ = false;
   bool fuse_dual_ = true;  // PDT_NO_FUSED_DUAL: the solvers' dual update always in its own kernel
   bool colz_ = false;  // the column kernel's zero-slot specialisation applies
   std::vector<int> col_x_h_;

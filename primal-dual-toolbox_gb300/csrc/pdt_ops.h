@@ -43,6 +43,9 @@ struct SolverHooks {
                      int* tick, cudaStream_t st, PhaseMarker* mk = nullptr, const DualStep* dual = nullptr) = 0;
   // Whether round() can run a W x H dual update in blocks its launches leave idle.
   virtual bool can_fuse_dual(int W, int H) { return false; }
+  // While on, the rounds launch beside other problems' kernels (batched solves): prefer kernels that
+  // leave room on each SM over the ones fastest alone.
+  virtual void set_concurrent(bool on) {}
   virtual int groups() = 0;
   virtual long long group_stride() = 0;
   // img <- K^H f from the compact layout (the solver's initial u0 = A^T f).
