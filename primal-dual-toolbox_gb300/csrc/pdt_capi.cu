@@ -725,19 +725,20 @@ class OptImpl {
     cudaStream_t aux = aux_;
     cudaEvent_t ev_fork = ev_fork_, ev_join = ev_join_;
     // one iteration: the dual update runs inside the operator's round where the operator has idle
-    // blocks for it, else on `aux`, forked from and joined back into `s`, concurrently with the round
-    // (profiling runs it in line so that every phase has its own interval)
+    // blocks for it (profiling then times it as part of that launch), else on `aux`, forked from and
+    // joined back into `s`, concurrently with the round (profiling runs it in line so that every phase
+    // has its own interval)
     const bool fused = hk->can_fuse_dual(W_, H_);
     pl.body = [=](int par, cudaStream_t s) {
       const int in = p0 ^ par, out = in ^ 1;
       const float2* ubar = static_cast<const float2*>(field(F_UB, in));
-      if (prof_) {
+      if (fused) {
+        const DualStep ds{ptrs(in), ptrs(out), sigma, atab, iter, W_, H_, is_tgv ? 1 : 0};
+        hk->round(ubar, r_.as<float2>(), fc_.as<float2>(), sigma, lambda, khr, nullptr, s, prof_, &ds);
+      } else if (prof_) {
         launch_mri_dual(is_tgv, W_, H_, ptrs(in), ptrs(out), sigma, atab, iter, s);
         prof_->mark(is_tgv ? "mri_dual_tgv" : "mri_dual_tv", s);
         hk->round(ubar, r_.as<float2>(), fc_.as<float2>(), sigma, lambda, khr, nullptr, s, prof_);
-      } else if (fused) {
-        const DualStep ds{ptrs(in), ptrs(out), sigma, atab, iter, W_, H_, is_tgv ? 1 : 0};
-        hk->round(ubar, r_.as<float2>(), fc_.as<float2>(), sigma, lambda, khr, nullptr, s, nullptr, &ds);
       } else {
         PDT_CUDA_CHECK(cudaEventRecord(ev_fork, s));
         PDT_CUDA_CHECK(cudaStreamWaitEvent(aux, ev_fork, 0));
