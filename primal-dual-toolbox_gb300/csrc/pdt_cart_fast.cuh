@@ -39,6 +39,7 @@ __global__ void __launch_bounds__(32 * WPB) fl_rows_fwd(CartDev d, const float2*
     fs2s[i] = d.fslot2s[i];
   }
   pdl_wait();  // ubar comes from the previous kernel; t1 may still be read by it
+  pdl_trigger();
   if (tick && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) atomicAdd(tick, 1);
   __syncthreads();
   const int lane = threadIdx.x & 31, t = lane & (L - 1);
@@ -87,6 +88,7 @@ __global__ void __launch_bounds__(32 * WPB) fl_cols(CartDev d, int mode, const f
   float2* tw = sm;
   for (int i = threadIdx.x; i < Hf; i += blockDim.x) tw[i] = d.twH[i];
   pdl_wait();  // t_in, r and fc come from earlier kernels
+  pdl_trigger();
   __syncthreads();
   const int lane = threadIdx.x & 31, t = lane & (L - 1);
   const int s0 = (blockIdx.x * WPB + (threadIdx.x >> 5)) * (32 / L) + lane / L;
@@ -195,6 +197,7 @@ __global__ void __launch_bounds__(32 * WPB) fl_cols64(CartDev d, int mode, const
   const int bar = 1 + pair;  // named barrier of this column's two warps (0 is __syncthreads)
   for (int i = threadIdx.x; i < Hf; i += blockDim.x) tw[i] = d.twH[i];
   pdl_wait();  // t_in, r and fc come from earlier kernels
+  pdl_trigger();
   __syncthreads();
   const int t = threadIdx.x & 63;
   const int s0 = blockIdx.x * (WPB / 2) + pair;
@@ -300,6 +303,7 @@ __global__ void __launch_bounds__(32 * WPB, 16 / WPB) fl_rows_adj(CartDev d, con
   }
   for (int i = threadIdx.x; i < R * W; i += blockDim.x) red[i] = c2(0.f, 0.f);
   pdl_wait();  // t2 comes from the previous kernel; out may still be read by earlier ones
+  pdl_trigger();
   const int lane = threadIdx.x & 31, t = lane & (L - 1);
   const int r = (threadIdx.x >> 5) * (32 / L) + lane / L;
   const int yi0 = blockIdx.x * R;

@@ -96,6 +96,7 @@ __global__ void __launch_bounds__(kTcAdjThreads, 1) tc_rows_adj(CartDev d, const
     // rows of blocks past the row tiles run the solver's dual update (no TMEM, no barriers); its inputs
     // come from before the previous launch, its outputs are read only after this launch completes
     pdl_wait();
+    pdl_trigger();
     const int db = (blockIdx.y - ntiles) * gridDim.x + blockIdx.x, nd = (gridDim.y - ntiles) * gridDim.x;
     if (ds.tgv)
       mri_dual_blocks<true>(ds, db, nd);
@@ -151,6 +152,7 @@ __global__ void __launch_bounds__(kTcAdjThreads, 1) tc_rows_adj(CartDev d, const
     }
   }
   pdl_wait();  // every thread: t2 comes from the column kernel
+  pdl_trigger();
   if (tid == 32) {
     const uint32_t idesc = tc::idesc_tf32(kTcRows, nb);
     for (int j = 0; j < nch && ok; ++j) {
@@ -377,6 +379,7 @@ __global__ void __launch_bounds__(kTcFwdThreads, 1) tc_rows_fwd(CartDev d, const
     }
   }
   pdl_wait();  // every thread: ubar comes from the previous kernel; t1 may still be read by it
+  pdl_trigger();
   if (tick && blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && tid == 0) atomicAdd(tick, 1);
   if (tid == 32) {
     const uint32_t idesc = tc::idesc_tf32(kTcRows, nb);

@@ -30,6 +30,10 @@ __host__ __device__ __forceinline__ float2 conjf2(float2 a) { return c2(a.x, -a.
 // launched while its predecessor in the stream finishes; pdl_wait() blocks until the predecessor grid
 // has completed and its writes are visible (it returns at once for an ordinary launch).
 __device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+// Lets the next kernel in the stream launch once every block of this grid has executed it (or exited), so
+// that its blocks take SMs as they free up and run their set-up before their own pdl_wait(). Called right
+// after pdl_wait(): only the next grid is launched early, and it still waits for this one to complete.
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 #endif
 
 // |z|^2 of a pixel (real or complex).

@@ -290,6 +290,7 @@ template <bool TGV>
 __global__ void __launch_bounds__(NT) mri_primal_kernel(int W, int H, ImgPtrs out, const float2* __restrict__ khr,
                                                         int G, long long gstride, float tau, int* __restrict__ iter) {
   pdl_wait();  // K^H r comes from the previous kernel
+  pdl_trigger();
   if (iter && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) atomicAdd(iter, 1);
   const int x = blockIdx.x * TX + threadIdx.x % TX, y = blockIdx.y * TY + threadIdx.x / TX;
   if (x >= W || y >= H) return;
