@@ -353,12 +353,14 @@ class CartesianOp : public OpImpl, public SolverHooks {
   }
   long long group_stride() override { return (long long)dev_.Hi * dev_.W; }
   // The dual update rides in the tensor-core adjoint launch when its row tiles leave at least
-  // kMinDualBlocks SMs free (one CTA per SM), one row of dual blocks per N range.
+  // kMinDualBlocks SMs free (one CTA per SM), one row of dual blocks per N range, and no more rows than
+  // give each thread a pixel.
   static constexpr int kMinDualBlocks = 8;
   int dual_rows() {
     const int gx = (2 * dev_.W + tc_adj_nb(tune_.nr) - 1) / tc_adj_nb(tune_.nr);
     const int idle = g_num_sms - gx * tc_adj_tiles();
-    return idle >= kMinDualBlocks ? idle / gx : 0;
+    const long long need = ((long long)dev_.W * dev_.Hi + kTcAdjThreads - 1) / kTcAdjThreads;  // blocks
+    return idle >= kMinDualBlocks ? (int)std::min<long long>(idle / gx, (need + gx - 1) / gx) : 0;
   }
   void set_concurrent(bool on) override { concurrent_ = on; }
   bool can_fuse_dual(int W, int H) override {
