@@ -523,26 +523,48 @@ class CartesianOp : public OpImpl, public SolverHooks {
     if (tcb_nb_ == NB) return;
     const int W = dev_.W, ns = dev_.ns, nch = tc_adj_chunks(), nranges = (2 * W + NB - 1) / NB;
     std::vector<float> h((size_t)nranges * nch * 2 * NB * 32, 0.f);
-    const std::vector<double> wc = host_roots(W, 0), ws = host_roots(W, 1);  // cos, sin of 2 pi m / W
+    std::vector<float> wc(W), ws(W);  // cos, sin of 2 pi m / W, rounded from double
+    {
+      const std::vector<double> c = host_roots(W, 0), sn = host_roots(W, 1);
+      for (int m = 0; m < W; ++m) wc[m] = (float)c[m], ws[m] = (float)sn[m];
+    }
+    // exp(+2 pi i p_s q(x) / W) = conj(w^(p q)) with p_s the inverse-FFT input slot of sampled column s and
+    // q(x) = (x - W/2) mod W; along a tile row x advances by one, so the root index advances by p_s
     for (int i = 0; i < nranges; ++i) {
       const int n0 = i * NB, nb = std::min(NB, (2 * W - n0 + 15) & ~15);
+      const int x0 = n0 >> 1, x1 = std::min(W, (n0 + nb) >> 1);
+      const int q0 = ((x0 - dev_.oxW) % W + W) % W;
       for (int j = 0; j < nch; ++j) {
         float* hi = &h[((size_t)i * nch + j) * 2 * NB * 32];
         float* lo = hi + (size_t)nb * 32;
-        for (int n = 0; n < nb; ++n) {
-          const int x = (n0 + n) >> 1, o = (n0 + n) & 1;
-          if (x >= W) continue;
-          const int q = ((x - dev_.oxW) % W + W) % W;
-          for (int k = 0; k < 32; ++k) {
-            const int s = 16 * j + (k >> 1), ri = k & 1;
-            if (s >= ns) continue;
-            const int p = (col_x_h_[s] + dev_.mxW) % W;
-            const int m = (int)(((long long)p * q) % W);
-            const float er = (float)wc[m], ei = (float)ws[m];  // exp(+2 pi i m / W) = conj(w^(p q))
-            const float v = o == 0 ? (ri == 0 ? er : -ei) : (ri == 0 ? ei : er);
-            const int pos = n * 32 + (((k >> 2) ^ (n & 7)) << 2) + (k & 3);
-            hi[pos] = tc_host_tf32(v);
-            lo[pos] = tc_host_tf32(v - hi[pos]);
+        const int kn = std::min(16, ns - 16 * j);  // sampled columns of this K chunk
+        int m[16], p[16];
+        for (int kk = 0; kk < kn; ++kk) {
+          p[kk] = (col_x_h_[16 * j + kk] + dev_.mxW) % W;
+          m[kk] = (int)(((long long)p[kk] * q0) % W);
+        }
+        // rows n = 2 (x - x0) + o (o = re/im output), K elements k = 2 kk + (re/im input):
+        // [[Re e, -Im e], [Im e, Re e]], 128-byte swizzle of the 16-byte chunks within a row
+        for (int x = x0; x < x1; ++x) {
+          const int n = 2 * (x - x0);
+          for (int o = 0; o < 2; ++o) {
+            float* hr = hi + (size_t)(n + o) * 32;
+            float* lr = lo + (size_t)(n + o) * 32;
+            const int sw = (n + o) & 7;
+            for (int kk = 0; kk < kn; ++kk) {
+              const float er = wc[m[kk]], ei = ws[m[kk]];
+              const float v0 = o == 0 ? er : ei, v1 = o == 0 ? -ei : er;
+              const int k0 = 2 * kk, k1 = k0 + 1;
+              const int a0 = (((k0 >> 2) ^ sw) << 2) + (k0 & 3), a1 = (((k1 >> 2) ^ sw) << 2) + (k1 & 3);
+              hr[a0] = tc_host_tf32(v0);
+              lr[a0] = tc_host_tf32(v0 - hr[a0]);
+              hr[a1] = tc_host_tf32(v1);
+              lr[a1] = tc_host_tf32(v1 - hr[a1]);
+            }
+          }
+          for (int kk = 0; kk < kn; ++kk) {
+            m[kk] += p[kk];
+            if (m[kk] >= W) m[kk] -= W;
           }
         }
       }
@@ -675,12 +697,15 @@ class CartesianOp : public OpImpl, public SolverHooks {
     // sampled columns
     const float* mask = reinterpret_cast<const float*>(mk.host.data());
     std::vector<int> col_x;
-    for (int x = 0; x < W; ++x)
-      for (int y = 0; y < Hf; ++y)
-        if (mask[(size_t)y * W + x] != 0.0f) {
-          col_x.push_back(x);
-          break;
-        }
+    {
+      std::vector<char> sampled(W, 0);  // row by row: the mask is stored W-fastest
+      for (int y = 0; y < Hf; ++y) {
+        const float* row = mask + (size_t)y * W;
+        for (int x = 0; x < W; ++x) sampled[x] |= row[x] != 0.0f;
+      }
+      for (int x = 0; x < W; ++x)
+        if (sampled[x]) col_x.push_back(x);
+    }
     d.ns = (int)col_x.size();
     // lane-FFT kernels where the length has a compiled split (they fix the compact k-space order)
     frow_ = find_row_kernels(W);
@@ -746,11 +771,13 @@ class CartesianOp : public OpImpl, public SolverHooks {
                         sizeof(float) * maskc.size() + sizeof(float2) * ((size_t)W + Hf);
     tables_.ensure(need);
     char* base = tables_.as<char>();
+    std::vector<char> staged(need);  // assembled on the host, uploaded in one copy below
     size_t off = 0;
     auto put = [&](const void* src, size_t bytes) {
       off = (off + 15) & ~(size_t)15;
+      if (off + bytes > need) throw Error(PDT_ERR_STATE, name_ + ": operator tables overflow their allocation");
+      if (bytes) std::memcpy(staged.data() + off, src, bytes);
       char* dst = base + off;
-      if (bytes) PDT_CUDA_CHECK(cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice));
       off += bytes;
       return dst;
     };
@@ -762,6 +789,7 @@ class CartesianOp : public OpImpl, public SolverHooks {
     d.fslot2s = reinterpret_cast<const int*>(put(fslot2s.data(), sizeof(int) * W));
     d.maskc = reinterpret_cast<const float*>(put(maskc.data(), sizeof(float) * maskc.size()));
     d.kperm = fcol_.ok() ? reinterpret_cast<const int*>(put(kperm.data(), sizeof(int) * Hf)) : nullptr;
+    PDT_CUDA_CHECK(cudaMemcpy(base, staged.data(), off, cudaMemcpyHostToDevice));
     scratch_.ensure(std::max<size_t>(1, (size_t)C * d.ns * d.Hi) * sizeof(float2));
     for (int w = 0; w < 3; ++w) {
       if (frow_.ok()) {
