@@ -832,6 +832,14 @@ class CartesianOp : public OpImpl, public SolverHooks {
   void autotune() {
     if (!frow_.ok() && !fcol_.ok() && !tcf_ok_ && !tca_ok_) return;
     if (pinned_tune()) return;
+    // candidates are timed with the kernels of a problem alone (an operator first prepared inside a
+    // batched solve would otherwise time the concurrent row split for every forward and adjoint choice)
+    struct Alone {
+      bool& flag;
+      const bool saved;
+      explicit Alone(bool& f) : flag(f), saved(f) { flag = false; }
+      ~Alone() { flag = saved; }
+    } alone(concurrent_);
     static std::mutex g_tune_mu;
     static std::map<std::array<int, 6>, std::pair<Tune, int>> g_tune_cache;
     const std::array<int, 6> key = {dev_.W, dev_.Hf, dev_.Hi, dev_.C, dev_.ns, dev_.sens ? 1 : 0};
