@@ -30,6 +30,7 @@
 #include <mutex>
 #include <sstream>
 
+#include "pdt_cart_tiles.h"
 #include "pdt_device.cuh"
 #include "pdt_fftplan.h"
 #include "pdt_ops.h"
@@ -223,23 +224,6 @@ size_t rows_smem(const CartDev& d, bool with_acc) {
   return sizeof(float2) * ((size_t)d.W + 2 * (size_t)d.RB * d.ldW + (with_acc ? (size_t)d.RB * d.W : 0));
 }
 size_t cols_smem(const CartDev& d) { return sizeof(float2) * ((size_t)d.Hf + 2 * (size_t)d.CB * d.ldH); }
-
-// v rounded to TF32 (10 explicit mantissa bits, ties away from zero): the host side of split_tf32
-float tc_host_tf32(float v) {
-  uint32_t u;
-  std::memcpy(&u, &v, 4);
-  u = (u + 0x1000u) & 0xFFFFE000u;
-  std::memcpy(&v, &u, 4);
-  return v;
-}
-
-// cos (which = 0) or sin (which = 1) of 2 pi m / n for m < n, in double precision
-std::vector<double> host_roots(int n, int which) {
-  const double two_pi = 6.283185307179586476925286766559;
-  std::vector<double> r(n);
-  for (int m = 0; m < n; ++m) r[m] = which ? std::sin(two_pi * m / n) : std::cos(two_pi * m / n);
-  return r;
-}
 
 int g_num_sms = 0;
 int g_max_smem = 0;
@@ -509,7 +493,7 @@ class CartesianOp : public OpImpl, public SolverHooks {
                                       tc_err()));
     count_launch();
   }
-  int tc_adj_chunks() const { return (2 * dev_.ns + 31) / 32; }
+  int tc_adj_chunks() const { return tc_adj_chunk_count(dev_.ns); }
   // image rows per adjoint row tile: the tile's 128 rows hold them for every coil
   int tc_adj_yb() const { return kTcRows / dev_.C; }
   int tc_adj_tiles() const { return (dev_.Hi + tc_adj_yb() - 1) / tc_adj_yb(); }
@@ -521,54 +505,8 @@ class CartesianOp : public OpImpl, public SolverHooks {
   // output), K element k = 2 s + (re/im input), 128-byte swizzle. Values in double precision, then split.
   void build_tc_adj_tiles(int NB) {
     if (tcb_nb_ == NB) return;
-    const int W = dev_.W, ns = dev_.ns, nch = tc_adj_chunks(), nranges = (2 * W + NB - 1) / NB;
-    std::vector<float> h((size_t)nranges * nch * 2 * NB * 32, 0.f);
-    std::vector<float> wc(W), ws(W);  // cos, sin of 2 pi m / W, rounded from double
-    {
-      const std::vector<double> c = host_roots(W, 0), sn = host_roots(W, 1);
-      for (int m = 0; m < W; ++m) wc[m] = (float)c[m], ws[m] = (float)sn[m];
-    }
-    // exp(+2 pi i p_s q(x) / W) = conj(w^(p q)) with p_s the inverse-FFT input slot of sampled column s and
-    // q(x) = (x - W/2) mod W; along a tile row x advances by one, so the root index advances by p_s
-    for (int i = 0; i < nranges; ++i) {
-      const int n0 = i * NB, nb = std::min(NB, (2 * W - n0 + 15) & ~15);
-      const int x0 = n0 >> 1, x1 = std::min(W, (n0 + nb) >> 1);
-      const int q0 = ((x0 - dev_.oxW) % W + W) % W;
-      for (int j = 0; j < nch; ++j) {
-        float* hi = &h[((size_t)i * nch + j) * 2 * NB * 32];
-        float* lo = hi + (size_t)nb * 32;
-        const int kn = std::min(16, ns - 16 * j);  // sampled columns of this K chunk
-        int m[16], p[16];
-        for (int kk = 0; kk < kn; ++kk) {
-          p[kk] = (col_x_h_[16 * j + kk] + dev_.mxW) % W;
-          m[kk] = (int)(((long long)p[kk] * q0) % W);
-        }
-        // rows n = 2 (x - x0) + o (o = re/im output), K elements k = 2 kk + (re/im input):
-        // [[Re e, -Im e], [Im e, Re e]], 128-byte swizzle of the 16-byte chunks within a row
-        for (int x = x0; x < x1; ++x) {
-          const int n = 2 * (x - x0);
-          for (int o = 0; o < 2; ++o) {
-            float* hr = hi + (size_t)(n + o) * 32;
-            float* lr = lo + (size_t)(n + o) * 32;
-            const int sw = (n + o) & 7;
-            for (int kk = 0; kk < kn; ++kk) {
-              const float er = wc[m[kk]], ei = ws[m[kk]];
-              const float v0 = o == 0 ? er : ei, v1 = o == 0 ? -ei : er;
-              const int k0 = 2 * kk, k1 = k0 + 1;
-              const int a0 = (((k0 >> 2) ^ sw) << 2) + (k0 & 3), a1 = (((k1 >> 2) ^ sw) << 2) + (k1 & 3);
-              hr[a0] = tc_host_tf32(v0);
-              lr[a0] = tc_host_tf32(v0 - hr[a0]);
-              hr[a1] = tc_host_tf32(v1);
-              lr[a1] = tc_host_tf32(v1 - hr[a1]);
-            }
-          }
-          for (int kk = 0; kk < kn; ++kk) {
-            m[kk] += p[kk];
-            if (m[kk] >= W) m[kk] -= W;
-          }
-        }
-      }
-    }
+    std::vector<float> h;
+    build_tc_adj_table(dev_.W, dev_.ns, col_x_h_.data(), dev_.mxW, dev_.oxW, NB, h);
     tcb_.ensure(h.size() * sizeof(float));
     PDT_CUDA_CHECK(cudaMemcpy(tcb_.p, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice));
     tcb_nb_ = NB;
