@@ -1,5 +1,5 @@
-// pdt_cart_tiles.h -- host construction of the tensor-core adjoint rows' DFT-factor operand tiles
-// (plain C++, no CUDA: also compiled for the host-side layout tests).
+// pdt_cart_tiles.h -- host construction of the tensor-core row passes' DFT-factor operand tiles (plain
+// C++, no CUDA: also compiled for the host-side layout tests).
 //
 // The adjoint rows compute g_c[y][x] = sum_s t2[c][s][y] exp(+2 pi i p_s q(x) / W), with p_s the
 // inverse-FFT input slot of sampled column s, p_s = (col_x[s] + mxW) mod W, and q(x) = (x - oxW) mod W
@@ -84,6 +84,43 @@ inline void build_tc_adj_table(int W, int ns, const int* col_x, int mxW, int oxW
         for (int kk = 0; kk < kn; ++kk) {
           m[kk] += p[kk];
           if (m[kk] >= W) m[kk] -= W;
+        }
+      }
+    }
+  }
+}
+
+// The forward rows' factor for tc_rows_fwd: t1[c][s][y] = sum_x (ubar . sens_c)[y][x] w^(q(x) f_s) with
+// w = exp(-2 pi i / W), q(x) = (x + mxW) mod W the ifftshift slot of image column x and f_s = (col_x[s] - oxW)
+// mod W the forward-FFT output slot of sampled column s. Layout: [s tile z of 128 sampled columns][K chunk
+// j of 16 image columns][hi rows | lo rows], chunk stride 2 nbmax 32 floats with nbmax = round16(2 min(128,
+// ns)); row n = 2 sl + o (output s = 128 z + sl, re/im part o; a tile's nb = round16(2 nsl) rows), K element
+// k = 2 (x - 16 j) + (re/im input), the same 2 x 2 blocks, swizzle and split as the adjoint table.
+inline int tc_fwd_rows_max(int ns) { return (2 * std::min(128, ns) + 15) & ~15; }
+
+inline void build_tc_fwd_table(int W, int ns, const int* col_x, int mxW, int oxW, std::vector<float>& h) {
+  const int nchT = (2 * W + 31) / 32, stiles = (ns + 127) / 128;
+  const int nbmax = tc_fwd_rows_max(ns);
+  h.assign((size_t)stiles * nchT * 2 * nbmax * 32, 0.f);
+  const std::vector<double> wc = host_roots(W, 0), ws = host_roots(W, 1);  // cos, sin of 2 pi m / W
+  for (int z = 0; z < stiles; ++z) {
+    const int nsl = std::min(128, ns - 128 * z), nb = (2 * nsl + 15) & ~15;
+    for (int j = 0; j < nchT; ++j) {
+      float* hi = &h[((size_t)z * nchT + j) * 2 * nbmax * 32];
+      float* lo = hi + (size_t)nb * 32;
+      for (int n = 0; n < 2 * nsl; ++n) {
+        const int s = 128 * z + (n >> 1), o = n & 1;
+        const int f = ((col_x[s] - oxW) % W + W) % W;  // forward-FFT output slot of s
+        for (int k = 0; k < 32; ++k) {
+          const int x = 16 * j + (k >> 1), ri = k & 1;
+          if (x >= W) continue;
+          const int q = (x + mxW) % W;  // ifftshift slot of image column x
+          const int m = (int)(((long long)q * f) % W);
+          const float er = (float)wc[m], ei = -(float)ws[m];  // w^(q f) = exp(-2 pi i m / W)
+          const float v = o == 0 ? (ri == 0 ? er : -ei) : (ri == 0 ? ei : er);
+          const int pos = n * 32 + (((k >> 2) ^ (n & 7)) << 2) + (k & 3);
+          hi[pos] = tc_host_tf32(v);
+          lo[pos] = tc_host_tf32(v - hi[pos]);
         }
       }
     }

@@ -440,7 +440,7 @@ class CartesianOp : public OpImpl, public SolverHooks {
   };
 
   int tc_adj_nb(int nr) const { return std::min(kTcAdjMaxNB, ((2 * dev_.W + nr - 1) / nr + 15) & ~15); }
-  int tc_fwd_nb() const { return (2 * std::min(128, dev_.ns) + 15) & ~15; }
+  int tc_fwd_nb() const { return tc_fwd_rows_max(dev_.ns); }
   int tc_fwd_stages() const {
     return std::min(kTcMaxStages,
                     (int)(((size_t)g_max_smem - tc_fwd_smem(tc_fwd_nb(), 0)) / tc_stage_bytes(tc_fwd_nb())));
@@ -451,32 +451,8 @@ class CartesianOp : public OpImpl, public SolverHooks {
   // w^(q(x) f_s), values in double precision, then split.
   void build_tc_fwd_tiles() {
     if (tcf_built_) return;
-    const int W = dev_.W, ns = dev_.ns, nchT = (2 * W + 31) / 32, stiles = (ns + 127) / 128;
-    const int nbmax = tc_fwd_nb();
-    std::vector<float> h((size_t)stiles * nchT * 2 * nbmax * 32, 0.f);
-    const std::vector<double> wc = host_roots(W, 0), ws = host_roots(W, 1);  // cos, sin of 2 pi m / W
-    for (int z = 0; z < stiles; ++z) {
-      const int nsl = std::min(128, ns - 128 * z), nb = (2 * nsl + 15) & ~15;
-      for (int j = 0; j < nchT; ++j) {
-        float* hi = &h[((size_t)z * nchT + j) * 2 * nbmax * 32];
-        float* lo = hi + (size_t)nb * 32;
-        for (int n = 0; n < 2 * nsl; ++n) {
-          const int s = 128 * z + (n >> 1), o = n & 1;
-          const int f = ((col_x_h_[s] - dev_.oxW) % W + W) % W;  // forward-FFT output slot of s
-          for (int k = 0; k < 32; ++k) {
-            const int x = 16 * j + (k >> 1), ri = k & 1;
-            if (x >= W) continue;
-            const int q = (x + dev_.mxW) % W;  // ifftshift slot of image column x
-            const int m = (int)(((long long)q * f) % W);
-            const float er = (float)wc[m], ei = -(float)ws[m];  // w^(q f) = exp(-2 pi i m / W)
-            const float v = o == 0 ? (ri == 0 ? er : -ei) : (ri == 0 ? ei : er);
-            const int pos = n * 32 + (((k >> 2) ^ (n & 7)) << 2) + (k & 3);
-            hi[pos] = tc_host_tf32(v);
-            lo[pos] = tc_host_tf32(v - hi[pos]);
-          }
-        }
-      }
-    }
+    std::vector<float> h;
+    build_tc_fwd_table(dev_.W, dev_.ns, col_x_h_.data(), dev_.mxW, dev_.oxW, h);
     tcf_tiles_.ensure(h.size() * sizeof(float));
     PDT_CUDA_CHECK(cudaMemcpy(tcf_tiles_.p, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice));
     tcf_built_ = true;
