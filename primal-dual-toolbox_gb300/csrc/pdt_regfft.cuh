@@ -157,7 +157,6 @@ struct TwoLevel {
 };
 
 
-#ifndef PDT_HOST_EMULATION
 // ------------------------------------------------------------------------------------------------
 // Lane-distributed transform of length n = M * L over a group of L lanes (L = 8, 16, 32):
 // lane t holds x[t + L j] (j < M) in registers. The forward transform is an M-point register FFT per
@@ -170,6 +169,7 @@ struct TwoLevel {
 // ------------------------------------------------------------------------------------------------
 constexpr int ct_log2(int n) { return n <= 1 ? 0 : 1 + ct_log2(n / 2); }
 
+#ifndef PDT_HOST_EMULATION
 __device__ __forceinline__ float2 shfl_xor2(float2 v, int m) {
   return c2(__shfl_xor_sync(0xffffffffu, v.x, m), __shfl_xor_sync(0xffffffffu, v.y, m));
 }
@@ -179,6 +179,18 @@ template <int L>
 __device__ __forceinline__ int lane_brev(int t) {
   return (int)(__brev((unsigned)t) >> (32 - ct_log2(L)));
 }
+#else
+// host build of the layout tests: the exchange between lanes is supplied by the test harness, which runs
+// one host thread per lane
+float2 shfl_xor2(float2 v, int m);
+
+template <int L>
+inline int lane_brev(int t) {
+  int r = 0;
+  for (int b = 0; b < ct_log2(L); ++b) r |= ((t >> b) & 1) << (ct_log2(L) - 1 - b);
+  return r;
+}
+#endif
 
 template <int M, int L>
 struct LaneFft {
@@ -228,6 +240,7 @@ struct LaneFft {
   }
 };
 
+#ifndef PDT_HOST_EMULATION
 // The same transform over two warps (n = M * 64): lanes 0-31 of the first warp and 32-63 of the second
 // hold the sequence. The stage that pairs lane t with t ^ 32 goes through the shared-memory buffer xbuf
 // (M x 64 values) between two syncs of the named barrier bar_id (64 threads); the others are shuffles.

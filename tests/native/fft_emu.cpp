@@ -3,7 +3,10 @@
 // buffer and write the other). Used by tests/test_fft_emulated.py to check the FFT plan and butterflies
 // against numpy on the CPU before any GPU run.
 #include <cmath>
+#include <condition_variable>
 #include <cstring>
+#include <mutex>
+#include <thread>
 #include <vector>
 struct float2 { float x, y; };
 inline float2 make_float2(float a, float b) { return {a, b}; }
@@ -106,5 +109,85 @@ extern "C" int emu_regfft(float* data, int n, int inverse) {
 extern "C" int emu_twolevel(float* data, int a, int b, int inverse) {
   EMU_TL(16, 23) EMU_TL(32, 20) EMU_TL(16, 20) EMU_TL(16, 16) EMU_TL(12, 16) EMU_TL(16, 24) EMU_TL(8, 8)
   EMU_TL(16, 12) EMU_TL(8, 16) EMU_TL(32, 24) EMU_TL(16, 32) EMU_TL(8, 12) EMU_TL(8, 20)
+  return 1;
+}
+
+// ---- the lane-distributed transform (LaneFft, pdt_regfft.cuh): one host thread per lane ------------
+namespace {
+// L threads that meet at a barrier around every exchange, like the L lanes of a lane group
+struct LaneGroup {
+  int L = 0;
+  std::vector<float2> slot;
+  std::mutex mu;
+  std::condition_variable cv;
+  int count = 0;
+  long gen = 0;
+  void barrier() {
+    std::unique_lock<std::mutex> lk(mu);
+    const long g = gen;
+    if (++count == L) {
+      count = 0;
+      ++gen;
+      cv.notify_all();
+    } else {
+      cv.wait(lk, [&] { return gen != g; });
+    }
+  }
+};
+thread_local LaneGroup* g_group = nullptr;
+thread_local int g_lane = 0;
+}  // namespace
+
+namespace pdt {
+float2 shfl_xor2(float2 v, int m) {
+  LaneGroup& G = *g_group;
+  G.slot[g_lane] = v;
+  G.barrier();
+  const float2 r = G.slot[g_lane ^ m];
+  G.barrier();
+  return r;
+}
+}  // namespace pdt
+
+// forward: natural order in, natural order out (each lane's X[k1 + M brev_L(t)] put back in place);
+// inverse: the same order in reverse, unnormalised
+template <int M, int L>
+static void lanefft(float* data, int inverse) {
+  using F = pdt::LaneFft<M, L>;
+  constexpr int n = M * L;
+  std::vector<float2> tw(n), out(n);
+  pdt::fill_twiddles(n, tw.data());
+  LaneGroup G;
+  G.L = L;
+  G.slot.resize(L);
+  std::vector<std::thread> lanes;
+  for (int t = 0; t < L; ++t)
+    lanes.emplace_back([&, t] {
+      g_group = &G;
+      g_lane = t;
+      float2 v[M];
+      const int kb = M * pdt::lane_brev<L>(t);
+      if (!inverse) {
+        for (int j = 0; j < M; ++j) v[j] = {data[2 * (t + L * j)], data[2 * (t + L * j) + 1]};
+        F::fwd(v, t, tw.data());
+        for (int k1 = 0; k1 < M; ++k1) out[k1 + kb] = v[k1];
+      } else {
+        for (int k1 = 0; k1 < M; ++k1) v[k1] = {data[2 * (k1 + kb)], data[2 * (k1 + kb) + 1]};
+        F::inv(v, t, tw.data());
+        for (int j = 0; j < M; ++j) out[t + L * j] = v[j];
+      }
+    });
+  for (auto& th : lanes) th.join();
+  for (int i = 0; i < n; ++i) {
+    data[2 * i] = out[i].x;
+    data[2 * i + 1] = out[i].y;
+  }
+}
+
+#define EMU_LANE(M, L) if (m == M && l == L) { lanefft<M, L>(data, inverse); return 0; }
+extern "C" int emu_lanefft(float* data, int m, int l, int inverse) {
+  EMU_LANE(4, 8) EMU_LANE(6, 8) EMU_LANE(8, 8) EMU_LANE(6, 16) EMU_LANE(8, 16) EMU_LANE(12, 16)
+  EMU_LANE(16, 16) EMU_LANE(10, 32) EMU_LANE(46, 8) EMU_LANE(23, 16) EMU_LANE(12, 32) EMU_LANE(16, 32)
+  EMU_LANE(20, 32) EMU_LANE(24, 32)
   return 1;
 }

@@ -14,7 +14,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 @pytest.fixture(scope="module")
 def emu(tmp_path_factory):
     out = str(tmp_path_factory.mktemp("fftemu") / "fft_emu.so")
-    subprocess.check_call(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-o", out,
+    subprocess.check_call(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-pthread", "-o", out,
                            os.path.join(HERE, "native", "fft_emu.cpp")])
     lib = ctypes.CDLL(out)
     lib.emu_fft.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int]
@@ -68,6 +68,28 @@ def test_two_level_fft_matches_numpy(emu, ab, inverse):
     x = (rng.standard_normal(n) + 1j * rng.standard_normal(n)).astype(np.complex64)
     y = x.copy()
     assert emu.emu_twolevel(y.ctypes.data, a, b, inverse) == 0
+    x64 = x.astype(np.complex128)
+    ref = np.fft.ifft(x64) * n if inverse else np.fft.fft(x64)
+    assert np.abs(y - ref).max() / np.abs(ref).max() < 5e-6
+
+
+# (M, L) of every lane-FFT split the Cartesian kernels compile (n = M L), including both splits of 368
+LANE_SPLITS = [(4, 8), (6, 8), (8, 8), (6, 16), (8, 16), (12, 16), (16, 16), (10, 32), (46, 8), (23, 16), (12, 32),
+               (16, 32), (20, 32), (24, 32)]
+
+
+@pytest.mark.parametrize("ml", LANE_SPLITS)
+@pytest.mark.parametrize("inverse", [0, 1])
+def test_lane_fft_matches_numpy(emu, ml, inverse):
+    """LaneFft<M, L> with one host thread per lane: the M-point register FFT, the twiddle and the log2 L
+    exchange stages, against numpy (forward; unnormalised inverse)."""
+    m, l = ml
+    n = m * l
+    emu.emu_lanefft.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+    rng = np.random.default_rng(3 * n + inverse)
+    x = (rng.standard_normal(n) + 1j * rng.standard_normal(n)).astype(np.complex64)
+    y = x.copy()
+    assert emu.emu_lanefft(y.ctypes.data, m, l, inverse) == 0
     x64 = x.astype(np.complex128)
     ref = np.fft.ifft(x64) * n if inverse else np.fft.fft(x64)
     assert np.abs(y - ref).max() / np.abs(ref).max() < 5e-6
