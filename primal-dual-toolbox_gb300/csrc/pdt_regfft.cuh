@@ -180,9 +180,10 @@ __device__ __forceinline__ int lane_brev(int t) {
   return (int)(__brev((unsigned)t) >> (32 - ct_log2(L)));
 }
 #else
-// host build of the layout tests: the exchange between lanes is supplied by the test harness, which runs
-// one host thread per lane
+// host build of the layout tests: the exchange between lanes and the 64-thread barrier are supplied by
+// the test harness, which runs one host thread per lane
 float2 shfl_xor2(float2 v, int m);
+void emu_sync64(int bar_id);
 
 template <int L>
 inline int lane_brev(int t) {
@@ -240,7 +241,6 @@ struct LaneFft {
   }
 };
 
-#ifndef PDT_HOST_EMULATION
 // The same transform over two warps (n = M * 64): lanes 0-31 of the first warp and 32-63 of the second
 // hold the sequence. The stage that pairs lane t with t ^ 32 goes through the shared-memory buffer xbuf
 // (M x 64 values) between two syncs of the named barrier bar_id (64 threads); the others are shuffles.
@@ -251,7 +251,11 @@ struct LaneFft64 {
   static constexpr int n = M * L;
 
   static __device__ __forceinline__ void sync64(int bar_id) {
+#ifndef PDT_HOST_EMULATION
     asm volatile("bar.sync %0, 64;" ::"r"(bar_id) : "memory");
+#else
+    emu_sync64(bar_id);
+#endif
   }
 
   static __device__ __forceinline__ void fwd(float2 (&v)[M], int t, const float2* __restrict__ tw, float2* xbuf,
@@ -326,6 +330,5 @@ struct LaneFft64 {
   }
 };
 
-#endif  // PDT_HOST_EMULATION
 
 }  // namespace pdt

@@ -147,6 +147,7 @@ float2 shfl_xor2(float2 v, int m) {
   G.barrier();
   return r;
 }
+void emu_sync64(int) { g_group->barrier(); }
 }  // namespace pdt
 
 // forward: natural order in, natural order out (each lane's X[k1 + M brev_L(t)] put back in place);
@@ -189,5 +190,45 @@ extern "C" int emu_lanefft(float* data, int m, int l, int inverse) {
   EMU_LANE(4, 8) EMU_LANE(6, 8) EMU_LANE(8, 8) EMU_LANE(6, 16) EMU_LANE(8, 16) EMU_LANE(12, 16)
   EMU_LANE(16, 16) EMU_LANE(10, 32) EMU_LANE(46, 8) EMU_LANE(23, 16) EMU_LANE(12, 32) EMU_LANE(16, 32)
   EMU_LANE(20, 32) EMU_LANE(24, 32)
+  return 1;
+}
+
+// the two-warp transform (LaneFft64): 64 threads, the cross-warp stage through a shared buffer
+template <int M>
+static void lanefft64(float* data, int inverse) {
+  using F = pdt::LaneFft64<M>;
+  constexpr int L = 64, n = M * L;
+  std::vector<float2> tw(n), out(n), xbuf((size_t)M * 64);
+  pdt::fill_twiddles(n, tw.data());
+  LaneGroup G;
+  G.L = L;
+  G.slot.resize(L);
+  std::vector<std::thread> lanes;
+  for (int t = 0; t < L; ++t)
+    lanes.emplace_back([&, t] {
+      g_group = &G;
+      g_lane = t;
+      float2 v[M];
+      const int kb = M * pdt::lane_brev<L>(t);
+      if (!inverse) {
+        for (int j = 0; j < M; ++j) v[j] = {data[2 * (t + L * j)], data[2 * (t + L * j) + 1]};
+        F::fwd(v, t, tw.data(), xbuf.data(), 1);
+        for (int k1 = 0; k1 < M; ++k1) out[k1 + kb] = v[k1];
+      } else {
+        for (int k1 = 0; k1 < M; ++k1) v[k1] = {data[2 * (k1 + kb)], data[2 * (k1 + kb) + 1]};
+        F::inv(v, t, tw.data(), xbuf.data(), 1);
+        for (int j = 0; j < M; ++j) out[t + L * j] = v[j];
+      }
+    });
+  for (auto& th : lanes) th.join();
+  for (int i = 0; i < n; ++i) {
+    data[2 * i] = out[i].x;
+    data[2 * i + 1] = out[i].y;
+  }
+}
+
+extern "C" int emu_lanefft64(float* data, int m, int inverse) {
+  if (m == 10) { lanefft64<10>(data, inverse); return 0; }
+  if (m == 6) { lanefft64<6>(data, inverse); return 0; }
   return 1;
 }

@@ -93,3 +93,19 @@ def test_lane_fft_matches_numpy(emu, ml, inverse):
     x64 = x.astype(np.complex128)
     ref = np.fft.ifft(x64) * n if inverse else np.fft.fft(x64)
     assert np.abs(y - ref).max() / np.abs(ref).max() < 5e-6
+
+
+@pytest.mark.parametrize("m", [10, 6])
+@pytest.mark.parametrize("inverse", [0, 1])
+def test_two_warp_lane_fft_matches_numpy(emu, m, inverse):
+    """LaneFft64<M> (n = 64 M over two warps; 640 = 10 x 64 is the readout-length column transform): the
+    cross-warp stage through the shared buffer between 64-thread barriers, the rest as shuffles."""
+    n = 64 * m
+    emu.emu_lanefft64.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
+    rng = np.random.default_rng(5 * n + inverse)
+    x = (rng.standard_normal(n) + 1j * rng.standard_normal(n)).astype(np.complex64)
+    y = x.copy()
+    assert emu.emu_lanefft64(y.ctypes.data, m, inverse) == 0
+    x64 = x.astype(np.complex128)
+    ref = np.fft.ifft(x64) * n if inverse else np.fft.fft(x64)
+    assert np.abs(y - ref).max() / np.abs(ref).max() < 5e-6
