@@ -226,11 +226,12 @@ PDT_API pdt_status pdt_batch_solve(pdt_batch* b, int verbose, void* stream);
  * another framework's memory pool or under a fixed device-memory budget, real-time loops that must not
  * enter the allocator, plugins whose host owns every allocation. All pointers are device pointers the
  * caller owns: sens {W,H,C} complex64, mask {W,H} float, img {W,H} or {W,H/2} (roos) complex64, kspace
- * {W,H,C} complex64 (every element is written). The scratch is a 32 MiB static device array that every
- * GPU loading libpdt.so holds until exit; C * W * image_rows * 8 bytes must fit in it, otherwise
- * PDT_ERR_UNSUPPORTED. The first call on a device resolves the array's address (cudaGetSymbolAddress),
- * so make that first call before any stream capture. Calls share the array: calls that overlap on the
- * GPU race and must be serialised by the caller. */
+ * {W,H,C} complex64 (every element is written). The scratch is a 32 MiB static device array (plus a
+ * 64 KiB twiddle table) that every GPU loading libpdt.so holds until exit; C * W * image_rows * 8 bytes
+ * must fit in it and W, H must be at most 4096, otherwise PDT_ERR_UNSUPPORTED. The first call on a
+ * device resolves the array's address (cudaGetSymbolAddress), so make that first call before any stream
+ * capture. Calls share the arrays: calls that overlap on the GPU race and must be serialised by the
+ * caller. */
 PDT_API pdt_status pdt_cartesian_forward_noalloc(int roos, const void* sens, const void* mask, int W, int H, int C,
                                                  const void* img, void* kspace, void* stream);
 

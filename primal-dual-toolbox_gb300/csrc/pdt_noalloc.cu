@@ -6,84 +6,60 @@
 // them: the caller passes the inputs and the output, and the only scratch the computation needs (the
 // k-space rows between the row and the column FFT passes) lives in one file-scope static device array
 // of kNoAllocScratchBytes that every GPU which loads this library holds until the process exits.
-// Twiddle factors and FFT plans are computed inside the kernels, so nothing else is allocated either.
+// The FFT plans are factorised on the host and passed by value; the twiddle factors are written by a
+// small kernel into a second, 64 KiB file-scope device table at the start of every call, so nothing
+// else is allocated either.
 //
-// The array is shared by every call: a call overwrites every scratch element it later reads, so
-// nothing has to start at zero, but calls that overlap on the GPU (different streams, or different
-// host threads) race on it. Serialise them.
+// The arrays are shared by every call: a call overwrites every scratch and twiddle element it later
+// reads, so nothing has to start at zero, but calls that overlap on the GPU (different streams, or
+// different host threads) race on them. Serialise them.
 #include <cmath>
 #include <mutex>
 #include <string>
 
 #include "pdt_device.cuh"
+#include "pdt_fftplan.h"
 #include "pdt_internal.h"
 
 namespace pdt {
 namespace {
 
 constexpr size_t kNoAllocScratchBytes = size_t(32) << 20;  // 32 MiB
+constexpr int kNoAllocMaxLen = 4096;                        // longest FFT the twiddle table holds
 constexpr int kMaxDevices = 64;
 constexpr int kNaThreads = 256;
 constexpr int kNaRB = 4;  // image rows per block in the row pass
 constexpr int kNaCB = 4;  // k-space columns per block in the column pass
 
 // The scratch itself. In host code this name is only a stand-in for the symbol: its device address
-// comes from cudaGetSymbolAddress (noalloc_scratch_ptr below).
+// comes from cudaGetSymbolAddress (noalloc_device below).
 static __device__ __align__(256) float2 g_noalloc_scratch[kNoAllocScratchBytes / sizeof(float2)];
+// Twiddle factors of the row FFT (first kNoAllocMaxLen entries) and of the column FFT (the rest). Only
+// device code names it.
+static __device__ __align__(256) float2 g_noalloc_tw[2 * kNoAllocMaxLen];
 
+// Per-device set-up, done once under g_noalloc_mu: the scratch's device address and the kernels'
+// shared-memory limit. A cudaDeviceReset invalidates it; the library does not expect one between calls.
+struct NaDevice {
+  float2* scratch = nullptr;
+  bool ready = false;
+};
 std::mutex g_noalloc_mu;
-float2* g_noalloc_ptr[kMaxDevices] = {};
+NaDevice g_noalloc_dev[kMaxDevices];
 
-// Device address of the scratch on the current device, resolved once per device.
-float2* noalloc_scratch_ptr() {
-  int dev = 0;
-  PDT_CUDA_CHECK(cudaGetDevice(&dev));
-  if (dev < 0 || dev >= kMaxDevices) throw Error(PDT_ERR_UNSUPPORTED, "device ordinal out of range");
-  std::lock_guard<std::mutex> lock(g_noalloc_mu);
-  if (!g_noalloc_ptr[dev]) {
-    void* p = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess)
-      throw Error(PDT_ERR_CUDA, std::string("cudaGetSymbolAddress(scratch) failed: ") + cudaGetErrorString(e));
-    g_noalloc_ptr[dev] = static_cast<float2*>(p);
-  }
-  return g_noalloc_ptr[dev];
+// tw[t] = exp(-2 pi i t / n) for the row (n = W) and column (n = H) transforms, in double.
+__global__ void na_twiddles_kernel(int W, int H) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= W + H) return;
+  const int n = i < W ? W : H;
+  const int t = i < W ? i : i - W;
+  double sn, cs;
+  sincospi(-2.0 * (double)t / (double)n, &sn, &cs);
+  g_noalloc_tw[(i < W ? 0 : kNoAllocMaxLen) + t] = c2((float)cs, (float)sn);
 }
 
-// Radix factorisation of n (8s, one 4 or 2, then odd factors) computed in the kernel.
-__device__ bool plan_on_device(int n, FftPlan* pl) {
-  pl->n = n;
-  pl->nst = 0;
-  int m = n;
-  while (m % 8 == 0) {
-    if (pl->nst >= kMaxStages) return false;
-    pl->radix[pl->nst++] = 8;
-    m /= 8;
-  }
-  if (m % 4 == 0) {
-    pl->radix[pl->nst++] = 4;
-    m /= 4;
-  }
-  if (m % 2 == 0) {
-    pl->radix[pl->nst++] = 2;
-    m /= 2;
-  }
-  for (int f = 3; m > 1; f += 2)
-    while (m % f == 0) {
-      if (pl->nst >= kMaxStages) return false;
-      pl->radix[pl->nst++] = f;
-      m /= f;
-    }
-  return true;
-}
-
-// tw[t] = exp(-2 pi i t / n), evaluated in double.
-__device__ void twiddles_on_device(int n, float2* tw) {
-  for (int t = threadIdx.x; t < n; t += blockDim.x) {
-    double s, c;
-    sincospi(-2.0 * (double)t / (double)n, &s, &c);
-    tw[t] = c2((float)c, (float)s);
-  }
+__device__ void load_twiddles(int n, int off, float2* tw) {
+  for (int t = threadIdx.x; t < n; t += blockDim.x) tw[t] = g_noalloc_tw[off + t];
 }
 
 struct NaGeom {
@@ -93,17 +69,15 @@ struct NaGeom {
 };
 
 // Row pass: ubar rows (x sens_c) -> FFT along W -> scratch[c][kx][yi] for every FFT slot kx.
-__global__ void __launch_bounds__(kNaThreads) na_rows_kernel(NaGeom g, const float2* __restrict__ sens,
+__global__ void __launch_bounds__(kNaThreads) na_rows_kernel(NaGeom g, FftPlan plan, const float2* __restrict__ sens,
                                                              const float2* __restrict__ img,
                                                              float2* __restrict__ scratch) {
   extern __shared__ float2 sm[];
-  __shared__ FftPlan plan;
   const int ld = g.W + 1;
   float2* tw = sm;
   float2* A = tw + g.W;
   float2* B = A + kNaRB * ld;
-  if (threadIdx.x == 0) plan_on_device(g.W, &plan);
-  twiddles_on_device(g.W, tw);
+  load_twiddles(g.W, 0, tw);
   const int yi0 = blockIdx.x * kNaRB;
   const int c = blockIdx.y;
   const int nr = min(kNaRB, g.Hi - yi0);
@@ -125,17 +99,15 @@ __global__ void __launch_bounds__(kNaThreads) na_rows_kernel(NaGeom g, const flo
 }
 
 // Column pass: FFT along Hf of every k-space column, orthonormal scale, fftshift, mask -> dense output.
-__global__ void __launch_bounds__(kNaThreads) na_cols_kernel(NaGeom g, const float* __restrict__ mask,
+__global__ void __launch_bounds__(kNaThreads) na_cols_kernel(NaGeom g, FftPlan plan, const float* __restrict__ mask,
                                                              const float2* __restrict__ scratch,
                                                              float2* __restrict__ kspace) {
   extern __shared__ float2 sm[];
-  __shared__ FftPlan plan;
   const int ld = g.Hf + 1;
   float2* tw = sm;
   float2* A = tw + g.Hf;
   float2* B = A + kNaCB * ld;
-  if (threadIdx.x == 0) plan_on_device(g.Hf, &plan);
-  twiddles_on_device(g.Hf, tw);
+  load_twiddles(g.Hf, kNoAllocMaxLen, tw);
   const int k0 = blockIdx.x * kNaCB;
   const int c = blockIdx.y;
   const int ncb = min(kNaCB, g.W - k0);
@@ -158,7 +130,24 @@ __global__ void __launch_bounds__(kNaThreads) na_cols_kernel(NaGeom g, const flo
   }
 }
 
-bool g_na_attr_set[kMaxDevices] = {};
+// Device address of the scratch on the current device; the first call on a device resolves it and
+// raises the kernels' dynamic shared-memory limit, under one lock.
+float2* noalloc_device(int dev, int max_smem) {
+  if (dev < 0 || dev >= kMaxDevices) throw Error(PDT_ERR_UNSUPPORTED, "device ordinal out of range");
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  NaDevice& d = g_noalloc_dev[dev];
+  if (!d.ready) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess)
+      throw Error(PDT_ERR_CUDA, std::string("cudaGetSymbolAddress(scratch) failed: ") + cudaGetErrorString(e));
+    PDT_CUDA_CHECK(cudaFuncSetAttribute(na_rows_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem - 1024));
+    PDT_CUDA_CHECK(cudaFuncSetAttribute(na_cols_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem - 1024));
+    d.scratch = static_cast<float2*>(p);
+    d.ready = true;
+  }
+  return d.scratch;
+}
 
 }  // namespace
 }  // namespace pdt
@@ -192,6 +181,12 @@ extern "C" pdt_status pdt_cartesian_forward_noalloc(int roos, const void* sens, 
       throw Error(PDT_ERR_UNSUPPORTED, "pdt_cartesian_forward_noalloc: coils x W x image rows x 8 bytes = " +
                                            std::to_string(need) + " exceeds the " +
                                            std::to_string(kNoAllocScratchBytes) + "-byte static scratch");
+    if (W > kNoAllocMaxLen || H > kNoAllocMaxLen)
+      throw Error(PDT_ERR_UNSUPPORTED, "pdt_cartesian_forward_noalloc: W and H must be at most " +
+                                           std::to_string(kNoAllocMaxLen));
+    FftPlan plan_w, plan_h;
+    if (!make_fft_plan(W, &plan_w) || !make_fft_plan(H, &plan_h))
+      throw Error(PDT_ERR_UNSUPPORTED, "pdt_cartesian_forward_noalloc: no FFT plan for these lengths");
     const size_t smem_rows = sizeof(float2) * ((size_t)W + 2 * (size_t)kNaRB * (W + 1));
     const size_t smem_cols = sizeof(float2) * ((size_t)H + 2 * (size_t)kNaCB * (H + 1));
     int dev = 0, max_smem = 0;
@@ -199,19 +194,17 @@ extern "C" pdt_status pdt_cartesian_forward_noalloc(int roos, const void* sens, 
     PDT_CUDA_CHECK(cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
     if (smem_rows > (size_t)max_smem - 1024 || smem_cols > (size_t)max_smem - 1024)
       throw Error(PDT_ERR_UNSUPPORTED, "pdt_cartesian_forward_noalloc: FFT length too large for shared memory");
-    float2* scratch = noalloc_scratch_ptr();
-    if (dev < kMaxDevices && !g_na_attr_set[dev]) {
-      PDT_CUDA_CHECK(cudaFuncSetAttribute(na_rows_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem - 1024));
-      PDT_CUDA_CHECK(cudaFuncSetAttribute(na_cols_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem - 1024));
-      g_na_attr_set[dev] = true;
-    }
+    float2* scratch = noalloc_device(dev, max_smem);
     cudaStream_t st = static_cast<cudaStream_t>(stream);
+    na_twiddles_kernel<<<(W + H + 255) / 256, 256, 0, st>>>(W, H);
+    PDT_LAUNCH_CHECK();
+    count_launch();
     na_rows_kernel<<<dim3((g.Hi + kNaRB - 1) / kNaRB, C), kNaThreads, smem_rows, st>>>(
-        g, static_cast<const float2*>(sens), static_cast<const float2*>(img), scratch);
+        g, plan_w, static_cast<const float2*>(sens), static_cast<const float2*>(img), scratch);
     PDT_LAUNCH_CHECK();
     count_launch();
     na_cols_kernel<<<dim3((W + kNaCB - 1) / kNaCB, C), kNaThreads, smem_cols, st>>>(
-        g, static_cast<const float*>(mask), scratch, static_cast<float2*>(kspace));
+        g, plan_h, static_cast<const float*>(mask), scratch, static_cast<float2*>(kspace));
     PDT_LAUNCH_CHECK();
     count_launch();
     return PDT_OK;

@@ -13,7 +13,9 @@ import sys
 import numpy as np
 
 here = os.path.dirname(os.path.abspath(__file__))
-ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+if len(sys.argv) != 2:
+    sys.exit("usage: python tests/golden/make_golden.py <path of the reference checkout>")
+ref = sys.argv[1]
 data = os.path.join(ref, "data")
 
 for name in ("random4", "regular4"):
