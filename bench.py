@@ -261,6 +261,7 @@ def run_ours(args):
         wall = time.perf_counter() - t0
     launches = pdt.launch_count() - n0
     dev_s = ev0.elapsed_time(ev1) / 1e3
+    parity = _parity_fp64(case, opt.getResult()) if rank == 0 else None
     t_max = max_over_ranks(dev_s, dist)
     value = replica_throughput(ITERS, args.steps, world, t_max)
 
@@ -386,6 +387,7 @@ def run_ours(args):
             "phases": phase_info,
             "tuning": tuning,
             "cpu_baseline": cpu,
+            "parity": parity,
             "time_to_1e-4": conv,
             "e2e_streamed": streamed,
             "batched": batched,
@@ -510,6 +512,28 @@ def _khr_planes(tuning):
     return 1 if m.group(2) == ",cluster" else int(m.group(1))
 
 
+FP64_FIXTURE = os.path.join(ROOT, "tests", "golden", "config2_fp64.npz")
+
+
+def _parity_fp64(case, u):
+    """rel-L2 of the timed solve's result to the FP64 CPU oracle's result of the same 1001 iterations on the
+    same inputs (tests/golden/config2_fp64.npz, written by tests/golden/make_config2_fp64.py)."""
+    import hashlib
+
+    if not os.path.exists(FP64_FIXTURE):
+        return {"unavailable": "tests/golden/config2_fp64.npz is missing"}
+    z = np.load(FP64_FIXTURE)
+    h = hashlib.sha256()
+    for k in ("rawdata", "sens", "mask"):
+        h.update(np.ascontiguousarray(case[k]).tobytes())
+    ref = z["u"].astype(np.complex128)
+    err = float(np.linalg.norm(u.astype(np.complex128) - ref) / np.linalg.norm(ref))
+    return {"rel_l2_fp64": err, "tolerance": 1e-4, "pass": bool(err <= 1e-4),
+            "oracle": f"FP64 CPU oracle, the same {int(z['max_iter']) + 1} iterations from the same inputs "
+                      f"(tests/golden/config2_fp64.npz: {float(z['seconds']):.0f} s on {int(z['threads'])} threads)",
+            "inputs_identical_to_oracle_run": h.hexdigest() == str(z["inputs_sha256"])}
+
+
 def _cpu_baseline(case, seconds=10.0, threads=None):
     """The reference iteration on the host cores: the CPU oracle restatement (FP32 mirror), all threads."""
     from oracle import oracle
@@ -527,7 +551,14 @@ def _cpu_baseline(case, seconds=10.0, threads=None):
 
     n = max(2, int(seconds / max(run(2) / 2, 1e-3)))
     dt = run(n)
-    return {"value": round(n / dt, 3), "unit": "iters/s", "cores": threads, "kind": "port",
+    # the FP64 oracle of the same iteration (the precision the parity figure is measured against)
+    t0 = time.perf_counter()
+    n64 = max(2, n // 3)
+    oracle.op_solve("cartesian_roos", case["sens"], case["mask"], case["rawdata"], "tgv_mri", alpha0=case["alpha0"],
+                    alpha1=case["alpha1"], reduction=REDUCTION, max_iter=n64 - 1, u0=u0.astype(np.complex128),
+                    prec=64)
+    fp64 = {"value": round(n64 / (time.perf_counter() - t0), 3), "unit": "iters/s", "iterations": n64}
+    return {"value": round(n / dt, 3), "unit": "iters/s", "cores": threads, "kind": "port", "fp64": fp64,
             "sample": f"the first {n} of the {ITERS} iterations of one solve from u0 = A^H f (the one-off A^H f, "
                       f"about one iteration's operator work, outside the sample), FP32 mirror of the reference "
                       f"iteration"}

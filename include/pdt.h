@@ -155,8 +155,14 @@ PDT_API pdt_status pdt_opt_set_noisy_data(pdt_opt* opt, const void* f, int ndim,
 PDT_API pdt_status pdt_opt_set_input0(pdt_opt* opt, const void* u0, int ndim, const int64_t* size, int is_device,
                               void* stream);
 /* solve (tgvmrioptimizer.cu:93-203, tvoptimizer.cu:76-125, tgvoptimizer.cu:80-141, ...): runs
- * max_iter + 1 iterations from the current state (u0 = A^H f or f when no state is set). */
+ * max_iter + 1 iterations from the current state (u0 = A^H f or f when no state is set). The
+ * with-operator solvers check every new u and v for NaN and Inf on the device; with a NULL stream the
+ * call returns PDT_ERR_NUMERIC when one appeared (the state then holds the non-finite iterate). */
 PDT_API pdt_status pdt_opt_solve(pdt_opt* opt, int verbose, void* stream);
+/* No counterpart in the reference: the non-finite check of solves enqueued on an explicit stream. Waits
+ * for `stream`, returns PDT_ERR_NUMERIC if a NaN or Inf appeared in u or v since the last check (and
+ * clears the flag), else PDT_OK. */
+PDT_API pdt_status pdt_opt_status(pdt_opt* opt, void* stream);
 /* getResult (tgvmrioptimizer.cu:48-52): size query, then a copy of u into dst. */
 PDT_API pdt_status pdt_opt_result_size(pdt_opt* opt, int* ndim, int64_t* size);
 PDT_API pdt_status pdt_opt_get_result(pdt_opt* opt, void* dst, int is_device, void* stream);
@@ -172,8 +178,18 @@ PDT_API pdt_status pdt_opt_profile(pdt_opt* opt, int iters, void* stream, int ma
  * each the size of u0; v0 may be NULL); p = q = 0. */
 PDT_API pdt_status pdt_opt_set_input0_uv(pdt_opt* opt, const void* u0, const void* v0, int ndim, const int64_t* size,
                                          int is_device, void* stream);
-/* Copies one state plane: 0 u, 1 u-bar, 2 vx, 3 vy, 4 v-bar x, 5 v-bar y, 6 px, 7 py, 8 qxx, 9 qyy, 10 qxy. */
+/* Copies one state plane: 0 u, 1 u-bar, 2 vx, 3 vy, 4 v-bar x, 5 v-bar y, 6 px, 7 py, 8 qxx, 9 qyy, 10 qxy
+ * (each the size of u), or 11 the k-space dual r of a with-operator optimizer (the size of the noisy data,
+ * in its layout; entries on phase-encode lines the mask never samples are not held and read as 0).
+ * The reference keeps this state in TgvMriOptimizer's members u_, u__, v_, v__, p_, q_, r_
+ * (tgvmrioptimizer.h:121-140) and has no accessor for it. */
 PDT_API pdt_status pdt_opt_get_field(pdt_opt* opt, int field, void* dst, int is_device, void* stream);
+/* Replaces one state plane (the fields of pdt_opt_get_field): planes 0-10 need an existing state
+ * (setInput0 or a solve first), r needs the operator and the noisy data. The next solve() continues
+ * from the new state, so exporting every field and importing it into a fresh optimizer resumes a solve
+ * exactly. No counterpart in the reference, whose setInput0 / setNoisyData reset v, p, q and r to 0
+ * (tgvmrioptimizer.cu:62-91). */
+PDT_API pdt_status pdt_opt_set_field(pdt_opt* opt, int field, const void* src, int is_device, void* stream);
 /* Energy of the current state accumulated in FP64: out = {total, data, first-order, second-order} --
  * 1/2 ||K u - f||^2 + alpha1 sum |grad u - v| + alpha0 sum |eps(v)| (TGV-MRI at its final alpha); the
  * TGV / TV with-operator optimizers weight the data term 1 / (2 lambda) (their r-prox), the denoising
@@ -219,6 +235,15 @@ PDT_API pdt_status pdt_batch_create(pdt_batch** out);
 PDT_API pdt_status pdt_batch_destroy(pdt_batch* b);
 PDT_API pdt_status pdt_batch_add(pdt_batch* b, pdt_opt* opt);
 PDT_API pdt_status pdt_batch_solve(pdt_batch* b, int verbose, void* stream);
+
+/* ---- test hook (no counterpart in the reference) ------------------------------------------------- */
+/* Every wait of the tensor-core kernels on an mbarrier is bounded (200 ms); a kernel that gives up
+ * records an error word, waits (bounded) for its own copies and MMAs in flight, frees its tensor memory
+ * and returns, and the next synchronous call raises PDT_ERR_TIMEOUT. With on != 0 those kernels
+ * withhold one arrival (an operand barrier of the Cartesian tensor-core row passes; the first tile's
+ * MMA commit of block 0 of a tensor-core convolution), so that tests can run the give-up path; 0
+ * restores normal operation. Call it only while none of those kernels run. */
+PDT_API pdt_status pdt_debug_drop_arrival(int on);
 
 /* ---- allocation-free entry point ---------------------------------------------------------------- */
 /* No counterpart in the reference. The Cartesian forward operator (MriCartesianOperator, or with

@@ -259,6 +259,7 @@ static void run_iterations(IterGraph& g, uint64_t key, int n, int n_per_graph,
 // Optimizers
 // ------------------------------------------------------------------------------------------------
 enum Field { F_U, F_UB, F_VX, F_VY, F_VBX, F_VBY, F_PX, F_PY, F_QXX, F_QYY, F_QXY, F_COUNT };
+constexpr int F_R = F_COUNT;  // the k-space dual r (with-operator optimizers), dense user layout
 
 class OptImpl {
  public:
@@ -336,12 +337,58 @@ class OptImpl {
     }
   }
 
+  // One plane of the state (0..10), or with F_R the k-space dual r in the user's dense k-space layout.
   void get_field(int f, void* dst, bool is_device, cudaStream_t st) {
     if (!has_state_) throw Error(PDT_ERR_STATE, "There is no result yet!");
+    if (f == F_R) {
+      SolverHooks* hk = r_hooks(st);
+      if (r_reset_ || r_.bytes != std::max<size_t>(hk->compact_elems(), 1) * sizeof(float2))
+        throw Error(PDT_ERR_STATE, "There is no dual state yet: solve() first");
+      const size_t bytes = numel_of(fsize_) * sizeof(float2);
+      if (is_device) {
+        hk->scatter(r_.as<float2>(), static_cast<float2*>(dst), st);
+      } else {
+        DevBuf tmp;
+        tmp.ensure(std::max<size_t>(bytes, 1));
+        hk->scatter(r_.as<float2>(), tmp.as<float2>(), st);
+        PDT_CUDA_CHECK(cudaMemcpyAsync(dst, tmp.p, bytes, cudaMemcpyDeviceToHost, st));
+        PDT_CUDA_CHECK(cudaStreamSynchronize(st));
+      }
+      return;
+    }
     if (f < 0 || f >= F_COUNT) throw Error(PDT_ERR_INVALID_ARGUMENT, "unknown field");
     PDT_CUDA_CHECK(cudaMemcpyAsync(dst, field(f, parity_), plane_bytes(),
                                    is_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, st));
     if (!is_device) PDT_CUDA_CHECK(cudaStreamSynchronize(st));
+  }
+
+  // Replaces one plane of the state (0..10; a state must exist: setInput0 or a solve first), or with
+  // F_R the k-space dual r from the user's dense k-space layout (entries on phase-encode lines the mask
+  // never samples are not held: they never reach u). The next solve() continues from the new state.
+  void set_field(int f, const void* src, bool is_device, cudaStream_t st) {
+    if (f == F_R) {
+      SolverHooks* hk = r_hooks(st);
+      const size_t nk = hk->compact_elems();
+      if (r_.bytes != std::max<size_t>(nk, 1) * sizeof(float2)) {
+        r_.ensure(std::max<size_t>(nk, 1) * sizeof(float2));
+        ++version_;
+      }
+      const size_t bytes = numel_of(fsize_) * sizeof(float2);
+      if (is_device) {
+        hk->gather(static_cast<const float2*>(src), r_.as<float2>(), st);
+      } else {
+        DevBuf tmp;
+        tmp.ensure(std::max<size_t>(bytes, 1));
+        PDT_CUDA_CHECK(cudaMemcpyAsync(tmp.p, src, bytes, cudaMemcpyHostToDevice, st));
+        hk->gather(tmp.as<float2>(), r_.as<float2>(), st);
+        PDT_CUDA_CHECK(cudaStreamSynchronize(st));
+      }
+      r_reset_ = false;
+      return;
+    }
+    if (f < 0 || f >= F_COUNT) throw Error(PDT_ERR_INVALID_ARGUMENT, "unknown field");
+    if (!has_state_) throw Error(PDT_ERR_STATE, "There is no state yet: setInput0 or solve() first");
+    copy_in(field(f, parity_), src, plane_bytes(), is_device, st);
   }
 
   // Energy of the current primal state in FP64: out = {total, data term, first-order term, second-order term}.
@@ -457,6 +504,31 @@ class OptImpl {
     if (!has_state_) throw Error(PDT_ERR_STATE, "There is no result yet!");
     return usize_;
   }
+  // Reads and clears the with-operator solvers' non-finite flag (word 2 of the alpha table's header, set
+  // by the primal kernel when a new u or v is NaN or infinite); throws PDT_ERR_NUMERIC if it was set.
+  // Waits for `st`. The reference has no such check (its solve loop only checks launches,
+  // tgvmrioptimizer.cu:163-198).
+  void check_numeric(cudaStream_t st) {
+    if (!with_op() || !alpha_.p) return;
+    int* w = alpha_.as<int>() + 2;
+    int flag = 0;
+    PDT_CUDA_CHECK(cudaMemcpyAsync(&flag, w, sizeof(int), cudaMemcpyDeviceToHost, st));
+    PDT_CUDA_CHECK(cudaStreamSynchronize(st));
+    if (!flag) return;
+    PDT_CUDA_CHECK(cudaMemsetAsync(w, 0, sizeof(int), st));
+    PDT_CUDA_CHECK(cudaStreamSynchronize(st));
+    throw Error(PDT_ERR_NUMERIC, "Non-finite values (NaN or Inf) appeared in the primal variables: check the noisy "
+                                 "data, the operator's constants and the parameters");
+  }
+
+  // Everything the solve's kernels report on the device: a bounded wait of the operator's kernels that
+  // gave up (PDT_ERR_TIMEOUT) first, then the non-finite flag (PDT_ERR_NUMERIC). Waits for `st`.
+  void check_device(cudaStream_t st) {
+    PDT_CUDA_CHECK(cudaStreamSynchronize(st));
+    if (op_) op_->check_device_errors();
+    check_numeric(st);
+  }
+
   void get_result(void* dst, bool is_device, cudaStream_t st) {
     if (!has_state_) throw Error(PDT_ERR_STATE, "There is no result yet!");
     const size_t bytes = plane_bytes();
@@ -516,6 +588,15 @@ class OptImpl {
       }
     }
     for (auto& v : ms) v /= iters;
+  }
+
+  // The operator hooks that hold r, after the checks a k-space dual needs.
+  SolverHooks* r_hooks(cudaStream_t st) {
+    if (!with_op()) throw Error(PDT_ERR_INVALID_ARGUMENT, "only the with-operator optimizers have a k-space dual");
+    check_ready();
+    SolverHooks* hk = op_->hooks();
+    ensure_fc(hk, st);
+    return hk;
   }
 
   // Streams are created on first use so that handles can be made (and misused) without a device.
@@ -855,6 +936,17 @@ class BatchImpl {
     opts_.push_back(o);
   }
   size_t size() const { return opts_.size(); }
+  // Raises the first problem's device report (and clears every problem's).
+  void check_device(cudaStream_t st) {
+    std::string first;
+    pdt_status code = PDT_OK;
+    for (OptImpl* o : opts_) try {
+        o->check_device(st);
+      } catch (const Error& e) {
+        if (first.empty()) first = e.what(), code = e.code;
+      }
+    if (!first.empty()) throw Error(code, first);
+  }
 
   void solve(bool verbose, cudaStream_t st) {
     if (opts_.empty()) return;
@@ -1120,6 +1212,7 @@ static pdt_status op_apply(bool adjoint, pdt_op* op, const void* src, int src_nd
       op->impl->forward(s, ds, bd.as<float2>(), dd, st);
     if (db) PDT_CUDA_CHECK(cudaMemcpyAsync(dst, bd.p, db, cudaMemcpyDeviceToHost, st));
     PDT_CUDA_CHECK(cudaStreamSynchronize(st));
+    op->impl->check_device_errors();
   });
 }
 
@@ -1266,7 +1359,24 @@ pdt_status pdt_opt_solve(pdt_opt* opt, int verbose, void* stream) {
     opt->impl->check_ready();
     cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : opt->impl->own_stream();
     opt->impl->solve(verbose != 0, st);
-    if (!stream) PDT_CUDA_CHECK(cudaStreamSynchronize(st));
+    if (!stream) {
+      PDT_CUDA_CHECK(cudaStreamSynchronize(st));
+      opt->impl->check_device(st);
+    }
+  });
+}
+
+pdt_status pdt_debug_drop_arrival(int on) {
+  return guarded([&] {
+    cartesian_set_drop_arrival(on);
+    cnn_set_drop_arrival(on);
+  });
+}
+
+pdt_status pdt_opt_status(pdt_opt* opt, void* stream) {
+  return guarded([&] {
+    need(opt, "optimizer");
+    opt->impl->check_device(stream ? static_cast<cudaStream_t>(stream) : opt->impl->own_stream());
   });
 }
 
@@ -1311,6 +1421,16 @@ pdt_status pdt_opt_get_field(pdt_opt* opt, int field, void* dst, int is_device, 
     opt->impl->result_size();
     cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : opt->impl->own_stream();
     opt->impl->get_field(field, dst, is_device != 0, st);
+    if (!stream) PDT_CUDA_CHECK(cudaStreamSynchronize(st));
+  });
+}
+
+pdt_status pdt_opt_set_field(pdt_opt* opt, int field, const void* src, int is_device, void* stream) {
+  return guarded([&] {
+    need(opt, "optimizer");
+    need(src, "source");
+    cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : opt->impl->own_stream();
+    opt->impl->set_field(field, src, is_device != 0, st);
     if (!stream) PDT_CUDA_CHECK(cudaStreamSynchronize(st));
   });
 }
@@ -1399,7 +1519,10 @@ pdt_status pdt_batch_solve(pdt_batch* b, int verbose, void* stream) {
     need(b, "batch");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     b->impl->solve(verbose != 0, st);
-    if (!stream) PDT_CUDA_CHECK(cudaStreamSynchronize(st));
+    if (!stream) {
+      PDT_CUDA_CHECK(cudaStreamSynchronize(st));
+      b->impl->check_device(st);
+    }
   });
 }
 

@@ -54,8 +54,9 @@ __device__ __forceinline__ float4 tc_cmulc2(float4 a, float4 b) {  // a . conj(b
 // Stage layout in shared memory (bytes from the 1024-aligned base): [A hi | A lo | B hi | B lo] per
 // stage, two stages, then the kernel's tables.
 __host__ __device__ inline uint32_t tc_stage_bytes(int nbmax) { return 2 * kTcTileA + 2u * (uint32_t)nbmax * 128u; }
-inline size_t tc_adj_smem(int NB, int nst) { return 1024 + (size_t)nst * tc_stage_bytes(NB) + 16 * kTcMaxStages + 32; }
-inline size_t tc_fwd_smem(int nb, int nst) { return 1024 + (size_t)nst * tc_stage_bytes(nb) + 16 * kTcMaxStages + 32; }
+// barriers after the stages: full, empty and copy (8 bytes each per stage), accb, the TMEM slot
+inline size_t tc_adj_smem(int NB, int nst) { return 1024 + (size_t)nst * tc_stage_bytes(NB) + 24 * kTcMaxStages + 32; }
+inline size_t tc_fwd_smem(int nb, int nst) { return 1024 + (size_t)nst * tc_stage_bytes(nb) + 24 * kTcMaxStages + 32; }
 
 // Issues the MMAs of one staged K chunk (ksteps <= 4 steps of K = 8) and commits them to `bar`.
 __device__ __forceinline__ void tc_issue_chunk(uint32_t tmem, uint32_t a_hi, uint32_t a_lo, uint32_t b_hi,
@@ -87,6 +88,18 @@ constexpr int kTcStageItems = (kTcRows * 8 + kTcStagers - 1) / kTcStagers;  // s
 constexpr int kTcAdjMaxNB = 256;    // output columns (re/im) per CTA
 constexpr int kTcCoilUnroll = 16;   // coil-sum loads issued together
 
+// Thread 0 waits until the DFT-factor copies it started (chunks 0 .. issued-1, stage j % nst) have
+// landed, so that no copy into this CTA's shared memory is still in flight when the CTA reuses it or
+// exits -- after a wait gave up the MMA thread may not have consumed them. A copy into a stage starts
+// only after the MMAs of the stage's previous chunk, hence after that chunk's copy phase completed, so
+// only each stage's last phase can be pending.
+__device__ __forceinline__ void copies_drain(uint64_t* copied, int issued, int nst, int* err) {
+  for (int b = 0; b < nst && b < issued; ++b) {
+    const int j = b + ((issued - 1 - b) / nst) * nst;  // last chunk copied into stage b
+    if (!tc::mbar_wait(&copied[b], (j / nst) & 1)) atomicCAS(err, 0, 0x600 | j);
+  }
+}
+
 template <bool SENS>
 __global__ void __launch_bounds__(kTcAdjThreads, 1) tc_rows_adj(CartDev d, const float2* __restrict__ t2,
                                                              const unsigned char* __restrict__ btiles,
@@ -108,9 +121,10 @@ __global__ void __launch_bounds__(kTcAdjThreads, 1) tc_rows_adj(CartDev d, const
   unsigned char* sm = tc_align1024(tc_smem_raw);
   const int W = d.W, ns = d.ns, Hi = d.Hi, C = d.C, yb = d.tc_yb;
   const uint32_t stage_bytes = tc_stage_bytes(NB);
-  uint64_t* full = reinterpret_cast<uint64_t*>(sm + nst * stage_bytes);  // B copies + A stores landed
+  uint64_t* full = reinterpret_cast<uint64_t*>(sm + nst * stage_bytes);  // A stores of a stage landed
   uint64_t* empty = full + kTcMaxStages;                                  // MMAs of a stage done
-  uint64_t* accb = empty + kTcMaxStages;                                  // every MMA done (one phase)
+  uint64_t* copied = empty + kTcMaxStages;                                // B copy of a stage landed
+  uint64_t* accb = copied + kTcMaxStages;                                 // every MMA done (one phase)
   uint32_t* tslot = reinterpret_cast<uint32_t*>(accb + 1);
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -123,8 +137,9 @@ __global__ void __launch_bounds__(kTcAdjThreads, 1) tc_rows_adj(CartDev d, const
 
   if (tid == 0) {
     for (int i = 0; i < nst; ++i) {
-      tc::mbar_init(&full[i], 1 + kTcStagers / 32);
+      tc::mbar_init(&full[i], kTcStagers / 32);
       tc::mbar_init(&empty[i], 1);
+      tc::mbar_init(&copied[i], 1);
     }
     tc::mbar_init(accb, 1);
     tc::fence_mbar_init();
@@ -139,6 +154,8 @@ __global__ void __launch_bounds__(kTcAdjThreads, 1) tc_rows_adj(CartDev d, const
   const uint32_t bbytes = 2u * (uint32_t)nb * 128u;
   const unsigned char* bsrc = btiles + (size_t)blockIdx.x * nch * 2 * NB * 128;
   bool ok = true;
+  int issued = 0;  // DFT-factor chunks whose copies thread 0 has started
+  const bool drop = tc::g_drop_arrival != 0;
   if (tid == 0) {  // DFT-factor tiles (constants: the first copies may start before the column kernel ends)
     for (int j = 0; j < nch && ok; ++j) {
       const int b = j % nst;
@@ -147,8 +164,9 @@ __global__ void __launch_bounds__(kTcAdjThreads, 1) tc_rows_adj(CartDev d, const
         atomicCAS(err, 0, 0x100 | j);
         break;
       }
-      tc::mbar_arrive_expect_tx(&full[b], bbytes);
-      tc::bulk_g2s(base + b * stage_bytes + 2 * kTcTileA, bsrc + (size_t)j * 2 * NB * 128, bbytes, &full[b]);
+      tc::mbar_arrive_expect_tx(&copied[b], bbytes);
+      tc::bulk_g2s(base + b * stage_bytes + 2 * kTcTileA, bsrc + (size_t)j * 2 * NB * 128, bbytes, &copied[b]);
+      issued = j + 1;
     }
   }
   pdl_wait();  // every thread: t2 comes from the column kernel
@@ -157,7 +175,7 @@ __global__ void __launch_bounds__(kTcAdjThreads, 1) tc_rows_adj(CartDev d, const
     const uint32_t idesc = tc::idesc_tf32(kTcRows, nb);
     for (int j = 0; j < nch && ok; ++j) {
       const int b = j % nst;
-      ok = tc::mbar_wait(&full[b], (j / nst) & 1);
+      ok = tc::mbar_wait(&full[b], (j / nst) & 1) && tc::mbar_wait(&copied[b], (j / nst) & 1);
       if (!ok) {
         atomicCAS(err, 0, 0x200 | j);  // the MMA thread gave up waiting for chunk j's operands
         break;
@@ -231,9 +249,10 @@ __global__ void __launch_bounds__(kTcAdjThreads, 1) tc_rows_adj(CartDev d, const
       }
       tc::fence_async_smem();
       __syncwarp();
-      if (lane == 0) tc::mbar_arrive(&full[b]);  // one arrival per staging warp
+      if (lane == 0 && !(drop && j == 0 && warp == 2)) tc::mbar_arrive(&full[b]);  // one arrival per staging warp
     }
   }
+  if (tid == 0) copies_drain(copied, issued, nst, err);
 
   // coil-map values of this thread's first output item: the other threads load them while the MMAs run
   const int yrows = min(yb, Hi - ybase);  // image rows of this tile
@@ -337,9 +356,10 @@ __global__ void __launch_bounds__(kTcFwdThreads, 1) tc_rows_fwd(CartDev d, const
   const int nb = (2 * nsl + 15) & ~15;
   const int nbmax = (2 * min(128, ns) + 15) & ~15;  // B tile stride of the precomputed tiles
   const uint32_t stage_bytes = tc_stage_bytes(nb);
-  uint64_t* full = reinterpret_cast<uint64_t*>(sm + nst * stage_bytes);  // B copies + A stores landed
+  uint64_t* full = reinterpret_cast<uint64_t*>(sm + nst * stage_bytes);  // A stores of a stage landed
   uint64_t* empty = full + kTcMaxStages;                                  // MMAs of a stage done
-  uint64_t* accb = empty + kTcMaxStages;                                  // every MMA done (one phase)
+  uint64_t* copied = empty + kTcMaxStages;                                // B copy of a stage landed
+  uint64_t* accb = copied + kTcMaxStages;                                 // every MMA done (one phase)
   uint32_t* tslot = reinterpret_cast<uint32_t*>(accb + 1);
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -350,8 +370,9 @@ __global__ void __launch_bounds__(kTcFwdThreads, 1) tc_rows_fwd(CartDev d, const
 
   if (tid == 0) {
     for (int i = 0; i < nst; ++i) {
-      tc::mbar_init(&full[i], 1 + kTcFwdStagers / 32);
+      tc::mbar_init(&full[i], kTcFwdStagers / 32);
       tc::mbar_init(&empty[i], 1);
+      tc::mbar_init(&copied[i], 1);
     }
     tc::mbar_init(accb, 1);
     tc::fence_mbar_init();
@@ -366,6 +387,8 @@ __global__ void __launch_bounds__(kTcFwdThreads, 1) tc_rows_fwd(CartDev d, const
   const unsigned char* bsrc = btiles + ((size_t)blockIdx.z * nchT + jb) * 2 * nbmax * 128;
 
   bool ok = true;
+  int issued = 0;  // DFT-factor chunks whose copies thread 0 has started
+  const bool drop = tc::g_drop_arrival != 0;
   if (tid == 0) {  // DFT-factor tiles (constants, may start before the previous kernel ends)
     for (int jl = 0; jl < nch && ok; ++jl) {
       const int b = jl % nst;
@@ -374,8 +397,10 @@ __global__ void __launch_bounds__(kTcFwdThreads, 1) tc_rows_fwd(CartDev d, const
         atomicCAS(err, 0, 0x1100 | jl);
         break;
       }
-      tc::mbar_arrive_expect_tx(&full[b], bbytes);
-      tc::bulk_g2s(base + b * stage_bytes + 2 * kTcTileA, bsrc + (size_t)jl * 2 * nbmax * 128, bbytes, &full[b]);
+      tc::mbar_arrive_expect_tx(&copied[b], bbytes);
+      tc::bulk_g2s(base + b * stage_bytes + 2 * kTcTileA, bsrc + (size_t)jl * 2 * nbmax * 128, bbytes,
+                   &copied[b]);
+      issued = jl + 1;
     }
   }
   pdl_wait();  // every thread: ubar comes from the previous kernel; t1 may still be read by it
@@ -385,7 +410,7 @@ __global__ void __launch_bounds__(kTcFwdThreads, 1) tc_rows_fwd(CartDev d, const
     const uint32_t idesc = tc::idesc_tf32(kTcRows, nb);
     for (int jl = 0; jl < nch && ok; ++jl) {
       const int b = jl % nst;
-      ok = tc::mbar_wait(&full[b], (jl / nst) & 1);
+      ok = tc::mbar_wait(&full[b], (jl / nst) & 1) && tc::mbar_wait(&copied[b], (jl / nst) & 1);
       if (!ok) {
         atomicCAS(err, 0, 0x1200 | jl);
         break;
@@ -462,9 +487,10 @@ __global__ void __launch_bounds__(kTcFwdThreads, 1) tc_rows_fwd(CartDev d, const
       }
       tc::fence_async_smem();
       __syncwarp();
-      if (lane == 0) tc::mbar_arrive(&full[b]);  // one arrival per staging warp
+      if (lane == 0 && !(drop && jl == 0 && warp == 2)) tc::mbar_arrive(&full[b]);  // one arrival per staging warp
     }
   }
+  if (tid == 0) copies_drain(copied, issued, nst, err);
   const bool done = __syncthreads_and(ok);
   tc::fence_after_sync();
   // accumulator -> shared memory as complex values [sl][tile row] (a warp's rows are consecutive); the

@@ -220,6 +220,18 @@ __global__ void gather_kernel(CartDev d, const float2* __restrict__ dense, float
   }
 }
 
+// compact [c][s][Hf] -> dense user k-space (W, Hf, C); the caller zeroes the unsampled columns first
+__global__ void scatter_kernel(CartDev d, const float2* __restrict__ compact, float2* __restrict__ dense) {
+  const size_t n = (size_t)d.C * d.ns * d.Hf;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const int P = (int)(i % d.Hf);
+    const int ypos = d.kperm ? d.kperm[P] : P;
+    const size_t cs = i / d.Hf;
+    const int s = (int)(cs % d.ns), c = (int)(cs / d.ns);
+    dense[((size_t)c * d.Hf + ypos) * d.W + d.col_x[s]] = compact[i];
+  }
+}
+
 size_t rows_smem(const CartDev& d, bool with_acc) {
   return sizeof(float2) * ((size_t)d.W + 2 * (size_t)d.RB * d.ldW + (with_acc ? (size_t)d.RB * d.W : 0));
 }
@@ -271,14 +283,17 @@ class CartesianOp : public OpImpl, public SolverHooks {
     return constant(0, PDT_C64, 3).size;
   }
   SolverHooks* hooks() override { return this; }
-  std::string tuning() override {
-    prepare();
+  void check_device_errors() override {
     if (const int e = take_tc_error()) {
       char code[16];
       std::snprintf(code, sizeof code, "0x%x", e);
       throw Error(PDT_ERR_TIMEOUT, name_ + ": a tensor-core row kernel gave up a bounded wait (code " + code +
                                        "); results since the last check are not valid");
     }
+  }
+  std::string tuning() override {
+    prepare();
+    check_device_errors();
     std::ostringstream os;
     os << "W=" << dev_.W << " H=" << dev_.Hf << " C=" << dev_.C << " sampled_columns=" << dev_.ns;
     if (tune_.tcf)
@@ -327,6 +342,16 @@ class CartesianOp : public OpImpl, public SolverHooks {
     const size_t n = (size_t)dev_.C * dev_.ns * dev_.Hf;
     const int blocks = (int)std::min<size_t>((n + 255) / 256, 4096);
     gather_kernel<<<blocks, 256, 0, st>>>(dev_, dense, compact);
+    PDT_LAUNCH_CHECK();
+    count_launch();
+  }
+  void scatter(const float2* compact, float2* dense, cudaStream_t st) override {
+    prepare();
+    launch_fill_zero(dense, sizeof(float2) * (size_t)dev_.C * dev_.Hf * dev_.W, st);
+    if (dev_.ns == 0) return;
+    const size_t n = (size_t)dev_.C * dev_.ns * dev_.Hf;
+    const int blocks = (int)std::min<size_t>((n + 255) / 256, 4096);
+    scatter_kernel<<<blocks, 256, 0, st>>>(dev_, compact, dense);
     PDT_LAUNCH_CHECK();
     count_launch();
   }
@@ -936,5 +961,7 @@ class CartesianOp : public OpImpl, public SolverHooks {
 };
 
 std::shared_ptr<OpImpl> make_cartesian_operator(pdt_op_kind kind) { return std::make_shared<CartesianOp>(kind); }
+
+void cartesian_set_drop_arrival(int on) { PDT_CUDA_CHECK(tc::set_drop_arrival(on)); }
 
 }  // namespace pdt

@@ -130,7 +130,8 @@ __global__ void __launch_bounds__(kConvTcThreads) conv3x3_tc(const bf16* __restr
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
-    if (tid == 0) {
+    // (the test hook withholds block 0's first tile: no MMAs and no commit, so the wait below runs out)
+    if (tid == 0 && !(it == 0 && blockIdx.x == 0 && tc::g_drop_arrival)) {
       const uint32_t idesc = tc::idesc_bf16(128, CH);
       for (int tap = 0; tap < NTAP; ++tap) {
         const uint32_t a0 = in_base + 16 * ((tap / 3) * (kConvTcTW + 2) + tap % 3);
@@ -141,6 +142,9 @@ __global__ void __launch_bounds__(kConvTcThreads) conv3x3_tc(const bf16* __restr
       tc::mma_commit(bar);
     }
     ok = tc::mbar_wait(bar, it & 1);  // every thread waits each phase in turn
+    // after a give-up, wait once more (bounded) for MMAs still in flight before the tile buffer, the
+    // accumulator and finally the tensor memory are released
+    if (!ok) tc::mbar_wait(bar, it & 1);
     tc::fence_after_sync();
     float v[16];
     tc::tmem_ld16(tmem + ((uint32_t)(32 * q) << 16) + 16 * h, v);
@@ -870,6 +874,8 @@ class WarmStartCnn {
   int B_n_ = 0, H_n_ = 0, W_n_ = 0;
   long step_ = 0;
 };
+
+void cnn_set_drop_arrival(int on) { PDT_CUDA_CHECK(tc::set_drop_arrival(on)); }
 
 }  // namespace pdt
 

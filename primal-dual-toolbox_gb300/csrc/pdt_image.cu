@@ -273,7 +273,9 @@ __global__ void __launch_bounds__(NT) tgv_denoise_step_kernel(int W, int H, ImgP
 //   primal  u+ = u + tau (div- p - K^H r),            v+ = v + tau (div_h- q + p)       (p, q from out)
 // u and v are read only at their own pixel and update in place; u-bar and v-bar go to `out`.
 // iter[0] is the iteration index (incremented by the primal kernel, which runs after the dual kernel
-// has read it), iter[1] the length of the alpha table.
+// has read it), iter[1] the length of the alpha table, iter[2] the non-finite flag: the primal kernel
+// sets it to 1 when a new u or v is not finite (NaN or infinite data or operator output propagate
+// into u within an iteration or two); the host reads and clears it.
 // ------------------------------------------------------------------------------------------------
 template <bool TGV>
 __global__ void __launch_bounds__(NT) mri_dual_kernel(int W, int H, ImgPtrs in, ImgPtrs out, float sigma,
@@ -297,7 +299,7 @@ __global__ void __launch_bounds__(NT) mri_primal_kernel(int W, int H, ImgPtrs ou
   const size_t idx = (size_t)y * W + x;
   float2 kh = khr[idx];
   for (int g = 1; g < G; ++g) kh += khr[idx + (size_t)g * gstride];
-  mri_primal_pixel<TGV>(W, H, out, x, y, kh, tau);
+  if (!mri_primal_pixel<TGV>(W, H, out, x, y, kh, tau) && iter) iter[2] = 1;
 }
 
 __global__ void tick_kernel(int* tick) { atomicAdd(tick, 1); }

@@ -162,4 +162,9 @@ void reduce_kkt(int W, int H, const float2* khr, const float2* px, const float2*
 // *tick += 1 (one thread).
 void launch_tick(int* tick, cudaStream_t st);
 
+// Test hook of the bounded waits (pdt_debug_drop_arrival): the tensor-core kernels of the Cartesian
+// operators and of the warm-start network withhold one arrival while it is on.
+void cartesian_set_drop_arrival(int on);
+void cnn_set_drop_arrival(int on);
+
 }  // namespace pdt

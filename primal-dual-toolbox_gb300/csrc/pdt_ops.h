@@ -32,6 +32,8 @@ struct SolverHooks {
   virtual size_t compact_elems() = 0;
   // dense user k-space -> compact layout
   virtual void gather(const float2* dense, float2* compact, cudaStream_t st) = 0;
+  // compact layout -> dense user k-space (entries the compact layout does not hold are written as 0)
+  virtual void scatter(const float2* compact, float2* dense, cudaStream_t st) = 0;
   // One operator round of a primal-dual iteration:
   //   r <- (r + sigma (K ubar - f)) / (1 + sigma lambda);   khr <- K^H r
   // khr receives `groups()` partial sums spaced `group_stride()` elements apart.
@@ -84,6 +86,11 @@ class OpImpl {
 
   // Launch configuration chosen by the operator's autotuner ("" when it has none).
   virtual std::string tuning() { return ""; }
+
+  // Raises (and clears) what the operator's kernels reported on the device since the last check: a
+  // bounded wait that gave up (PDT_ERR_TIMEOUT). Reads device memory: call only where the caller waits
+  // for the work anyway.
+  virtual void check_device_errors() {}
 
   // Checks for solvers: constants complete, sizes consistent.
   void operator_check(const Dims& in, const Dims& out);

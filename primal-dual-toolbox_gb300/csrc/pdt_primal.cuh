@@ -18,8 +18,10 @@ __device__ __forceinline__ float2 bdiff(const float2* __restrict__ f, size_t idx
   return (pos > 0) ? ((pos < n - 1) ? f[idx] - f[idx - step] : -f[idx - step]) : f[idx];
 }
 
+// Returns false when the new u (or v) is not finite: the solvers' non-finite check, on values already
+// in registers.
 template <bool TGV>
-__device__ __forceinline__ void mri_primal_pixel(int W, int H, const ImgPtrs& out, int x, int y, float2 kh,
+__device__ __forceinline__ bool mri_primal_pixel(int W, int H, const ImgPtrs& out, int x, int y, float2 kh,
                                                  float tau) {
   const size_t idx = (size_t)y * W + x;
   const float2* px = static_cast<const float2*>(out.px);
@@ -30,6 +32,7 @@ __device__ __forceinline__ void mri_primal_pixel(int W, int H, const ImgPtrs& ou
   const float2 un = ou + tau * (d - kh);
   u[idx] = un;
   static_cast<float2*>(out.ub)[idx] = 2.0f * un - ou;
+  bool finite = isfinite(un.x) && isfinite(un.y);
   if constexpr (TGV) {
     const float2* qxx = static_cast<const float2*>(out.qxx);
     const float2* qyy = static_cast<const float2*>(out.qyy);
@@ -45,7 +48,9 @@ __device__ __forceinline__ void mri_primal_pixel(int W, int H, const ImgPtrs& ou
     vy[idx] = vyn;
     static_cast<float2*>(out.vbx)[idx] = 2.0f * vxn - ovx;
     static_cast<float2*>(out.vby)[idx] = 2.0f * vyn - ovy;
+    finite = finite && isfinite(vxn.x) && isfinite(vxn.y) && isfinite(vyn.x) && isfinite(vyn.y);
   }
+  return finite;
 }
 
 __device__ __forceinline__ float dual_proj_scale(float n, float alpha) { return 1.0f / fmaxf(1.0f, n / alpha); }

@@ -376,6 +376,10 @@ class RadialOp : public OpImpl, public SolverHooks {
     prepare();
     PDT_CUDA_CHECK(cudaMemcpyAsync(compact, dense, sizeof(float2) * dev_.C * dev_.Ns, cudaMemcpyDeviceToDevice, st));
   }
+  void scatter(const float2* compact, float2* dense, cudaStream_t st) override {
+    prepare();
+    PDT_CUDA_CHECK(cudaMemcpyAsync(dense, compact, sizeof(float2) * dev_.C * dev_.Ns, cudaMemcpyDeviceToDevice, st));
+  }
   int groups() override {
     prepare();
     return G_;

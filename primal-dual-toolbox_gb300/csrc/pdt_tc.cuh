@@ -122,9 +122,13 @@ __device__ __forceinline__ uint64_t global_ns() {
   return t;
 }
 
+constexpr uint64_t kWaitLimitNs = 200000000ull;  // 200 ms
+
 // Waits for the phase with the given parity to complete; gives up (returns false) after about
-// `limit_ns` nanoseconds so that a lost arrival ends in an error status instead of a hung kernel.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint64_t limit_ns = 200000000ull) {
+// `limit_ns` nanoseconds so that a lost arrival ends in an error status instead of a hung kernel. A
+// kernel that gives up still waits (with the same limit) for the copies and MMAs it has issued before
+// it frees its tensor memory and exits.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint64_t limit_ns = kWaitLimitNs) {
   if (mbar_try_wait(bar, parity)) return true;
   const uint64_t t0 = global_ns();
   for (uint32_t i = 0;; ++i) {
@@ -132,6 +136,14 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint64
     if ((i & 255u) == 255u && global_ns() - t0 > limit_ns) return false;
   }
 }
+
+// Test hook for the give-up path: while non-zero, the tensor-core kernels withhold one arrival (the
+// Cartesian row kernels: staging warp 2's arrival for operand chunk 0; the convolution: block 0's MMAs
+// and commit for its first tile), so that one bounded wait runs out. Nothing else sets it; each
+// translation unit including this header has its own copy, set by set_drop_arrival in that unit.
+static __device__ int g_drop_arrival = 0;
+
+static inline cudaError_t set_drop_arrival(int on) { return cudaMemcpyToSymbol(g_drop_arrival, &on, sizeof(int)); }
 
 // Tensor memory: one warp allocates `ncols` columns (a power of two >= 32) and writes the address to
 // shared memory; the same warp frees them.

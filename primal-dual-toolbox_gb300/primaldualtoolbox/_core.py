@@ -220,8 +220,13 @@ class _Optimizer:
     def getParameters(self):
         return self._params_cls(self)
 
+    _noisy_shape = None
+    _tgv = True
+    _with_op = True
+
     def setNoisyData(self, f, stream=None):
         b = Buffer(f, self._dtype)
+        self._noisy_shape = b.shape
         check(lib.pdt_opt_set_noisy_data(self._h, b.ptr, len(b.shape), _lib.iu_size(b.shape), b.is_device,
                                          _lib.stream_handle(stream)))
 
@@ -238,7 +243,8 @@ class _Optimizer:
         self._op = op
 
     FIELDS = {"u": 0, "ubar": 1, "vx": 2, "vy": 3, "vbarx": 4, "vbary": 5, "px": 6, "py": 7, "qxx": 8, "qyy": 9,
-              "qxy": 10}
+              "qxy": 10, "r": 11}
+    _TV_FIELDS = ("u", "ubar", "px", "py")
 
     def setInput0UV(self, u0, v0=None, stream=None):
         """Warm start of both TGV primals: u = u0, v = v0 (shape (2, H, W): vx, vy); duals reset to 0."""
@@ -249,12 +255,20 @@ class _Optimizer:
         check(lib.pdt_opt_set_input0_uv(self._h, b.ptr, vb.ptr if vb else None, len(b.shape), _lib.iu_size(b.shape),
                                         b.is_device, _lib.stream_handle(stream)))
 
-    def getField(self, name, out=None, stream=None):
-        """One plane of the solver state ('u', 'ubar', 'vx', 'vy', 'px', 'py', 'qxx', 'qyy', 'qxy', ...)."""
+    def _field_shape(self, name):
+        if name == "r":
+            if self._noisy_shape is None:
+                raise _lib.PdtError(5, "No noisy data is set!")
+            return self._noisy_shape
         nd = ctypes.c_int()
         size = (ctypes.c_int64 * 4)()
         check(lib.pdt_opt_result_size(self._h, ctypes.byref(nd), size))
-        shape = _lib.np_shape(nd.value, size)
+        return _lib.np_shape(nd.value, size)
+
+    def getField(self, name, out=None, stream=None):
+        """One plane of the solver state ('u', 'ubar', 'vx', 'vy', 'vbarx', 'vbary', 'px', 'py', 'qxx', 'qyy',
+        'qxy'), or 'r', the k-space dual of the with-operator optimizers, shaped like the noisy data."""
+        shape = self._field_shape(name)
         if out is None:
             out = np.empty(shape, dtype=self._dtype)
         b = Buffer(out, self._dtype)
@@ -262,6 +276,28 @@ class _Optimizer:
             raise ValueError(f"out has shape {b.shape}, expected {shape}")
         check(lib.pdt_opt_get_field(self._h, self.FIELDS[name], b.ptr, b.is_device, _lib.stream_handle(stream)))
         return out
+
+    def setField(self, name, arr, stream=None):
+        """Replace one plane of the solver state (names as getField); the next solve() continues from it."""
+        shape = self._field_shape(name)
+        b = Buffer(arr, self._dtype)
+        if b.shape != shape:
+            raise ValueError(f"{name} has shape {b.shape}, expected {shape}")
+        check(lib.pdt_opt_set_field(self._h, self.FIELDS[name], b.ptr, b.is_device, _lib.stream_handle(stream)))
+
+    def _state_names(self):
+        names = list(self.FIELDS) if self._tgv else list(self._TV_FIELDS) + ["r"]
+        return names if self._with_op else [n for n in names if n != "r"]
+
+    def getState(self, stream=None):
+        """Every primal and dual variable as a dict of numpy arrays (u, ubar, v, vbar, p, q and, with an
+        operator, r): with setState it resumes a solve exactly in another optimizer or process."""
+        return {n: self.getField(n, stream=stream) for n in self._state_names()}
+
+    def setState(self, state, stream=None):
+        """Import a state exported by getState (setNoisyData and setInput0 first: they size the state)."""
+        for n in self._state_names():
+            self.setField(n, state[n], stream=stream)
 
     def energy(self, stream=None):
         """FP64 energy of the current state: {'total', 'data', 'first_order', 'second_order'}."""
@@ -279,8 +315,14 @@ class _Optimizer:
         return {k: out[i] for i, k in enumerate(keys)}
 
     def solve(self, verbose=False, stream=None):
-        """Run max_iter + 1 primal-dual iterations (asynchronous when a stream is given)."""
+        """Run max_iter + 1 primal-dual iterations (asynchronous when a stream is given). Without a stream,
+        raises PdtError (PDT_ERR_NUMERIC) when a NaN or Inf appeared in u or v (with-operator solvers)."""
         check(lib.pdt_opt_solve(self._h, int(bool(verbose)), _lib.stream_handle(stream)))
+
+    def checkFinite(self, stream=None):
+        """The non-finite check of solves enqueued on a stream: waits for it and raises PdtError
+        (PDT_ERR_NUMERIC) if a NaN or Inf appeared in u or v since the last check."""
+        check(lib.pdt_opt_status(self._h, _lib.stream_handle(stream)))
 
     def profile(self, iters=10, stream=None):
         """Run `iters` further iterations launch by launch and return {kernel phase: mean ms per iteration}

@@ -15,6 +15,8 @@ class TvOptimizer_2f(_Optimizer):
     _kind = _lib.OPT_TV
     _dtype = np.float32
     _params_cls = TvParameters
+    _tgv = False
+    _with_op = False
 
 
 class TgvOptimizer_2f(_Optimizer):
@@ -22,6 +24,7 @@ class TgvOptimizer_2f(_Optimizer):
     _kind = _lib.OPT_TGV
     _dtype = np.float32
     _params_cls = TgvParameters
+    _with_op = False
 
 
 class TvOptimizer_2c(TvOptimizer_2f):

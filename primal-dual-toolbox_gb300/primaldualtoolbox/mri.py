@@ -139,6 +139,7 @@ class TvOptimizerWithOp_2c3c(_Optimizer):
     """TV with an operator (TvOptimizerWithOp), Cartesian operators."""
     _kind = _lib.OPT_TV_OP
     _params_cls = TvParameters
+    _tgv = False
     _operators = _OPS_3C
 
     def setOperator(self, op):
@@ -161,6 +162,7 @@ class TvOptimizer_2c2c(_Optimizer):
     """TV with an operator (TvOptimizerWithOp), radial and sampling operators."""
     _kind = _lib.OPT_TV_OP
     _params_cls = TvParameters
+    _tgv = False
     _operators = _OPS_2C
 
     def setOperator(self, op):

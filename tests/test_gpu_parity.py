@@ -213,21 +213,27 @@ def test_sampling_operator_tgv_mri(pdt, oracle):
     assert rel_l2(opt.getResult(), ref) <= SOLVE_TOL
 
 
-def test_tgv_mri_config2_full_size_short(pdt, oracle):
-    """Full 15 x 640 x 368 ROOS problem, 10 iterations, against the FP32 oracle."""
+@pytest.mark.parametrize("max_iter", [9, 1000])
+def test_tgv_mri_config2_full_size(pdt, oracle, max_iter):
+    """The benchmark problem itself: 15 coils x 640 x 368 with readout-oversampling removal, the sample's
+    schedule (reduction 2e-8, alpha0 = 2 alpha1), against the FP32-mirror oracle after 10 iterations and
+    after the stated 1000 -> 1001 iterations (50 replays of the captured 20-iteration graph, the device
+    alpha table through the whole continuation, the dual update in the tensor-core adjoint launch). The
+    1001-iteration oracle run takes about 70 s on 16 host cores."""
     case = _cart_case(C=15, H=640, W=368, roos=True, seed=0)
     op = pdt.mri.MriCartesianRemoveROOSOperator()
     op.setCoilSens(case["sens"])
     op.setMask(case["mask"])
     opt = pdt.mri.TgvMriOptimizer_2c3c()
     prm = opt.getParameters()
-    prm.reduction, prm.max_iter, prm.alpha1 = 2e-8, 9, case["alpha1"]
+    prm.reduction, prm.max_iter, prm.alpha1 = 2e-8, max_iter, case["alpha1"]
     prm.alpha0 = 2 * prm.alpha1
     opt.setOperator(op)
     opt.setNoisyData(case["rawdata"])
     opt.solve()
     ref = oracle.op_solve("cartesian_roos", case["sens"], case["mask"], case["rawdata"], "tgv_mri",
-                          alpha0=prm.alpha0, alpha1=prm.alpha1, reduction=prm.reduction, max_iter=9, prec=32)
+                          alpha0=prm.alpha0, alpha1=prm.alpha1, reduction=prm.reduction, max_iter=max_iter,
+                          prec=32)
     assert rel_l2(opt.getResult(), ref) <= SOLVE_TOL
 
 

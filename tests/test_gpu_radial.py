@@ -121,3 +121,30 @@ def synthetic_phantom(N):
     from primaldualtoolbox import synthetic
 
     return synthetic.mri_phantom(N, N, seed=0)
+
+
+def test_radial_config5_slice_200_iterations(pdt, oracle):
+    """One full radial slice of the benchmark: 256 x 256, 12 coils, 64 golden-angle spokes x 512 samples,
+    Kaiser-Bessel width 3 on a 1.5x grid, density weights sqrt|k|, 200 TGV-MRI iterations (reduction 2^-8)
+    against the FP32-mirror oracle (about 20 s on 16 host cores)."""
+    from primaldualtoolbox import synthetic
+
+    N, C = 256, 12
+    traj, k = radial_traj(64, 512, golden=True)
+    dcf = np.sqrt(np.abs(k)).astype(np.float32)[None, :]
+    sens = synthetic.coil_maps(C, N, N, seed=0)
+    op = _op(pdt, N, 1.5, 3, traj, dcf, sens)
+    f = op.forward(synthetic.mri_phantom(N, N, seed=0))
+    rng = np.random.default_rng(0)
+    f = f + (0.01 * np.abs(f).max() * (rng.standard_normal(f.shape) + 1j * rng.standard_normal(f.shape))).astype(
+        np.complex64)
+    a1 = float(np.float32(0.02 * float(np.abs(op.adjoint(f)).max())))
+    opt = pdt.mri.TgvMriOptimizer_2c2c()
+    prm = opt.getParameters()
+    prm.max_iter, prm.alpha1, prm.alpha0, prm.reduction = 199, a1, 2 * a1, 2.0 ** -8
+    opt.setOperator(op)
+    opt.setNoisyData(f)
+    opt.solve()
+    ref = oracle.radial_solve(traj, dcf, sens, f, N, 1.5, 3, "tgv_mri", alpha0=2 * a1, alpha1=a1,
+                              reduction=2.0 ** -8, max_iter=199, prec=32)
+    assert rel_l2(opt.getResult(), ref) <= 1e-4
