@@ -813,6 +813,29 @@ def run_ncu_case(args):
     import primaldualtoolbox as pdt
 
     stream = torch.cuda.current_stream()
+    if args.ncu_workload == "cnn":
+        # the warm-start network: one training step (forward, backward, Adam) on a batch of 4 images of
+        # 320 x 320 (the learned-warm-start configuration), --ncu-iters times between the profiler marks
+        from primaldualtoolbox import warmstart
+
+        rng = np.random.default_rng(0)
+
+        def img(*shape):
+            return torch.from_numpy((rng.standard_normal(shape) + 1j * rng.standard_normal(shape))
+                                    .astype(np.complex64)).cuda()
+
+        net = warmstart.WarmStartNet(seed=0)
+        u0, ut, vt = img(4, 320, 320), img(4, 320, 320), img(4, 2, 320, 320)
+        for _ in range(3):
+            net.train_step(u0, ut, vt, lr=1e-4, stream=stream)
+        torch.cuda.synchronize()
+        torch.cuda.profiler.start()
+        for _ in range(args.ncu_iters):
+            net.train_step(u0, ut, vt, lr=1e-4, stream=stream)
+        torch.cuda.synchronize()
+        torch.cuda.profiler.stop()
+        print(json.dumps({"ncu_case": "warmstart_cnn_train_step_4x320x320", "steps": args.ncu_iters}), flush=True)
+        return
     if args.ncu_workload == "radial":
         op, f, a1 = _radial_problem(pdt, seed=0)
         opt = pdt.mri.TgvMriOptimizer_2c2c()
@@ -908,8 +931,9 @@ def main():
     ap.add_argument("--radial-iters", type=int, default=200, help="radial leg: iterations per slice")
     ap.add_argument("--batch-cases", type=int, default=64, help="batched leg: independent problems (0 skips)")
     ap.add_argument("--batch-iters", type=int, default=200, help="batched leg: iterations per problem and step")
-    ap.add_argument("--ncu-workload", default="cartesian", choices=["cartesian", "radial"],
-                    help="profiling mode: the config-2 Cartesian problem or the config-5 radial slice")
+    ap.add_argument("--ncu-workload", default="cartesian", choices=["cartesian", "radial", "cnn"],
+                    help="profiling mode: the config-2 Cartesian problem, the config-5 radial slice or one "
+                         "training step of the warm-start network")
     ap.add_argument("--ncu-iters", type=int, default=0,
                     help="profiling mode: one solve of this many iterations between cudaProfilerStart/Stop")
     args = ap.parse_args()
