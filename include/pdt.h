@@ -159,6 +159,12 @@ PDT_API pdt_status pdt_opt_set_input0(pdt_opt* opt, const void* u0, int ndim, co
  * with-operator solvers check every new u and v for NaN and Inf on the device; with a NULL stream the
  * call returns PDT_ERR_NUMERIC when one appeared (the state then holds the non-finite iterate). */
 PDT_API pdt_status pdt_opt_solve(pdt_opt* opt, int verbose, void* stream);
+/* No counterpart in the reference, whose with-operator solvers fix tau = 1/16 (TGV-MRI) or 1/8 and
+ * sigma = 1/8 (tgvmrioptimizer.cu:132-134, t*optimizerwithop.cu): the primal and dual step sizes of the
+ * following solves of a with-operator optimizer; 0 restores the reference's value. Convergence needs
+ * tau * sigma * |K|^2 < 1 for the solver's whole linear operator (about 13 for TGV with an operator of
+ * norm 1). The reference's steps stay the default. */
+PDT_API pdt_status pdt_opt_set_steps(pdt_opt* opt, double tau, double sigma);
 /* No counterpart in the reference: the non-finite check of solves enqueued on an explicit stream. Waits
  * for `stream`, returns PDT_ERR_NUMERIC if a NaN or Inf appeared in u or v since the last check (and
  * clears the flag), else PDT_OK. */

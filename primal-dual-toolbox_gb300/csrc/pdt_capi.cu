@@ -285,6 +285,8 @@ class OptImpl {
   size_t pix() const { return cplx_ ? 8 : 4; }
 
   pdt_params params_;
+  // Step sizes of the with-operator solves when positive (pdt_opt_set_steps); 0: the reference's.
+  float step_tau_ = 0.f, step_sigma_ = 0.f;
 
   void set_operator(std::shared_ptr<OpImpl> op) {
     if (!with_op()) throw Error(PDT_ERR_INVALID_ARGUMENT, "this optimizer takes no operator");
@@ -757,8 +759,10 @@ class OptImpl {
       ++version_;
     }
     // step sizes (tgvmrioptimizer.cu:132-134; *withop.cu: tau = sigma = 1/8)
-    const float tau = kind_ == PDT_OPT_TGV_MRI ? 1.0f / 16.0f : 1.0f / 8.0f;
-    const float sigma = 1.0f / 8.0f;
+    float tau = kind_ == PDT_OPT_TGV_MRI ? 1.0f / 16.0f : 1.0f / 8.0f;
+    float sigma = 1.0f / 8.0f;
+    if (step_tau_ > 0.f) tau = step_tau_;  // pdt_opt_set_steps (no reference counterpart)
+    if (step_sigma_ > 0.f) sigma = step_sigma_;
     const float lambda = kind_ == PDT_OPT_TGV_MRI ? 1.0f : (float)params_.lambda;
     // alpha table for every iteration (tgvmrioptimizer.cu:144-155 in real_type)
     const unsigned K = params_.max_iter;
@@ -834,7 +838,8 @@ class OptImpl {
     pl.key = graph_key({(uintptr_t)img_.p, (uintptr_t)r_.p, (uintptr_t)fc_.p, (uintptr_t)khr_.p,
                         (uintptr_t)alpha_.p, (uintptr_t)alpha_.bytes, (uintptr_t)op_.get(),
                         (uintptr_t)op_->generation(), (uintptr_t)W_, (uintptr_t)H_, (uintptr_t)G, (uintptr_t)p0,
-                        (uintptr_t)is_tgv, (uintptr_t)fused, fbits(lambda), fbits(tau), (uintptr_t)version_});
+                        (uintptr_t)is_tgv, (uintptr_t)fused, fbits(lambda), fbits(tau), fbits(sigma),
+                        (uintptr_t)version_});
     return pl;
   }
 
@@ -1363,6 +1368,15 @@ pdt_status pdt_opt_solve(pdt_opt* opt, int verbose, void* stream) {
       PDT_CUDA_CHECK(cudaStreamSynchronize(st));
       opt->impl->check_device(st);
     }
+  });
+}
+
+pdt_status pdt_opt_set_steps(pdt_opt* opt, double tau, double sigma) {
+  return guarded([&] {
+    need(opt, "optimizer");
+    if (!(tau >= 0) || !(sigma >= 0)) throw Error(PDT_ERR_INVALID_ARGUMENT, "step sizes must be >= 0");
+    opt->impl->step_tau_ = (float)tau;
+    opt->impl->step_sigma_ = (float)sigma;
   });
 }
 

@@ -319,6 +319,11 @@ class _Optimizer:
         raises PdtError (PDT_ERR_NUMERIC) when a NaN or Inf appeared in u or v (with-operator solvers)."""
         check(lib.pdt_opt_solve(self._h, int(bool(verbose)), _lib.stream_handle(stream)))
 
+    def setSteps(self, tau=0.0, sigma=0.0):
+        """Primal / dual step sizes of the following solves (with-operator optimizers); 0 restores the
+        reference's (tau = 1/16 for TGV-MRI, else 1/8; sigma = 1/8)."""
+        check(lib.pdt_opt_set_steps(self._h, float(tau), float(sigma)))
+
     def checkFinite(self, stream=None):
         """The non-finite check of solves enqueued on a stream: waits for it and raises PdtError
         (PDT_ERR_NUMERIC) if a NaN or Inf appeared in u or v since the last check."""

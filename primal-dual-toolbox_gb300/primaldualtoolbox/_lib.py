@@ -32,7 +32,7 @@ EXPORTED = ["pdt_last_error", "pdt_version", "pdt_launch_count", "pdt_host_alloc
             "pdt_opt_create", "pdt_opt_destroy", "pdt_opt_get_params", "pdt_opt_set_params", "pdt_opt_set_operator",
             "pdt_opt_set_noisy_data", "pdt_opt_set_input0", "pdt_opt_solve", "pdt_opt_result_size",
             "pdt_opt_get_result", "pdt_opt_profile", "pdt_opt_set_input0_uv", "pdt_opt_get_field", "pdt_opt_energy",
-            "pdt_opt_gap", "pdt_opt_set_field", "pdt_opt_status", "pdt_debug_drop_arrival",
+            "pdt_opt_gap", "pdt_opt_set_field", "pdt_opt_status", "pdt_debug_drop_arrival", "pdt_opt_set_steps",
             "pdt_op_norm", "pdt_dist2", "pdt_batch_create", "pdt_batch_destroy", "pdt_batch_add",
             "pdt_batch_solve", "pdt_cnn_create", "pdt_cnn_destroy", "pdt_cnn_num_params", "pdt_cnn_get_params",
             "pdt_cnn_set_params", "pdt_cnn_get_grads", "pdt_cnn_train_step", "pdt_cnn_predict",
@@ -94,6 +94,7 @@ def _load():
     L.pdt_opt_get_field.argtypes = [vp, i, vp, i, vp]
     L.pdt_opt_set_field.argtypes = [vp, i, vp, i, vp]
     L.pdt_opt_status.argtypes = [vp, vp]
+    L.pdt_opt_set_steps.argtypes = [vp, ctypes.c_double, ctypes.c_double]
     L.pdt_debug_drop_arrival.argtypes = [i]
     L.pdt_opt_energy.argtypes = [vp, vp, ctypes.POINTER(ctypes.c_double)]
     L.pdt_opt_gap.argtypes = [vp, vp, ctypes.POINTER(ctypes.c_double)]
