@@ -303,13 +303,11 @@ def run_ours(args):
     if args.accuracy:
         from primaldualtoolbox import warmstart
 
-        conv = {"tgv_mri_15c_640x368_roos": time_to_accuracy(pdt, torch, case, dev, stream, True,
-                                                             per_iter_s=t_max / args.steps / ITERS,
-                                                             weights=warmstart.DEFAULT_WEIGHTS, max_plain=200000)}
-        c4 = _synthetic().cartesian_case(seed=4000, **CFG4)
-        dev4 = {k: torch.from_numpy(np.ascontiguousarray(c4[k])).cuda() for k in ("rawdata", "sens", "mask")}
-        conv["config4_15c_320x320"] = time_to_accuracy(pdt, torch, c4, dev4, stream, False,
-                                                       weights=warmstart.CONFIG4_WEIGHTS)
+        conv = {"tgv_mri_15c_640x368_roos": _cartesian_convergence(
+            pdt, torch, case, stream, True, per_iter_s=t_max / args.steps / ITERS, weights=warmstart.DEFAULT_WEIGHTS,
+            max_plain=200000)}
+        conv["config4_15c_320x320"] = _cartesian_convergence(pdt, torch, _synthetic().cartesian_case(seed=4000, **CFG4),
+                                                             stream, False, weights=warmstart.CONFIG4_WEIGHTS)
 
     # e2e: the public API with pinned host buffers, every input uploaded and the result read back
     host = {k: pdt.pinned_empty(case[k].shape, case[k].dtype) for k in ("rawdata", "sens", "mask")}
@@ -459,29 +457,30 @@ def _per_iteration_s(opt, prm, torch, stream, n=2000):
     return e0.elapsed_time(e1) / 1e3 / n
 
 
-def time_to_accuracy(pdt, torch, case, dev, stream, roos, per_iter_s=None, weights=None, target=1e-4,
-                     max_plain=400000):
-    """Wall time for the fixed-alpha TGV-MRI iteration (reduction 1) to reach rel-L2 <= target to its
+def time_to_accuracy(pdt, torch, make, u0, stream, per_iter_s=None, weights=None, steps=None, target=1e-4,
+                     max_plain=400000, max_dual=60000):
+    """Wall time for a fixed-alpha TGV-MRI iteration (reduction 1) to reach rel-L2 <= target to its
     converged solution u*, four ways: the reference's step sizes from the plain start u0 = A^H f (`plain`),
     the same from the learned warm start (`warm_start`: the network's (u, v), kept only when its FP64
     energy is lower), and both starts with the dual-weighted step sizes (`dual_weighted`,
-    `warm_start_dual_weighted`; warmstart.DUAL_WEIGHTED_STEPS, tau sigma = 1/16 instead of 1/128 and
-    sigma / tau = 1024 instead of 2). All four converge to the same saddle point. u* is the engine's
-    dual-weighted iterate after STAR_ITERS iterations; its stationarity under the reference's steps (the
-    change over 2000 further reference iterations) is reported. Times are iterations x the timed
-    per-iteration cost (+ the network's inference and energy check); errors are FP64 GPU reductions."""
+    `warm_start_dual_weighted`: sigma / tau = 1024 instead of 2, tau sigma (12 + |K|^2) = 0.8). All four
+    converge to the same saddle point. `make()` returns a fresh (operator, optimizer, parameters) with the
+    data set; u0 is the device image A^H f. u* is the engine's dual-weighted iterate after STAR_ITERS
+    iterations; its change over 2000 further iterations with the reference's steps is reported. Times are
+    iterations x the timed per-iteration cost (+ the network's inference and energy check); errors are
+    FP64 GPU reductions."""
     from primaldualtoolbox import warmstart
 
-    steps = warmstart.DUAL_WEIGHTED_STEPS
-    op, ref, prm = _fixed_alpha_optimizer(pdt, case, dev, stream, roos)
+    op, ref, prm = make()
+    if steps is None:
+        steps = warmstart.dual_weighted_steps(op.norm(iters=40))
     if per_iter_s is None:
         per_iter_s = _per_iteration_s(ref, prm, torch, stream)
-        op, ref, prm = _fixed_alpha_optimizer(pdt, case, dev, stream, roos)
+        op, ref, prm = make()
     ref.setSteps(*steps)
     prm.max_iter = STAR_ITERS - 1
     ref.solve(stream=stream)
-    Hi = case["mask"].shape[0] // 2 if roos else case["mask"].shape[0]
-    shape = (Hi, case["mask"].shape[1])
+    shape = tuple(u0.shape)
     u_star = torch.empty(shape, dtype=torch.complex64, device="cuda")
     ref.getResult(out=u_star, stream=stream)
     ref.setSteps(0, 0)
@@ -493,9 +492,6 @@ def time_to_accuracy(pdt, torch, case, dev, stream, roos, per_iter_s=None, weigh
     n_star = pdt.dist2(u_star) ** 0.5
     stationarity = pdt.dist2(u_ref, u_star) ** 0.5 / n_star
     del ref
-    u0 = torch.empty_like(u_star)
-    op.adjoint(dev["rawdata"], out=u0, stream=stream)
-    torch.cuda.synchronize()
     out = {"target_rel_l2": target, "alpha": "fixed (reduction 1)", "per_iteration_ms": round(per_iter_s * 1e3, 5),
            "u_star": {"iterations": STAR_ITERS, "steps": "dual_weighted",
                       "change_over_2000_reference_iterations": stationarity},
@@ -508,7 +504,7 @@ def time_to_accuracy(pdt, torch, case, dev, stream, roos, per_iter_s=None, weigh
         uw = torch.empty((1,) + shape, dtype=torch.complex64, device="cuda")
         vw = torch.empty((1, 2) + shape, dtype=torch.complex64, device="cuda")
         net.predict(u0.reshape((1,) + shape), uw, vw, stream=stream)  # warm-up
-        _, o, _ = _fixed_alpha_optimizer(pdt, case, dev, stream, roos)
+        _, o, _ = make()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
         choice = warmstart.warm_start(o, net, u0, torch, stream=stream)
@@ -517,23 +513,27 @@ def time_to_accuracy(pdt, torch, case, dev, stream, roos, per_iter_s=None, weigh
         inf_ms = e0.elapsed_time(e1)
         out["warm_start_choice"] = {k: (round(v, 6) if isinstance(v, float) else v) for k, v in choice.items()}
         out["warm_start_choice"]["inference_and_energy_ms"] = round(inf_ms, 3)
+        ws = torch.empty_like(u_star)
+        o.getResult(out=ws, stream=stream)
+        torch.cuda.synchronize()
+        out["warm_start_choice"]["start_rel_l2"] = pdt.dist2(ws, u_star) ** 0.5 / n_star
         out["weights"] = os.path.relpath(weights, ROOT)
 
     def leg(name, learned, dual):
-        _, o, p = _fixed_alpha_optimizer(pdt, case, dev, stream, roos)
+        _, o, p = make()
         if learned:
             warmstart.warm_start(o, net, u0, torch, stream=stream)
         else:
             o.setInput0(u0, stream=stream)
         if dual:
             o.setSteps(*steps)
-        it, err = _iterations_to(pdt, torch, o, p, u_star, n_star, stream, target, 250 if dual else 1000,
-                                 max_plain if not dual else 60000)
+        cap = max_dual if dual else max_plain
+        it, err = _iterations_to(pdt, torch, o, p, u_star, n_star, stream, target, 250 if dual else 1000, cap)
         res = {"iterations": it, "final_rel_l2": err}
         if it:
             res["ms"] = round(it * per_iter_s * 1e3 + (inf_ms if learned else 0.0), 3)
         else:
-            res["not_reached_within"] = max_plain if not dual else 60000
+            res["not_reached_within"] = cap
         out[name] = res
 
     leg("plain", False, False)
@@ -548,6 +548,20 @@ def time_to_accuracy(pdt, torch, case, dev, stream, roos, per_iter_s=None, weigh
             if not out["plain"].get("ms"):
                 out[k]["speedup_is_lower_bound"] = True
     return out
+
+
+def _cartesian_convergence(pdt, torch, case, stream, roos, **kw):
+    dev = {k: torch.from_numpy(np.ascontiguousarray(case[k])).cuda() for k in ("rawdata", "sens", "mask")}
+
+    def make():
+        return _fixed_alpha_optimizer(pdt, case, dev, stream, roos)
+
+    op, _, _ = make()
+    Hf, Wd = case["mask"].shape
+    u0 = torch.empty((Hf // 2 if roos else Hf, Wd), dtype=torch.complex64, device="cuda")
+    op.adjoint(dev["rawdata"], out=u0, stream=stream)
+    torch.cuda.synchronize()
+    return time_to_accuracy(pdt, torch, make, u0, stream, **kw)
 
 
 def _khr_planes(tuning):
@@ -729,7 +743,7 @@ def _radial_bytes():
     return fwd + prox + adj + c8 * RAD_N * RAD_N * 28
 
 
-def run_radial(pdt, torch, slices, iters):
+def run_radial(pdt, torch, slices, iters, converge=True):
     """Config 5: one radial slice alone, and `slices` slices advanced together (BatchSolver)."""
     probs = [_radial_problem(pdt, seed=s) for s in range(slices)]
     opts = []
@@ -759,6 +773,27 @@ def run_radial(pdt, torch, slices, iters):
     t1 = timed(lambda: opts[0].solve(stream=stream), 3)
     batch = pdt.batch.BatchSolver(opts)
     tb = timed(lambda: batch.solve(stream=stream), 2)
+    conv = None
+    if converge:
+        # time to rel-L2 1e-4 of one slice: reference vs dual-weighted steps, plain vs learned start
+        from primaldualtoolbox import warmstart
+
+        op0, f0, a10 = probs[0]
+        fd = torch.from_numpy(np.ascontiguousarray(f0)).cuda()
+
+        def make():
+            o = pdt.mri.TgvMriOptimizer_2c2c()
+            p = o.getParameters()
+            p.reduction, p.alpha1, p.alpha0 = 1.0, a10, 2 * a10
+            o.setOperator(op0)
+            o.setNoisyData(fd, stream=stream)
+            return op0, o, p
+
+        u0 = torch.empty((RAD_N, RAD_N), dtype=torch.complex64, device="cuda")
+        op0.adjoint(fd, out=u0, stream=stream)
+        torch.cuda.synchronize()
+        conv = time_to_accuracy(pdt, torch, make, u0, stream, weights=warmstart.CONFIG4_WEIGHTS, max_plain=150000)
+        conv["operator_norm"] = op0.norm(iters=40)
     return {"workload": f"radial_tgv2_{RAD_C}c_{RAD_N}x{RAD_N}_{RAD_SPOKES}spokes_x{RAD_RO}",
             "osf": RAD_OSF, "kernel_width": RAD_KW, "iterations_per_slice": iters, "tuning": probs[0][0].tuning(),
             "single_slice": {"value": round(iters / t1, 1), "unit": "iters/s"},
@@ -767,7 +802,8 @@ def run_radial(pdt, torch, slices, iters):
                                      "achieved": round(nbytes * slices * iters / tb / 1e9, 1), "peak": hbm,
                                      "peak_source": src, "unit": "GB/s",
                                      "frac": round(nbytes * slices * iters / tb / 1e9 / hbm, 4),
-                                     "algorithmic_bytes_per_slice_iteration": int(nbytes)}}}
+                                     "algorithmic_bytes_per_slice_iteration": int(nbytes)}},
+            "time_to_1e-4": conv}
 
 
 def run_denoising(pdt, torch, reps=3):

@@ -42,6 +42,15 @@ CONFIG4_WEIGHTS = os.path.join(_DATA, "warmstart_15c_320x320.npz")
 DUAL_WEIGHTED_STEPS = (1.0 / 128.0, 8.0)
 
 
+def dual_weighted_steps(op_norm=1.0, ratio=1024.0, margin=0.8):
+    """(tau, sigma) with sigma / tau = ratio and tau sigma (12 + |K|^2) = margin for an operator of norm
+    op_norm (12 bounds |[grad, -1; 0, eps]|^2 of the TGV part). For op_norm = 1 this is about
+    DUAL_WEIGHTED_STEPS."""
+    ts = margin / (12.0 + float(op_norm) ** 2)
+    tau = (ts / ratio) ** 0.5
+    return tau, ratio * tau
+
+
 def _bind():
     vp, i = ctypes.c_void_p, ctypes.c_int
     lib.pdt_cnn_create.argtypes = [ctypes.c_uint64, ctypes.POINTER(vp)]
