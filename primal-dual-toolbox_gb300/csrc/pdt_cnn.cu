@@ -372,18 +372,43 @@ __global__ void wgrad_reduce(const float* __restrict__ partial, int nblocks, int
 }
 
 // db[co] = sum over pixels of dy[p][co]: one block per channel, fixed-order tree.
-__global__ void bias_grad(const bf16* __restrict__ dy, size_t npix, int C, float* __restrict__ db) {
-  __shared__ float sh[256];
-  const int co = blockIdx.x;
-  float s = 0.f;
-  for (size_t p = threadIdx.x; p < npix; p += blockDim.x) s += __bfloat162float(dy[p * C + co]);
-  sh[threadIdx.x] = s;
-  __syncthreads();
-  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
-    if ((int)threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
-    __syncthreads();
+// Per-channel sums of dy [npix][C] (the bias gradient), stage 1: block b sums the pixels of its contiguous
+// chunk -- C / 2 threads per pixel, two channels each, so that a warp reads consecutive bytes -- and writes
+// partial[b][C]; sum_partials adds the blocks' partials in block order (deterministic).
+template <int C>
+__global__ void __launch_bounds__(256) bias_grad_partial(const bf16* __restrict__ dy, size_t npix,
+                                                         float* __restrict__ partial) {
+  constexpr int TPP = C / 2, PPB = 256 / TPP;  // threads per pixel, pixels per pass
+  __shared__ float2 sh[256];
+  const int t = threadIdx.x, cp = t % TPP, pr = t / TPP;
+  const size_t chunk = (npix + gridDim.x - 1) / gridDim.x;
+  const size_t p0 = (size_t)blockIdx.x * chunk, p1 = min(npix, p0 + chunk);
+  float2 acc = c2(0.f, 0.f);
+  for (size_t p = p0 + pr; p < p1; p += PPB) {
+    const __nv_bfloat162 v = reinterpret_cast<const __nv_bfloat162*>(dy + p * C)[cp];
+    acc.x += __low2float(v);
+    acc.y += __high2float(v);
   }
-  if (threadIdx.x == 0) db[co] = sh[0];
+  sh[t] = acc;
+  __syncthreads();
+  if (t < TPP) {
+    float2 a = c2(0.f, 0.f);
+    for (int r = 0; r < PPB; ++r) {
+      a.x += sh[r * TPP + t].x;
+      a.y += sh[r * TPP + t].y;
+    }
+    partial[(size_t)blockIdx.x * C + 2 * t] = a.x;
+    partial[(size_t)blockIdx.x * C + 2 * t + 1] = a.y;
+  }
+}
+
+// out[i] = sum over blocks b (in order) of partial[b * stride + i], i < n.
+__global__ void sum_partials(const float* __restrict__ partial, int nblocks, int stride, int n, float* __restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float s = 0.f;
+  for (int b = 0; b < nblocks; ++b) s += partial[(size_t)b * stride + i];
+  out[i] = s;
 }
 
 // w'[tap'][ci][co] = w[8 - tap'][co][ci] (padded to COP output / CIP input channels) for the data gradient.
@@ -427,38 +452,37 @@ __global__ void conv_in_fwd(const float* __restrict__ x, const float* __restrict
 }
 
 // First-layer weight gradient: dW[tap][co][cj] = sum_p x[p + d][cj] g[p][co]; block per (tap, co).
-__global__ void conv_in_wgrad(const float* __restrict__ x, const bf16* __restrict__ g, int B, int H, int W,
-                              float* __restrict__ dw, float* __restrict__ db) {
-  __shared__ float sh[3][256];
-  const int tap = blockIdx.x / CH, co = blockIdx.x % CH;
+// Weight and bias gradients of the 2 -> 32 input layer, stage 1: block b takes a contiguous chunk of
+// pixels; warp `tap` (nine warps), lane co; g is read as 64 consecutive bytes per pixel and x (two FP32
+// channels) is broadcast. partial[b][(tap CH + co) 2 + ci] = sum x[p + d(tap)][ci] g[p][co];
+// partial[b][NTAP CH 2 + co] = sum g[p][co]. sum_partials adds the blocks in order.
+constexpr int kConvInPartial = NTAP * CH * 2 + CH;
+constexpr int kPartialBlocksPerSm = 8;  // blocks per SM of the input-layer gradient (short chunks, more in flight)
+__global__ void __launch_bounds__(32 * NTAP) conv_in_wgrad_partial(const float* __restrict__ x,
+                                                                   const bf16* __restrict__ g, int B, int H, int W,
+                                                                   float* __restrict__ partial) {
+  const int tap = threadIdx.x >> 5, co = threadIdx.x & 31;
   const int ky = tap / 3 - 1, kx = tap % 3 - 1;
   const size_t n = (size_t)B * H * W;
+  const size_t chunk = (n + gridDim.x - 1) / gridDim.x;
+  const size_t p0 = (size_t)blockIdx.x * chunk, p1 = min(n, p0 + chunk);
+  const float2* x2 = reinterpret_cast<const float2*>(x);
   float s0 = 0.f, s1 = 0.f, sb = 0.f;
-  for (size_t p = threadIdx.x; p < n; p += blockDim.x) {
+  for (size_t p = p0; p < p1; ++p) {
     const int xx = (int)(p % W), yy = (int)((p / W) % H), b = (int)(p / ((size_t)W * H));
     const float gv = __bfloat162float(g[p * CH + co]);
     const int gy = yy + ky, gx = xx + kx;
     if (gy >= 0 && gy < H && gx >= 0 && gx < W) {
-      const size_t q = ((size_t)b * H + gy) * W + gx;
-      s0 += x[q * 2] * gv;
-      s1 += x[q * 2 + 1] * gv;
+      const float2 xv = x2[((size_t)b * H + gy) * W + gx];
+      s0 += xv.x * gv;
+      s1 += xv.y * gv;
     }
     sb += gv;
   }
-  sh[0][threadIdx.x] = s0;
-  sh[1][threadIdx.x] = s1;
-  sh[2][threadIdx.x] = sb;
-  __syncthreads();
-  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
-    if ((int)threadIdx.x < o)
-      for (int j = 0; j < 3; ++j) sh[j][threadIdx.x] += sh[j][threadIdx.x + o];
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) {
-    dw[(tap * CH + co) * 2] = sh[0][0];
-    dw[(tap * CH + co) * 2 + 1] = sh[1][0];
-    if (tap == 0) db[co] = sh[2][0];
-  }
+  float* out = partial + (size_t)blockIdx.x * kConvInPartial;
+  out[(tap * CH + co) * 2] = s0;
+  out[(tap * CH + co) * 2 + 1] = s1;
+  if (tap == 0) out[NTAP * CH * 2 + co] = sb;
 }
 
 // g = gin * relu'(z)   (BF16 in and out)
@@ -561,23 +585,32 @@ __global__ void prep_target(const float2* __restrict__ u0, const float2* __restr
 }
 
 // s[b] = max |u0| over image b; inv_s[b] = 1 / s[b] (1 for an all-zero image). Block per image.
-__global__ void image_scale(const float2* __restrict__ u0, size_t npix, float* __restrict__ s,
-                            float* __restrict__ inv_s) {
+// max |u0| of image blockIdx.y over the pixels of block column blockIdx.x, combined across blocks with an
+// integer atomicMax on the float's bits (non-negative floats order like their bit patterns, so the result
+// does not depend on the order); image_scale_finish turns the maxima into the scale and its inverse.
+__global__ void image_scale_max(const float2* __restrict__ u0, size_t npix, int* __restrict__ imax) {
   __shared__ float sh[256];
-  const float2* img = u0 + (size_t)blockIdx.x * npix;
+  const float2* img = u0 + (size_t)blockIdx.y * npix;
   float m = 0.f;
-  for (size_t i = threadIdx.x; i < npix; i += blockDim.x) m = fmaxf(m, sqrtf(abs2(img[i])));
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < npix; i += (size_t)gridDim.x * blockDim.x)
+    m = fmaxf(m, sqrtf(abs2(img[i])));
   sh[threadIdx.x] = m;
   __syncthreads();
   for (int o = blockDim.x / 2; o > 0; o >>= 1) {
     if ((int)threadIdx.x < o) sh[threadIdx.x] = fmaxf(sh[threadIdx.x], sh[threadIdx.x + o]);
     __syncthreads();
   }
-  if (threadIdx.x == 0) {
-    const float v = sh[0] > 0.f ? sh[0] : 1.f;
-    s[blockIdx.x] = v;
-    inv_s[blockIdx.x] = 1.f / v;
-  }
+  if (threadIdx.x == 0) atomicMax(imax + blockIdx.y, __float_as_int(sh[0]));
+}
+
+__global__ void image_scale_finish(const int* __restrict__ imax, int B, float* __restrict__ s,
+                                   float* __restrict__ inv_s) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= B) return;
+  const float m = __int_as_float(imax[b]);
+  const float v = m > 0.f ? m : 1.f;
+  s[b] = v;
+  inv_s[b] = 1.f / v;
 }
 
 inline int grid_for(size_t n) { return (int)std::min<size_t>((n + 255) / 256, 4096); }
@@ -703,8 +736,7 @@ class WarmStartCnn {
     const int tgrid = conv_tc_grid(B, H, W);
     // conv_out: dW, db, and dh6 = conv(go, W7') (8 -> 32 channels, padded to 16 input channels)
     wgrad(8, h_[6].as<bf16>(), go_.as<bf16>(), B, H, W, W_[7].g.as<float>(), st);
-    bias_grad<<<8, 256, 0, st>>>(go_.as<bf16>(), npix, 8, B_[7].g.as<float>());
-    PDT_LAUNCH_CHECK();
+    bias_gradient(go_.as<bf16>(), npix, 8, B_[7].g.as<float>(), st);
     // go is [npix][8]; the data-gradient kernel needs 16 input channels: pad into go16_
     pad8to16(go_.as<bf16>(), npix, st);
     flip_transpose<<<64, 256, 0, st>>>(W_[7].wb.as<bf16>(), 8, CH, 16, CH, wt_.as<bf16>());
@@ -712,7 +744,7 @@ class WarmStartCnn {
     conv3x3_mma<16, CH, EPI_LINEAR><<<grid, 32 * TH, 0, st>>>(go16_.as<bf16>(), wt_.as<bf16>(), nullptr, H, W,
                                                               gtmp_.as<bf16>(), nullptr, nullptr);
     PDT_LAUNCH_CHECK();
-    count_launch(4);
+    count_launch(3);  // mse_loss, flip_transpose, conv3x3_mma (the bias gradient counts its own)
     // residual stream gradient G (FP32): G = dh6
     zero_acc(npix * CH, st);
     add_into<<<grid_for(npix * CH), 256, 0, st>>>(gacc_.as<float>(), gtmp_.as<bf16>(), npix * CH);
@@ -723,21 +755,28 @@ class WarmStartCnn {
       relu_bwd<<<grid_for(npix * CH), 256, 0, st>>>(gbf_.as<bf16>(), z_[l].as<bf16>(), npix * CH, gz_.as<bf16>());
       PDT_LAUNCH_CHECK();
       wgrad(CH, h_[l - 1].as<bf16>(), gz_.as<bf16>(), B, H, W, W_[l].g.as<float>(), st);
-      bias_grad<<<CH, 256, 0, st>>>(gz_.as<bf16>(), npix, CH, B_[l].g.as<float>());
+      bias_gradient(gz_.as<bf16>(), npix, CH, B_[l].g.as<float>(), st);
       flip_transpose<<<64, 256, 0, st>>>(W_[l].wb.as<bf16>(), CH, CH, CH, CH, wt_.as<bf16>());
       conv3x3_tc<EPI_LINEAR><<<tgrid, kConvTcThreads, kConvTcSmem, st>>>(gz_.as<bf16>(), wt_.as<bf16>(), nullptr, B, H, W,
                                                                        gtmp_.as<bf16>(), nullptr, err_.as<int>());
       add_into<<<grid_for(npix * CH), 256, 0, st>>>(gacc_.as<float>(), gtmp_.as<bf16>(), npix * CH);
       PDT_LAUNCH_CHECK();
-      count_launch(6);
+      count_launch(5);  // to_bf16, relu_bwd, flip_transpose, conv3x3_tc, add_into
     }
     // conv_in: h1 = relu(z_0): dz0 = G * relu'(z0)
     to_bf16<<<grid_for(npix * CH), 256, 0, st>>>(gacc_.as<float>(), npix * CH, gbf_.as<bf16>());
     relu_bwd<<<grid_for(npix * CH), 256, 0, st>>>(gbf_.as<bf16>(), z_[0].as<bf16>(), npix * CH, gz_.as<bf16>());
-    conv_in_wgrad<<<NTAP * CH, 256, 0, st>>>(x_.as<float>(), gz_.as<bf16>(), B, H, W, W_[0].g.as<float>(),
-                                             B_[0].g.as<float>());
-    PDT_LAUNCH_CHECK();
-    count_launch(3);
+    {
+      const int nb = kPartialBlocksPerSm * sms_;
+      bpart_.ensure(sizeof(float) * (size_t)nb * kConvInPartial);
+      conv_in_wgrad_partial<<<nb, 32 * NTAP, 0, st>>>(x_.as<float>(), gz_.as<bf16>(), B, H, W, bpart_.as<float>());
+      sum_partials<<<(NTAP * CH * 2 + 255) / 256, 256, 0, st>>>(bpart_.as<float>(), nb, kConvInPartial,
+                                                               NTAP * CH * 2, W_[0].g.as<float>());
+      sum_partials<<<1, CH, 0, st>>>(bpart_.as<float>() + NTAP * CH * 2, nb, kConvInPartial, CH,
+                                     B_[0].g.as<float>());
+      PDT_LAUNCH_CHECK();
+    }
+    count_launch(5);
     std::vector<double> h(lb);
     PDT_CUDA_CHECK(cudaMemcpyAsync(h.data(), part_.p, sizeof(double) * lb, cudaMemcpyDeviceToHost, st));
     PDT_CUDA_CHECK(cudaStreamSynchronize(st));
@@ -764,10 +803,14 @@ class WarmStartCnn {
   const float* output() const { return o_.as<float>(); }
   // per-image scales of u0 (device): s, 1/s
   void scales(const float2* u0, int B, size_t npix_img, cudaStream_t st) {
-    sc_.ensure(2 * sizeof(float) * std::max(B, 1));
-    image_scale<<<B, 256, 0, st>>>(u0, npix_img, sc_.as<float>(), sc_.as<float>() + B);
+    sc_.ensure(3 * sizeof(float) * std::max(B, 1));  // scale [B], inverse [B], maxima as int bits [B]
+    int* imax = reinterpret_cast<int*>(sc_.as<float>() + 2 * B);
+    PDT_CUDA_CHECK(cudaMemsetAsync(imax, 0, sizeof(int) * B, st));
+    const int nbx = (int)std::max<size_t>(1, std::min<size_t>((npix_img + 255) / 256, (size_t)sms_));
+    image_scale_max<<<dim3(nbx, B), 256, 0, st>>>(u0, npix_img, imax);
+    image_scale_finish<<<(B + 127) / 128, 128, 0, st>>>(imax, B, sc_.as<float>(), sc_.as<float>() + B);
     PDT_LAUNCH_CHECK();
-    count_launch();
+    count_launch(2);
   }
   const float* scale_ptr() const { return sc_.as<float>(); }
   const float* inv_scale_ptr(int B) const { return sc_.as<float>() + B; }
@@ -869,7 +912,21 @@ class WarmStartCnn {
   }
 
   CnnParam W_[kLayers], B_[kLayers];
-  DevBuf x_, h_[7], z_[7], o_, go_, go16_, gtmp_, gbf_, gz_, gacc_, wt_, wpart_, part_, t_, sc_, err_;
+  DevBuf x_, h_[7], z_[7], o_, go_, go16_, gtmp_, gbf_, gz_, gacc_, wt_, wpart_, part_, t_, sc_, err_, bpart_;
+
+  // Bias gradient db[c] = sum over pixels of dy[p][c] (C = 8 or 32): chunked partial sums, then the
+  // partials in block order.
+  void bias_gradient(const bf16* dy, size_t npix, int C, float* db, cudaStream_t st) {
+    const int nb = 2 * sms_;
+    bpart_.ensure(sizeof(float) * (size_t)kPartialBlocksPerSm * sms_ * kConvInPartial);
+    if (C == 8)
+      bias_grad_partial<8><<<nb, 256, 0, st>>>(dy, npix, bpart_.as<float>());
+    else
+      bias_grad_partial<CH><<<nb, 256, 0, st>>>(dy, npix, bpart_.as<float>());
+    sum_partials<<<1, 64, 0, st>>>(bpart_.as<float>(), nb, C, C, db);
+    PDT_LAUNCH_CHECK();
+    count_launch(2);
+  }
   int sms_ = 1;
   int B_n_ = 0, H_n_ = 0, W_n_ = 0;
   long step_ = 0;

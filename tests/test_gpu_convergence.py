@@ -97,3 +97,27 @@ def test_learned_warm_start_on_held_out_case(pdt):
     n_plain, e_plain = _iterations_to(plain, pp, u_star, 2000, 200000)
     assert n_warm is not None
     assert n_plain is None or n_warm < n_plain, (n_warm, n_plain, e_plain)
+
+
+def test_dual_weighted_limit_is_a_fixed_point_of_the_fp64_oracle(pdt, oracle):
+    """The state the GPU reaches with the dual-weighted steps, handed to the FP64 oracle of the reference
+    iteration (reference steps, tgvmrioptimizer.cu:120-200) as its starting state: 3000 FP64 iterations
+    move u by less than 1e-5 relative, so the limit is the reference method's converged solution."""
+    from primaldualtoolbox import synthetic, warmstart
+
+    case = synthetic.cartesian_case(C=3, H=48, W=32, roos=False, seed=31)
+    _, o, p = _solver(pdt, case, case["rawdata"], False)
+    o.setSteps(*warmstart.DUAL_WEIGHTED_STEPS)
+    p.max_iter = 39999
+    o.solve()
+    st = o.getState()
+    names = {"vbarx": "vbx", "vbary": "vby"}
+    state = {names.get(k, k): v.astype(np.complex128) for k, v in st.items()}
+    unsampled = ~(case["mask"] != 0).any(axis=0)
+    # the engine does not hold r on never-sampled lines; the reference's r there is (r + sigma (0 - f)) / (1 + sigma)
+    # iterated from 0, i.e. it tends to -f, which is 0 for these (masked) data
+    assert np.all(case["rawdata"][:, :, unsampled] == 0)
+    u64 = oracle.op_solve("cartesian", case["sens"], case["mask"], case["rawdata"], "tgv_mri",
+                          alpha0=float(np.float32(case["alpha0"])), alpha1=float(np.float32(case["alpha1"])),
+                          reduction=1.0, max_iter=2999, prec=64, state=state)
+    assert np.linalg.norm(u64 - st["u"]) / np.linalg.norm(st["u"]) <= 1e-5
