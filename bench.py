@@ -710,24 +710,11 @@ RAD_N, RAD_C, RAD_SPOKES, RAD_RO, RAD_OSF, RAD_KW = 256, 12, 64, 512, 1.5, 3
 def _radial_problem(pdt, seed):
     """Config 5: 256 x 256 image, 12 coils, 64 golden-angle spokes x 512 readout samples (2x readout
     oversampling), Kaiser-Bessel width 3 on a 1.5x grid, density weights sqrt|k|, a seeded phantom and
-    seeded coil maps; f = A u + 1 % complex noise."""
-    from primaldualtoolbox import synthetic
+    seeded coil maps; f = A u + 1 % complex noise (primaldualtoolbox.warmstart.radial_problem)."""
+    from primaldualtoolbox import warmstart
 
-    ang = np.arange(RAD_SPOKES) * np.pi * (np.sqrt(5) - 1) / 2
-    r = (np.arange(RAD_RO) - RAD_RO / 2) / RAD_RO
-    k = (r[:, None] * np.exp(1j * ang[None, :])).ravel()
-    traj = np.array([k.imag, k.real]).astype(np.float32)  # [imag, real] as bin/mri_radial_test.py:38
-    dcf = np.sqrt(np.abs(k)).astype(np.float32)[None, :]
-    op = pdt.mri.MriRadialOperator({"osf": RAD_OSF, "sector_width": 8, "kernel_width": RAD_KW, "img_dim": RAD_N})
-    op.setTrajectory(traj)
-    op.setDcf(dcf)
-    op.setCoilSens(synthetic.coil_maps(RAD_C, RAD_N, RAD_N, seed=seed))
-    f = op.forward(synthetic.mri_phantom(RAD_N, RAD_N, seed=seed))
-    rng = np.random.default_rng(seed)
-    f = f + (0.01 * np.abs(f).max() * (rng.standard_normal(f.shape) + 1j * rng.standard_normal(f.shape))).astype(
-        np.complex64)
-    alpha1 = 0.02 * float(np.abs(op.adjoint(f)).max())
-    return op, f, alpha1
+    return warmstart.radial_problem(pdt, seed, N=RAD_N, C=RAD_C, spokes=RAD_SPOKES, readout=RAD_RO, osf=RAD_OSF,
+                                    kernel_width=RAD_KW)
 
 
 def _radial_bytes():
@@ -792,7 +779,7 @@ def run_radial(pdt, torch, slices, iters, converge=True):
         u0 = torch.empty((RAD_N, RAD_N), dtype=torch.complex64, device="cuda")
         op0.adjoint(fd, out=u0, stream=stream)
         torch.cuda.synchronize()
-        conv = time_to_accuracy(pdt, torch, make, u0, stream, weights=warmstart.CONFIG4_WEIGHTS, max_plain=150000)
+        conv = time_to_accuracy(pdt, torch, make, u0, stream, weights=warmstart.RADIAL_WEIGHTS, max_plain=150000)
         conv["operator_norm"] = op0.norm(iters=40)
     return {"workload": f"radial_tgv2_{RAD_C}c_{RAD_N}x{RAD_N}_{RAD_SPOKES}spokes_x{RAD_RO}",
             "osf": RAD_OSF, "kernel_width": RAD_KW, "iterations_per_slice": iters, "tuning": probs[0][0].tuning(),

@@ -402,13 +402,22 @@ __global__ void __launch_bounds__(256) bias_grad_partial(const bf16* __restrict_
   }
 }
 
-// out[i] = sum over blocks b (in order) of partial[b * stride + i], i < n.
-__global__ void sum_partials(const float* __restrict__ partial, int nblocks, int stride, int n, float* __restrict__ out) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+// out[i] = sum over blocks b of partial[b * stride + i], i < n: one CUDA block per output, its 128 threads
+// sum fixed strided subsets of the partials, then a fixed-order tree (the same order on every run).
+__global__ void __launch_bounds__(128) sum_partials(const float* __restrict__ partial, int nblocks, int stride, int n,
+                                                   float* __restrict__ out) {
+  __shared__ float sh[128];
+  const int i = blockIdx.x;
   if (i >= n) return;
   float s = 0.f;
-  for (int b = 0; b < nblocks; ++b) s += partial[(size_t)b * stride + i];
-  out[i] = s;
+  for (int b = threadIdx.x; b < nblocks; b += 128) s += partial[(size_t)b * stride + i];
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = 64; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[i] = sh[0];
 }
 
 // w'[tap'][ci][co] = w[8 - tap'][co][ci] (padded to COP output / CIP input channels) for the data gradient.
@@ -468,16 +477,28 @@ __global__ void __launch_bounds__(32 * NTAP) conv_in_wgrad_partial(const float* 
   const size_t p0 = (size_t)blockIdx.x * chunk, p1 = min(n, p0 + chunk);
   const float2* x2 = reinterpret_cast<const float2*>(x);
   float s0 = 0.f, s1 = 0.f, sb = 0.f;
-  for (size_t p = p0; p < p1; ++p) {
-    const int xx = (int)(p % W), yy = (int)((p / W) % H), b = (int)(p / ((size_t)W * H));
-    const float gv = __bfloat162float(g[p * CH + co]);
-    const int gy = yy + ky, gx = xx + kx;
-    if (gy >= 0 && gy < H && gx >= 0 && gx < W) {
-      const float2 xv = x2[((size_t)b * H + gy) * W + gx];
-      s0 += xv.x * gv;
-      s1 += xv.y * gv;
+  constexpr int U = 4;  // pixels whose loads are in flight together
+  for (size_t pb = p0; pb < p1; pb += U) {
+    float gv[U];
+    float2 xv[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const size_t p = pb + u;
+      gv[u] = 0.f;
+      xv[u] = c2(0.f, 0.f);
+      if (p < p1) {
+        const int xx = (int)(p % W), yy = (int)((p / W) % H), b = (int)(p / ((size_t)W * H));
+        gv[u] = __bfloat162float(g[p * CH + co]);
+        const int gy = yy + ky, gx = xx + kx;
+        if (gy >= 0 && gy < H && gx >= 0 && gx < W) xv[u] = x2[((size_t)b * H + gy) * W + gx];
+      }
     }
-    sb += gv;
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      s0 += xv[u].x * gv[u];
+      s1 += xv[u].y * gv[u];
+      sb += gv[u];
+    }
   }
   float* out = partial + (size_t)blockIdx.x * kConvInPartial;
   out[(tap * CH + co) * 2] = s0;
@@ -770,10 +791,9 @@ class WarmStartCnn {
       const int nb = kPartialBlocksPerSm * sms_;
       bpart_.ensure(sizeof(float) * (size_t)nb * kConvInPartial);
       conv_in_wgrad_partial<<<nb, 32 * NTAP, 0, st>>>(x_.as<float>(), gz_.as<bf16>(), B, H, W, bpart_.as<float>());
-      sum_partials<<<(NTAP * CH * 2 + 255) / 256, 256, 0, st>>>(bpart_.as<float>(), nb, kConvInPartial,
-                                                               NTAP * CH * 2, W_[0].g.as<float>());
-      sum_partials<<<1, CH, 0, st>>>(bpart_.as<float>() + NTAP * CH * 2, nb, kConvInPartial, CH,
-                                     B_[0].g.as<float>());
+      sum_partials<<<NTAP * CH * 2, 128, 0, st>>>(bpart_.as<float>(), nb, kConvInPartial, NTAP * CH * 2,
+                                                  W_[0].g.as<float>());
+      sum_partials<<<CH, 128, 0, st>>>(bpart_.as<float>() + NTAP * CH * 2, nb, kConvInPartial, CH, B_[0].g.as<float>());
       PDT_LAUNCH_CHECK();
     }
     count_launch(5);
@@ -923,7 +943,7 @@ class WarmStartCnn {
       bias_grad_partial<8><<<nb, 256, 0, st>>>(dy, npix, bpart_.as<float>());
     else
       bias_grad_partial<CH><<<nb, 256, 0, st>>>(dy, npix, bpart_.as<float>());
-    sum_partials<<<1, 64, 0, st>>>(bpart_.as<float>(), nb, C, C, db);
+    sum_partials<<<C, 128, 0, st>>>(bpart_.as<float>(), nb, C, C, db);
     PDT_LAUNCH_CHECK();
     count_launch(2);
   }

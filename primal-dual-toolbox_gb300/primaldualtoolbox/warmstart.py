@@ -32,6 +32,73 @@ _DATA = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data")
 DEFAULT_WEIGHTS = os.path.join(_DATA, "warmstart_15c_640x368.npz")
 # the learned-warm-start configuration: 15 coils, 320 x 320, 4x
 CONFIG4_WEIGHTS = os.path.join(_DATA, "warmstart_15c_320x320.npz")
+# radial: 12 coils, 256 x 256, 64 golden-angle spokes x 512 samples, Kaiser-Bessel width 3, grid 1.5x
+RADIAL_WEIGHTS = os.path.join(_DATA, "warmstart_radial_12c_256.npz")
+RADIAL_GEOMETRY = dict(N=256, C=12, spokes=64, readout=512, osf=1.5, kernel_width=3)
+
+
+def radial_trajectory(spokes=64, readout=512):
+    """(2, spokes * readout) float32 golden-angle trajectory in the reference sample's layout (row 0 the
+    imaginary, row 1 the real part of k, bin/mri_radial_test.py:38) and the density weights sqrt|k|."""
+    ang = np.arange(spokes) * np.pi * (np.sqrt(5) - 1) / 2
+    r = (np.arange(readout) - readout / 2) / readout
+    k = (r[:, None] * np.exp(1j * ang[None, :])).ravel()
+    return np.array([k.imag, k.real]).astype(np.float32), np.sqrt(np.abs(k)).astype(np.float32)[None, :]
+
+
+def radial_problem(pdt, seed, torch=None, N=256, C=12, spokes=64, readout=512, osf=1.5, kernel_width=3,
+                   noise=0.01, alpha_scale=0.02):
+    """A seeded radial TGV-MRI problem: MriRadialOperator with seeded coil maps, data f = A(phantom) plus
+    complex noise of `noise` x max|f|, alpha1 = alpha_scale x max|A^H f|. Returns (op, f, alpha1); f is a
+    device tensor when torch is given."""
+    from . import synthetic
+
+    traj, dcf = radial_trajectory(spokes, readout)
+    op = pdt.mri.MriRadialOperator({"osf": osf, "sector_width": 8, "kernel_width": kernel_width, "img_dim": N})
+    op.setTrajectory(traj)
+    op.setDcf(dcf)
+    op.setCoilSens(synthetic.coil_maps(C, N, N, seed=seed))
+    f = op.forward(synthetic.mri_phantom(N, N, seed=seed))
+    rng = np.random.default_rng(seed)
+    f = f + (noise * np.abs(f).max() * (rng.standard_normal(f.shape) + 1j * rng.standard_normal(f.shape))).astype(
+        np.complex64)
+    alpha1 = alpha_scale * float(np.abs(op.adjoint(f)).max())
+    if torch is not None:
+        f = torch.from_numpy(np.ascontiguousarray(f)).cuda()
+    return op, f, alpha1
+
+
+def make_radial_training_set(pdt, torch, n_cases, iters, seed0=1000, batch=16, log=print, steps=None):
+    """(u0, u*, v*) of n_cases seeded radial problems (RADIAL_GEOMETRY), u* after `iters` iterations at
+    fixed alpha with step sizes `steps` (None: the reference's), `batch` problems at a time."""
+    N = RADIAL_GEOMETRY["N"]
+    U0 = torch.empty((n_cases, N, N), dtype=torch.complex64, device="cuda")
+    UT = torch.empty_like(U0)
+    VT = torch.empty((n_cases, 2, N, N), dtype=torch.complex64, device="cuda")
+    t0 = time.time()
+    for start in range(0, n_cases, batch):
+        opts, keep = [], []
+        for i in range(start, min(n_cases, start + batch)):
+            op, f, a1 = radial_problem(pdt, seed0 + i, torch)
+            opt = pdt.mri.TgvMriOptimizer_2c2c()
+            prm = opt.getParameters()
+            prm.max_iter, prm.reduction, prm.alpha1, prm.alpha0 = iters - 1, 1.0, a1, 2 * a1
+            if steps:
+                opt.setSteps(*steps)
+            opt.setOperator(op)
+            opt.setNoisyData(f)
+            op.adjoint(f, out=U0[i])
+            opt.setInput0(U0[i])
+            opts.append((i, opt))
+            keep.append((op, f))
+        pdt.batch.BatchSolver([o for _, o in opts]).solve()
+        for i, opt in opts:
+            opt.getResult(out=UT[i])
+            opt.getField("vx", out=VT[i, 0])
+            opt.getField("vy", out=VT[i, 1])
+        torch.cuda.synchronize()
+        log(f"targets {min(n_cases, start + batch)}/{n_cases}  {time.time() - t0:.1f}s")
+    return U0, UT, VT
 
 # (tau, sigma) of the dual-weighted solve: the same primal-dual iteration with tau sigma = 1/16 (the
 # reference's TGV-MRI steps have tau sigma = 1/128; convergence needs tau sigma |K|^2 < 1, |K|^2 <= 13
@@ -244,6 +311,7 @@ def main():
     ap.add_argument("--iters", type=int, default=8000, help="dual-weighted iterations per training target")
     ap.add_argument("--shape", default="15,320,320", help="coils,FE,PE of the synthetic problems")
     ap.add_argument("--roos", type=int, default=0, help="1: readout-oversampling removal operator")
+    ap.add_argument("--radial", type=int, default=0, help="1: the radial geometry (RADIAL_GEOMETRY) instead")
     ap.add_argument("--epochs", type=int, default=12)
     ap.add_argument("--batch", type=int, default=8)
     ap.add_argument("--lr", type=float, default=1e-3)
@@ -253,10 +321,16 @@ def main():
     C, H, W = (int(x) for x in args.shape.split(","))
     shape = dict(C=C, H=H, W=W, roos=bool(args.roos))
     t0 = time.time()
-    U0, UT, VT = make_training_set(pdt, torch, args.cases, args.iters, **shape)
-    t_data = time.time() - t0
-    # held-out problems (other seeds) for the report
-    H0, HT, HV = make_training_set(pdt, torch, args.held_out, args.iters, seed0=500000, **shape)
+    if args.radial:
+        C, H, W = RADIAL_GEOMETRY["C"], RADIAL_GEOMETRY["N"], RADIAL_GEOMETRY["N"]
+        U0, UT, VT = make_radial_training_set(pdt, torch, args.cases, args.iters)
+        t_data = time.time() - t0
+        H0, HT, HV = make_radial_training_set(pdt, torch, args.held_out, args.iters, seed0=500000)
+    else:
+        U0, UT, VT = make_training_set(pdt, torch, args.cases, args.iters, **shape)
+        t_data = time.time() - t0
+        # held-out problems (other seeds) for the report
+        H0, HT, HV = make_training_set(pdt, torch, args.held_out, args.iters, seed0=500000, **shape)
     net = WarmStartNet(seed=0)
     t1 = time.time()
     losses = train(net, U0, UT, VT, epochs=args.epochs, batch=args.batch, lr=args.lr)
@@ -265,7 +339,7 @@ def main():
     held = evaluate(net, torch, H0, HT)
     net.save(args.out, cases=args.cases, target_iters=args.iters, epochs=args.epochs, batch=args.batch, lr=args.lr,
              losses=losses, data_seconds=t_data, train_seconds=t_train, shape=[C, H, W], roos=int(args.roos), accel=4,
-             target_steps=list(DUAL_WEIGHTED_STEPS), held_out=held)
+             target_steps=None if args.radial else list(DUAL_WEIGHTED_STEPS), radial=int(args.radial), held_out=held)
     print(json.dumps({"out": args.out, "losses": losses, "data_s": round(t_data, 1), "train_s": round(t_train, 1),
                       "held_out": held}))
 
