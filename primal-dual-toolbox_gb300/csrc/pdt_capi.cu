@@ -7,6 +7,8 @@
 #include <functional>
 #include <iostream>
 #include <map>
+#include <mutex>
+#include <tuple>
 #include <memory>
 #include <random>
 #include <sstream>
@@ -703,6 +705,12 @@ class OptImpl {
         launch_tgv_denoise_step(cplx_, W_, H_, ptrs(in), ptrs(out), f_.p, tau, sigma, lambda, a0, a1, s);
         if (prof_) prof_->mark("tgv_denoise_step", s);
       };
+    } else if (!tv_multi_faster(tau, sigma, lambda, st)) {
+      pl.body = [=](int par, cudaStream_t s) {
+        const int in = p0 ^ par, out = in ^ 1;
+        launch_tv_step(cplx_, W_, H_, ptrs(in), ptrs(out), f_.p, tau, sigma, lambda, s);
+        if (prof_) prof_->mark("tv_step", s);
+      };
     } else {
       // kTvStepsPerLaunch iterations per launch, then the remainder one at a time
       pl.n = pl.iters / kTvStepsPerLaunch;
@@ -721,6 +729,56 @@ class OptImpl {
     pl.key = graph_key({(uintptr_t)img_.p, (uintptr_t)f_.p, (uintptr_t)W_, (uintptr_t)H_, (uintptr_t)p0,
                         (uintptr_t)cplx_, fbits(lambda), fbits(a0), fbits(a1)});
     return pl;
+  }
+
+  // TV denoising runs kTvStepsPerLaunch iterations per launch (temporal blocking in shared memory, the
+  // faster choice while the state stays in L2) or one per launch (for large images the halo recompute can
+  // cost more than the DRAM passes it saves). Images of at least 2^20 pixels time both once per
+  // (W, H, pixel type) on zeroed scratch state -- 2 x 4 iterations against 8, best of two -- and the
+  // choice is kept for the process.
+  bool tv_multi_faster(float tau, float sigma, float lambda, cudaStream_t st) {
+    if ((size_t)W_ * H_ < ((size_t)1 << 20)) return true;
+    static std::mutex mu;
+    static std::map<std::tuple<int, int, bool>, bool> cache;
+    const auto key = std::make_tuple(W_, H_, cplx_);
+    std::lock_guard<std::mutex> lock(mu);
+    auto hit = cache.find(key);
+    if (hit != cache.end()) return hit->second;
+    DevBuf scratch;
+    scratch.ensure(img_.bytes);
+    PDT_CUDA_CHECK(cudaMemsetAsync(scratch.p, 0, scratch.bytes, st));
+    auto sp = [&](int set) {
+      ImgPtrs p = ptrs(set);
+      const ptrdiff_t shift = static_cast<char*>(scratch.p) - static_cast<char*>(img_.p);
+      for (void** q : {&p.u, &p.ub, &p.vx, &p.vy, &p.vbx, &p.vby, &p.px, &p.py, &p.qxx, &p.qyy, &p.qxy})
+        *q = static_cast<char*>(*q) + shift;
+      return p;
+    };
+    const uint64_t launches0 = g_launches.load();
+    cudaEvent_t e0, e1, e2;
+    PDT_CUDA_CHECK(cudaEventCreate(&e0));
+    PDT_CUDA_CHECK(cudaEventCreate(&e1));
+    PDT_CUDA_CHECK(cudaEventCreate(&e2));
+    float best_multi = 1e30f, best_single = 1e30f;
+    for (int rep = 0; rep < 2; ++rep) {
+      PDT_CUDA_CHECK(cudaEventRecord(e0, st));
+      for (int i = 0; i < 2; ++i) launch_tv_multi_step(cplx_, W_, H_, sp(i & 1), sp((i & 1) ^ 1), f_.p, tau, sigma, lambda, st);
+      PDT_CUDA_CHECK(cudaEventRecord(e1, st));
+      for (int i = 0; i < 2 * kTvStepsPerLaunch; ++i)
+        launch_tv_step(cplx_, W_, H_, sp(i & 1), sp((i & 1) ^ 1), f_.p, tau, sigma, lambda, st);
+      PDT_CUDA_CHECK(cudaEventRecord(e2, st));
+      PDT_CUDA_CHECK(cudaEventSynchronize(e2));
+      float m = 0, g = 0;
+      PDT_CUDA_CHECK(cudaEventElapsedTime(&m, e0, e1));
+      PDT_CUDA_CHECK(cudaEventElapsedTime(&g, e1, e2));
+      best_multi = std::min(best_multi, m);
+      best_single = std::min(best_single, g);
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaEventDestroy(e2);
+    g_launches.fetch_sub(g_launches.load() - launches0);  // tuning launches are not solver work
+    return cache[key] = best_multi <= best_single;
   }
 
   // TgvMriOptimizer::solve (tgvmrioptimizer.cu:93-203), TgvOptimizerWithOp::solve

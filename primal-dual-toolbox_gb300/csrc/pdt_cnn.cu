@@ -362,6 +362,134 @@ __global__ void __launch_bounds__(32 * NTAP) wgrad_mma(const bf16* __restrict__ 
       }
 }
 
+// Weight gradient of a 32 -> 32 layer on the tensor cores (tcgen05, kind::f16 BF16, FP32 in TMEM):
+//   dW[ky 3 + kx][co][ci] = sum_p x[p + (ky - 1, kx - 1)][ci] dy[p][co]
+// as D_ky[m = kx 32 + ci][n = co] = sum_k A[m][k] B[n][k] with K = the 16 pixels of one tile row: A is the
+// input tile shifted by kx (rows 96..127 zero), B the output gradient. Per 16 x 8 tile and tile row py,
+// three MMAs (ky = 0, 1, 2: A from halo row py + ky) of M = 128, N = 32, K = 16 into three accumulators
+// (TMEM columns 32 ky). Operands in shared memory in the no-swizzle K-major layout (a core matrix is 8
+// rows x 8 pixels, 16 bytes per row; the tile is staged transposed from the [pixel][channel] activations):
+//   A: [halo row 10][pixel half 2][row group 16][128 B], row group = 4 kx + ci / 8  (LBO 2048, SBO 128)
+//   B: [tile row 8][pixel half 2][channel group 4][128 B]                          (LBO 512, SBO 128)
+// CTAs are persistent over tiles and accumulate in TMEM; each writes partial[block][tap][co][ci], which
+// wgrad_reduce adds in block order.
+constexpr int kWgThreads = 256;
+constexpr uint32_t kWgA = 20 * 2048;  // 40 KB
+constexpr uint32_t kWgB = 16 * 512;   // 8 KB
+constexpr size_t kWgSmem = 1024 + kWgA + kWgB + 64;
+
+__device__ __forceinline__ void st_shared_b16(uint32_t addr, uint16_t v) {
+  asm volatile("st.shared.b16 [%0], %1;" ::"r"(addr), "h"(v) : "memory");
+}
+__device__ __forceinline__ uint16_t u4_elem(const uint4& v, int e) {
+  const uint32_t w = e < 2 ? v.x : e < 4 ? v.y : e < 6 ? v.z : v.w;
+  return (uint16_t)((e & 1) ? (w >> 16) : (w & 0xFFFFu));
+}
+
+__global__ void __launch_bounds__(kWgThreads) wgrad_tc(const bf16* __restrict__ x, const bf16* __restrict__ dy, int B,
+                                                       int H, int W, float* __restrict__ partial, int* __restrict__ err) {
+  extern __shared__ unsigned char wg_smem_raw[];
+  const uint32_t off = tc::smem_addr(wg_smem_raw);
+  unsigned char* sm = wg_smem_raw + ((1024u - (off & 1023u)) & 1023u);
+  const uint32_t a_base = tc::smem_addr(sm), b_base = a_base + kWgA;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(sm + kWgA + kWgB);
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(bar + 1);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int ntx = (W + TW - 1) / TW, nty = (H + TH - 1) / TH;
+  const int ntiles = ntx * nty * B;
+  if (tid == 0) {
+    tc::mbar_init(bar, 1);
+    tc::fence_mbar_init();
+  }
+  if (warp == 0) tc::tmem_alloc(tslot, 128);
+  // the zero rows 96..127 of A (row groups 12..15 of every block), written once
+  for (int i = tid; i < 20 * 4 * 8; i += kWgThreads) {
+    const int blk = i >> 5, g = 12 + ((i >> 3) & 3), q = i & 7;
+    asm volatile("st.shared.v4.b32 [%0], {%1, %1, %1, %1};" ::"r"(a_base + (blk * 16 + g) * 128 + q * 16), "r"(0u)
+                 : "memory");
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = *tslot;
+  const bool drop = tc::g_drop_arrival != 0;
+  bool ok = true;
+  int it = 0;
+  for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x, ++it) {
+    const int bx = t % ntx, by = (t / ntx) % nty, b = t / (ntx * nty);
+    const int x0 = bx * TW, y0 = by * TH;
+    // x halo tile -> A, transposed and shifted: item (halo row, halo column, channel group of 8)
+    for (int i = tid; i < (TH + 2) * (TW + 2) * 4; i += kWgThreads) {
+      const int cg = i & 3, col = (i >> 2) % (TW + 2), hy = (i >> 2) / (TW + 2);
+      const int gy = y0 + hy - 1, gx = x0 + col - 1;
+      uint4 v = make_uint4(0u, 0u, 0u, 0u);
+      if (gy >= 0 && gy < H && gx >= 0 && gx < W)
+        v = __ldg(reinterpret_cast<const uint4*>(x + (((size_t)b * H + gy) * W + gx) * CH) + cg);
+#pragma unroll
+      for (int kx = 0; kx < 3; ++kx) {
+        const int px = col - kx;
+        if (px < 0 || px >= TW) continue;
+        const uint32_t base = a_base + ((hy * 2 + (px >> 3)) * 16 + kx * 4 + cg) * 128 + (px & 7) * 2;
+#pragma unroll
+        for (int e = 0; e < 8; ++e) st_shared_b16(base + e * 16, u4_elem(v, e));
+      }
+    }
+    // dy tile -> B, transposed: item (tile row, pixel, channel group)
+    for (int i = tid; i < TH * TW * 4; i += kWgThreads) {
+      const int cg = i & 3, px = (i >> 2) % TW, py = (i >> 2) / TW;
+      const int gy = y0 + py, gx = x0 + px;
+      uint4 v = make_uint4(0u, 0u, 0u, 0u);
+      if (gy < H && gx < W) v = __ldg(reinterpret_cast<const uint4*>(dy + (((size_t)b * H + gy) * W + gx) * CH) + cg);
+      const uint32_t base = b_base + ((py * 2 + (px >> 3)) * 4 + cg) * 128 + (px & 7) * 2;
+#pragma unroll
+      for (int e = 0; e < 8; ++e) st_shared_b16(base + e * 16, u4_elem(v, e));
+    }
+    tc::fence_async_smem();
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    // (the test hook withholds block 0's first tile: no MMAs and no commit, so the wait below runs out)
+    if (tid == 0 && !(it == 0 && blockIdx.x == 0 && drop)) {
+      const uint32_t idesc = tc::idesc_bf16(128, CH);
+      for (int py = 0; py < TH; ++py)
+        for (int ky = 0; ky < 3; ++ky)
+          tc::mma_bf16(tmem + 32 * ky, tc::desc_interleave(a_base + (py + ky) * 2 * 2048, 2048, 128),
+                       tc::desc_interleave(b_base + py * 2 * 512, 512, 128), idesc, (it > 0 || py > 0) ? 1u : 0u);
+      tc::mma_commit(bar);
+    }
+    ok = tc::mbar_wait(bar, it & 1);
+    if (!ok) tc::mbar_wait(bar, it & 1);  // wait (bounded) for MMAs still in flight before the tiles are reused
+    tc::fence_after_sync();
+    ok = __syncthreads_and(ok);
+  }
+  // epilogue: TMEM lane m = kx 32 + ci (warps 0..3 own lanes 32 w .. 32 w + 31), column 32 ky + co
+  if (ok && warp < 4) {
+    const int m = 32 * warp + lane;
+    const uint32_t taddr = tmem + ((uint32_t)(32 * warp) << 16);
+    float* pb = partial + (size_t)blockIdx.x * NTAP * CH * CH;
+#pragma unroll
+    for (int ky = 0; ky < 3; ++ky) {
+      float v[16];
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        tc::tmem_ld16(taddr + 32 * ky + 16 * h, v);
+        if (m < 96) {
+          const int kx = m >> 5, ci = m & 31, tap = ky * 3 + kx;
+#pragma unroll
+          for (int j = 0; j < 16; ++j) pb[((size_t)tap * CH + 16 * h + j) * CH + ci] = v[j];
+        }
+      }
+    }
+  }
+  if (!ok && tid == 0) atomicCAS(err, 0, 0x2100);
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) {
+    tc::fence_after_sync();
+    tc::tmem_dealloc(tmem, 128);
+  }
+}
+
 // grad[i] = sum_b partial[b][i] (block order)
 __global__ void wgrad_reduce(const float* __restrict__ partial, int nblocks, int n, float* __restrict__ grad) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -371,7 +499,6 @@ __global__ void wgrad_reduce(const float* __restrict__ partial, int nblocks, int
   }
 }
 
-// db[co] = sum over pixels of dy[p][co]: one block per channel, fixed-order tree.
 // Per-channel sums of dy [npix][C] (the bias gradient), stage 1: block b sums the pixels of its contiguous
 // chunk -- C / 2 threads per pixel, two channels each, so that a warp reads consecutive bytes -- and writes
 // partial[b][C]; sum_partials adds the blocks' partials in block order (deterministic).
@@ -672,6 +799,7 @@ class WarmStartCnn {
     }
     for (auto fn : {conv3x3_tc<EPI_LINEAR>, conv3x3_tc<EPI_RELU_RES>})
       PDT_CUDA_CHECK(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kConvTcSmem));
+    PDT_CUDA_CHECK(cudaFuncSetAttribute(wgrad_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kWgSmem));
     err_.ensure(sizeof(int));
     PDT_CUDA_CHECK(cudaMemset(err_.p, 0, sizeof(int)));
     int dev = 0;
@@ -918,11 +1046,12 @@ class WarmStartCnn {
     PDT_CUDA_CHECK(cudaGetDevice(&dev));
     PDT_CUDA_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     const int tiles = B * ((W + TW - 1) / TW) * ((H + TH - 1) / TH);
-    const int nb = std::max(1, std::min(sms * 2, tiles));
+    // the tensor-core kernel: three persistent CTAs per SM (128 TMEM columns, 50 KB shared memory each)
+    const int nb = std::max(1, std::min(sms * (cout == CH ? 3 : 2), tiles));
     const int n = NTAP * cout * CH;
-    wpart_.ensure((size_t)nb * NTAP * CH * CH * sizeof(float));
+    wpart_.ensure((size_t)std::max(1, std::min(sms * 3, tiles)) * NTAP * CH * CH * sizeof(float));
     if (cout == CH)
-      wgrad_mma<CH><<<nb, 32 * NTAP, 0, st>>>(x, dy, B, H, W, wpart_.as<float>());
+      wgrad_tc<<<nb, kWgThreads, kWgSmem, st>>>(x, dy, B, H, W, wpart_.as<float>(), err_.as<int>());
     else
       wgrad_mma<8><<<nb, 32 * NTAP, 0, st>>>(x, dy, B, H, W, wpart_.as<float>());
     PDT_LAUNCH_CHECK();
