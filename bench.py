@@ -371,7 +371,7 @@ def run_ours(args):
 
     radial = None
     if args.radial_slices > 0:
-        radial = run_radial(pdt, torch, args.radial_slices, args.radial_iters)
+        radial = run_radial(pdt, torch, args.radial_slices, args.radial_iters, converge=bool(args.accuracy))
 
     batched = None
     if args.batch_cases > 0:

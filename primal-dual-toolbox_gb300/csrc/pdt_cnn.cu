@@ -490,6 +490,18 @@ __global__ void __launch_bounds__(kWgThreads) wgrad_tc(const bf16* __restrict__ 
   }
 }
 
+// Two-level fixed-order sum of partial[b][i] over the blocks b: stage 1 adds block range s (blockIdx.y) into
+// tmp[s][i], stage 2 (wgrad_reduce with nblocks = the range count) adds the ranges in order.
+constexpr int kWgRanges = 16;
+__global__ void wgrad_reduce_ranges(const float* __restrict__ partial, int nblocks, int n, float* __restrict__ tmp) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x, r = blockIdx.y;
+  if (i >= n) return;
+  const int b0 = (int)((long long)r * nblocks / gridDim.y), b1 = (int)((long long)(r + 1) * nblocks / gridDim.y);
+  float s = 0.f;
+  for (int b = b0; b < b1; ++b) s += partial[(size_t)b * n + i];
+  tmp[(size_t)r * n + i] = s;
+}
+
 // grad[i] = sum_b partial[b][i] (block order)
 __global__ void wgrad_reduce(const float* __restrict__ partial, int nblocks, int n, float* __restrict__ grad) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -1055,13 +1067,15 @@ class WarmStartCnn {
     else
       wgrad_mma<8><<<nb, 32 * NTAP, 0, st>>>(x, dy, B, H, W, wpart_.as<float>());
     PDT_LAUNCH_CHECK();
-    wgrad_reduce<<<grid_for(n), 256, 0, st>>>(wpart_.as<float>(), nb, n, grad);
+    wtmp_.ensure(sizeof(float) * (size_t)kWgRanges * NTAP * CH * CH);
+    wgrad_reduce_ranges<<<dim3((n + 255) / 256, kWgRanges), 256, 0, st>>>(wpart_.as<float>(), nb, n, wtmp_.as<float>());
+    wgrad_reduce<<<grid_for(n), 256, 0, st>>>(wtmp_.as<float>(), kWgRanges, n, grad);
     PDT_LAUNCH_CHECK();
-    count_launch(2);
+    count_launch(3);
   }
 
   CnnParam W_[kLayers], B_[kLayers];
-  DevBuf x_, h_[7], z_[7], o_, go_, go16_, gtmp_, gbf_, gz_, gacc_, wt_, wpart_, part_, t_, sc_, err_, bpart_;
+  DevBuf x_, h_[7], z_[7], o_, go_, go16_, gtmp_, gbf_, gz_, gacc_, wt_, wpart_, part_, t_, sc_, err_, bpart_, wtmp_;
 
   // Bias gradient db[c] = sum over pixels of dy[p][c] (C = 8 or 32): chunked partial sums, then the
   // partials in block order.

@@ -21,6 +21,7 @@
 //   rad_rows_inv   IFFT along x, crop, / deap, conj(sens_c) . and the coil sum
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <sstream>
 
@@ -652,6 +653,11 @@ class RadialOp : public OpImpl, public SolverHooks {
     const int rows_per_block = fast_.ok() ? fast_.per_block() : kRR;
     const int row_blocks = (N + rows_per_block - 1) / rows_per_block;
     G_ = std::max(1, std::min(C, (2 * g_rad_sms + row_blocks - 1) / row_blocks));
+    if (const char* env = std::getenv("PDT_RADIAL_GROUPS")) {  // coil groups of the adjoint row pass, pinned
+      const int g = std::atoi(env);
+      if (g < 1 || g > C) throw Error(PDT_ERR_INVALID_ARGUMENT, "PDT_RADIAL_GROUPS must be 1 .. coils");
+      G_ = g;
+    }
     dev_ = d;
     prepared_ = true;
   }
