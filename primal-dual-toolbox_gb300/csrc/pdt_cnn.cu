@@ -601,48 +601,57 @@ __global__ void conv_in_fwd(const float* __restrict__ x, const float* __restrict
 
 // First-layer weight gradient: dW[tap][co][cj] = sum_p x[p + d][cj] g[p][co]; block per (tap, co).
 // Weight and bias gradients of the 2 -> 32 input layer, stage 1: block b takes a contiguous chunk of
-// pixels; warp `tap` (nine warps), lane co; g is read as 64 consecutive bytes per pixel and x (two FP32
-// channels) is broadcast. partial[b][(tap CH + co) 2 + ci] = sum x[p + d(tap)][ci] g[p][co];
-// partial[b][NTAP CH 2 + co] = sum g[p][co]. sum_partials adds the blocks in order.
+// pixels; lane = output channel co, the eight warps take every eighth pixel of the chunk; for each pixel a
+// warp reads g[p][0..31] once (64 consecutive bytes) and the two input channels at the nine neighbours
+// (broadcast), and accumulates all 9 x 2 weight terms and the bias term. The warps' sums are added in warp
+// order in shared memory: partial[b][(tap CH + co) 2 + ci] = sum x[p + d(tap)][ci] g[p][co],
+// partial[b][NTAP CH 2 + co] = sum g[p][co]. sum_partials adds the blocks in a fixed order.
 constexpr int kConvInPartial = NTAP * CH * 2 + CH;
 constexpr int kPartialBlocksPerSm = 8;  // blocks per SM of the input-layer gradient (short chunks, more in flight)
-__global__ void __launch_bounds__(32 * NTAP) conv_in_wgrad_partial(const float* __restrict__ x,
-                                                                   const bf16* __restrict__ g, int B, int H, int W,
-                                                                   float* __restrict__ partial) {
-  const int tap = threadIdx.x >> 5, co = threadIdx.x & 31;
-  const int ky = tap / 3 - 1, kx = tap % 3 - 1;
+constexpr int kConvInWarps = 8;
+__global__ void __launch_bounds__(32 * kConvInWarps) conv_in_wgrad_partial(const float* __restrict__ x,
+                                                                           const bf16* __restrict__ g, int B, int H,
+                                                                           int W, float* __restrict__ partial) {
+  __shared__ float sh[kConvInWarps][2 * NTAP + 1][CH];
+  const int co = threadIdx.x & 31, w = threadIdx.x >> 5;
   const size_t n = (size_t)B * H * W;
   const size_t chunk = (n + gridDim.x - 1) / gridDim.x;
   const size_t p0 = (size_t)blockIdx.x * chunk, p1 = min(n, p0 + chunk);
   const float2* x2 = reinterpret_cast<const float2*>(x);
-  float s0 = 0.f, s1 = 0.f, sb = 0.f;
-  constexpr int U = 4;  // pixels whose loads are in flight together
-  for (size_t pb = p0; pb < p1; pb += U) {
-    float gv[U];
-    float2 xv[U];
+  float acc[NTAP][2], sb = 0.f;
 #pragma unroll
-    for (int u = 0; u < U; ++u) {
-      const size_t p = pb + u;
-      gv[u] = 0.f;
-      xv[u] = c2(0.f, 0.f);
-      if (p < p1) {
-        const int xx = (int)(p % W), yy = (int)((p / W) % H), b = (int)(p / ((size_t)W * H));
-        gv[u] = __bfloat162float(g[p * CH + co]);
-        const int gy = yy + ky, gx = xx + kx;
-        if (gy >= 0 && gy < H && gx >= 0 && gx < W) xv[u] = x2[((size_t)b * H + gy) * W + gx];
+  for (int t = 0; t < NTAP; ++t) acc[t][0] = acc[t][1] = 0.f;
+  for (size_t p = p0 + w; p < p1; p += kConvInWarps) {
+    const int xx = (int)(p % W), yy = (int)((p / W) % H), b = (int)(p / ((size_t)W * H));
+    const float gv = __bfloat162float(g[p * CH + co]);
+    sb += gv;
+#pragma unroll
+    for (int t = 0; t < NTAP; ++t) {
+      const int gy = yy + t / 3 - 1, gx = xx + t % 3 - 1;
+      if (gy >= 0 && gy < H && gx >= 0 && gx < W) {
+        const float2 xv = x2[((size_t)b * H + gy) * W + gx];
+        acc[t][0] += xv.x * gv;
+        acc[t][1] += xv.y * gv;
       }
     }
-#pragma unroll
-    for (int u = 0; u < U; ++u) {
-      s0 += xv[u].x * gv[u];
-      s1 += xv[u].y * gv[u];
-      sb += gv[u];
-    }
   }
+#pragma unroll
+  for (int t = 0; t < NTAP; ++t) {
+    sh[w][2 * t][co] = acc[t][0];
+    sh[w][2 * t + 1][co] = acc[t][1];
+  }
+  sh[w][2 * NTAP][co] = sb;
+  __syncthreads();
   float* out = partial + (size_t)blockIdx.x * kConvInPartial;
-  out[(tap * CH + co) * 2] = s0;
-  out[(tap * CH + co) * 2 + 1] = s1;
-  if (tap == 0) out[NTAP * CH * 2 + co] = sb;
+  for (int i = threadIdx.x; i < (2 * NTAP + 1) * CH; i += blockDim.x) {
+    const int j = i / CH, c = i - j * CH;  // j = 2 tap + ci, or 2 NTAP for the bias
+    float s = 0.f;
+    for (int ww = 0; ww < kConvInWarps; ++ww) s += sh[ww][j][c];
+    if (j < 2 * NTAP)
+      out[((j >> 1) * CH + c) * 2 + (j & 1)] = s;
+    else
+      out[NTAP * CH * 2 + c] = s;
+  }
 }
 
 // g = gin * relu'(z)   (BF16 in and out)
@@ -930,7 +939,8 @@ class WarmStartCnn {
     {
       const int nb = kPartialBlocksPerSm * sms_;
       bpart_.ensure(sizeof(float) * (size_t)nb * kConvInPartial);
-      conv_in_wgrad_partial<<<nb, 32 * NTAP, 0, st>>>(x_.as<float>(), gz_.as<bf16>(), B, H, W, bpart_.as<float>());
+      conv_in_wgrad_partial<<<nb, 32 * kConvInWarps, 0, st>>>(x_.as<float>(), gz_.as<bf16>(), B, H, W,
+                                                              bpart_.as<float>());
       sum_partials<<<NTAP * CH * 2, 128, 0, st>>>(bpart_.as<float>(), nb, kConvInPartial, NTAP * CH * 2,
                                                   W_[0].g.as<float>());
       sum_partials<<<CH, 128, 0, st>>>(bpart_.as<float>() + NTAP * CH * 2, nb, kConvInPartial, CH, B_[0].g.as<float>());
