@@ -666,6 +666,32 @@ __global__ void add_into(float* __restrict__ acc, const bf16* __restrict__ g, si
     acc[i] += __bfloat162float(g[i]);
 }
 
+// g = bf16(acc) * relu'(z): the residual stream's FP32 gradient rounded to BF16 (the same rounding as a
+// separate conversion) and masked by the ReLU's derivative, four elements per thread.
+__global__ void relu_bwd_acc(const float* __restrict__ acc, const bf16* __restrict__ z, size_t n, bf16* __restrict__ g) {
+  const size_t n4 = n / 4;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n4; i += (size_t)gridDim.x * blockDim.x) {
+    const float4 a = reinterpret_cast<const float4*>(acc)[i];
+    const uint2 zz = reinterpret_cast<const uint2*>(z)[i];
+    const __nv_bfloat162 z01 = *reinterpret_cast<const __nv_bfloat162*>(&zz.x);
+    const __nv_bfloat162 z23 = *reinterpret_cast<const __nv_bfloat162*>(&zz.y);
+    const bf16 zero = __float2bfloat16(0.f);
+    const bf16 g0 = __bfloat162float(z01.x) > 0.f ? __float2bfloat16(a.x) : zero;
+    const bf16 g1 = __bfloat162float(z01.y) > 0.f ? __float2bfloat16(a.y) : zero;
+    const bf16 g2 = __bfloat162float(z23.x) > 0.f ? __float2bfloat16(a.z) : zero;
+    const bf16 g3 = __bfloat162float(z23.y) > 0.f ? __float2bfloat16(a.w) : zero;
+    uint2 o;
+    __nv_bfloat162 o01, o23;
+    o01.x = g0;
+    o01.y = g1;
+    o23.x = g2;
+    o23.y = g3;
+    o.x = *reinterpret_cast<const uint32_t*>(&o01);
+    o.y = *reinterpret_cast<const uint32_t*>(&o23);
+    reinterpret_cast<uint2*>(g)[i] = o;
+  }
+}
+
 __global__ void to_bf16(const float* __restrict__ a, size_t n, bf16* __restrict__ out) {
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
     out[i] = __float2bfloat16(a[i]);
@@ -921,8 +947,8 @@ class WarmStartCnn {
     PDT_LAUNCH_CHECK();
     for (int l = 6; l >= 1; --l) {
       // h_l = h_{l-1} + relu(z_l), z_l = conv_l(h_{l-1}):  dz = G * relu'(z_l); dh_{l-1} = G + conv_l^T(dz)
-      to_bf16<<<grid_for(npix * CH), 256, 0, st>>>(gacc_.as<float>(), npix * CH, gbf_.as<bf16>());
-      relu_bwd<<<grid_for(npix * CH), 256, 0, st>>>(gbf_.as<bf16>(), z_[l].as<bf16>(), npix * CH, gz_.as<bf16>());
+      relu_bwd_acc<<<grid_for(npix * CH / 4), 256, 0, st>>>(gacc_.as<float>(), z_[l].as<bf16>(), npix * CH,
+                                                             gz_.as<bf16>());
       PDT_LAUNCH_CHECK();
       wgrad(CH, h_[l - 1].as<bf16>(), gz_.as<bf16>(), B, H, W, W_[l].g.as<float>(), st);
       bias_gradient(gz_.as<bf16>(), npix, CH, B_[l].g.as<float>(), st);
@@ -931,11 +957,11 @@ class WarmStartCnn {
                                                                        gtmp_.as<bf16>(), nullptr, err_.as<int>());
       add_into<<<grid_for(npix * CH), 256, 0, st>>>(gacc_.as<float>(), gtmp_.as<bf16>(), npix * CH);
       PDT_LAUNCH_CHECK();
-      count_launch(5);  // to_bf16, relu_bwd, flip_transpose, conv3x3_tc, add_into
+      count_launch(4);  // relu_bwd_acc, flip_transpose, conv3x3_tc, add_into
     }
     // conv_in: h1 = relu(z_0): dz0 = G * relu'(z0)
-    to_bf16<<<grid_for(npix * CH), 256, 0, st>>>(gacc_.as<float>(), npix * CH, gbf_.as<bf16>());
-    relu_bwd<<<grid_for(npix * CH), 256, 0, st>>>(gbf_.as<bf16>(), z_[0].as<bf16>(), npix * CH, gz_.as<bf16>());
+    relu_bwd_acc<<<grid_for(npix * CH / 4), 256, 0, st>>>(gacc_.as<float>(), z_[0].as<bf16>(), npix * CH,
+                                                           gz_.as<bf16>());
     {
       const int nb = kPartialBlocksPerSm * sms_;
       bpart_.ensure(sizeof(float) * (size_t)nb * kConvInPartial);
@@ -946,7 +972,7 @@ class WarmStartCnn {
       sum_partials<<<CH, 128, 0, st>>>(bpart_.as<float>() + NTAP * CH * 2, nb, kConvInPartial, CH, B_[0].g.as<float>());
       PDT_LAUNCH_CHECK();
     }
-    count_launch(5);
+    count_launch(4);  // relu_bwd_acc, conv_in_wgrad_partial, two sum_partials
     std::vector<double> h(lb);
     PDT_CUDA_CHECK(cudaMemcpyAsync(h.data(), part_.p, sizeof(double) * lb, cudaMemcpyDeviceToHost, st));
     PDT_CUDA_CHECK(cudaStreamSynchronize(st));
