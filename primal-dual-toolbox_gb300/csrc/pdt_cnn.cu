@@ -13,6 +13,7 @@
 // the weight gradient is a second implicit GEMM with pixels as K, reduced over blocks in block order.
 #include <cuda_bf16.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <random>
@@ -50,15 +51,18 @@ enum Epi {
   EPI_LINEAR = 0,    // out = z (BF16)
   EPI_RELU = 1,      // zsave = z, out = relu(z)
   EPI_RELU_RES = 2,  // zsave = z, out = in + relu(z)   (CIN == COUT)
-  EPI_F32 = 3        // out32 = z (FP32)
+  EPI_F32 = 3,       // out32 = z (FP32)
+  EPI_ACC = 4,       // acc32 += bf16(z)  (a residual stream's FP32 gradient; the BF16 rounding of a stored z)
+  EPI_F32_BF16 = 5   // out32 = bf16(z), stored as FP32 (starts a residual stream's gradient)
 };
 
 // 32 -> 32 channel 3 x 3 convolution on the fifth-generation tensor cores (tcgen05 kind::f16, BF16
 // operands, FP32 accumulator in tensor memory), as an implicit GEMM without an im2col copy. One CTA computes
 // a tile of 8 x 16 pixels (x, y) = the 128 rows of one MMA tile, rows ordered y-major. The input tile with
 // its one-pixel zero halo (10 x 18 pixels) sits in shared memory in the no-swizzle K-major layout: channel
-// group g (8 channels, 16 bytes) of pixel p at byte g 2880 + 16 p, so eight consecutive pixels form a core
-// matrix; the 8-pixel groups of the M tile are one halo row (160 bytes) apart, and tap (ky, kx) is the
+// group g (8 channels, 16 bytes) of pixel p at byte g 2912 + 16 p, so eight consecutive pixels form a core
+// matrix (the group stride, two pixels more than the 180 of a group, puts the four groups of a pixel in
+// four different bank quarters, so the halo's 16-byte stores do not conflict); the 8-pixel groups of the M tile are one halo row (160 bytes) apart, and tap (ky, kx) is the
 // same layout started 16 (10 ky + kx) bytes in. The weights sit the same way ([tap][g][co] x 16 bytes).
 // K = (tap, channel) = 288 in 18 MMAs of K = 16 (two channel groups), N = 32 output channels. One thread
 // issues the MMAs and commits them to an mbarrier; the epilogue reads pixel rows from tensor memory
@@ -66,30 +70,42 @@ enum Epi {
 constexpr int kConvTcThreads = 256;
 constexpr int kConvTcTW = 8, kConvTcTH = 16;                      // tile: 8 pixels wide, 16 rows
 constexpr int kConvTcHaloPix = (kConvTcTW + 2) * (kConvTcTH + 2);  // 180
-constexpr uint32_t kConvTcGroup = 16 * kConvTcHaloPix;             // 2880: one channel group of the tile
-constexpr uint32_t kConvTcIn = 4 * kConvTcGroup;                   // 11,520 bytes
+constexpr uint32_t kConvTcGroup = 16 * (kConvTcHaloPix + 2);       // 2912: one channel group of the tile
+constexpr uint32_t kConvTcIn = 4 * kConvTcGroup;                   // 11,648 bytes
 constexpr uint32_t kConvTcW = NTAP * 4 * 32 * 16;                   // 18,432 bytes
-// the allocation also covers reads with the two descriptor strides exchanged (2880 x 15 + 160 x 1 + 128
-// past a tap start below 11,520 + 18,432), so no operand read can leave it
-constexpr size_t kConvTcSmem = 1024 + 65536 + 64;
+// The farthest operand byte an MMA reads: A at tap (2, 2), channel groups 2, 3: 16 (2 10 + 2) + 2 2912 +
+// 2912 (second K core matrix) + 15 160 (last 8-pixel group) + 128 = 11,616 <= kConvTcIn; B at tap 8, groups
+// 2, 3: (8 4 + 2) 512 + 512 + 3 128 + 128 = 18,432 = kConvTcW. The mbarrier, the tensor-memory slot and
+// the 32 biases (FP32) follow the weights.
+constexpr size_t kConvTcSmem = 1024 + kConvTcIn + kConvTcW + 16 + 128;
+constexpr int kConvTcItems = kConvTcHaloPix * 4;                                 // 720 16-byte items per tile
+constexpr int kConvTcPre = (kConvTcItems + kConvTcThreads - 1) / kConvTcThreads;  // 3 per thread
+
+__device__ __forceinline__ void ld_shared_v4(uint32_t addr, uint32_t (&v)[4]) {
+  asm volatile("ld.shared.v4.b32 {%0, %1, %2, %3}, [%4];" : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]) : "r"(addr));
+}
 
 // Persistent: a CTA loads the weights once and walks tiles t = blockIdx.x, + gridDim.x, ... of the
-// (x tiles) x (y tiles) x B grid; the completion barrier's phase alternates per tile.
+// (x tiles) x (y tiles) x B grid; the completion barrier's phase alternates per tile. The next tile's halo
+// is loaded into registers right after this tile's MMAs are issued, so its global-load latency overlaps
+// the MMAs and the epilogue; it is stored to shared memory once the tile buffer is free.
 template <int EPI>
-__global__ void __launch_bounds__(kConvTcThreads) conv3x3_tc(const bf16* __restrict__ in, const bf16* __restrict__ w,
+__global__ void __launch_bounds__(kConvTcThreads, 4) conv3x3_tc(const bf16* __restrict__ in, const bf16* __restrict__ w,
                                                             const float* __restrict__ bias, int B, int H, int W,
                                                             bf16* __restrict__ out, bf16* __restrict__ zsave,
-                                                            int* __restrict__ err) {
-  static_assert(EPI == EPI_LINEAR || EPI == EPI_RELU_RES, "epilogues of the 32 -> 32 layers");
+                                                            int* __restrict__ err, float* __restrict__ acc32) {
+  static_assert(EPI == EPI_RELU_RES || EPI == EPI_ACC, "epilogues of the 32 -> 32 layers");
   extern __shared__ unsigned char conv_smem_raw[];
   const uint32_t off = tc::smem_addr(conv_smem_raw);
   unsigned char* sm = conv_smem_raw + ((1024u - (off & 1023u)) & 1023u);
   const uint32_t in_base = tc::smem_addr(sm), w_base = in_base + kConvTcIn;
-  uint64_t* bar = reinterpret_cast<uint64_t*>(sm + 65536);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(sm + kConvTcIn + kConvTcW);
   uint32_t* tslot = reinterpret_cast<uint32_t*>(bar + 1);
+  float* bias_s = reinterpret_cast<float*>(sm + kConvTcIn + kConvTcW + 16);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int ntx = (W + kConvTcTW - 1) / kConvTcTW, nty = (H + kConvTcTH - 1) / kConvTcTH;
   const int ntiles = ntx * nty * B;
+  if (tid < CH) bias_s[tid] = bias ? bias[tid] : 0.f;
   if (tid == 0) {
     tc::mbar_init(bar, 1);
     tc::fence_mbar_init();
@@ -108,23 +124,37 @@ __global__ void __launch_bounds__(kConvTcThreads) conv3x3_tc(const bf16* __restr
   tc::fence_after_sync();
   const uint32_t tmem = *tslot;
   const int q = warp & 3, h = warp >> 2;
-  bool ok = true;
-  int it = 0;
-  for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x, ++it) {
+  // the halo of tile t: item i = (pixel, channel group) of 16 bytes, zero outside the image
+  uint4 pre[kConvTcPre];
+  auto fetch = [&](int t) {
     const int bx = t % ntx, by = (t / ntx) % nty, b = t / (ntx * nty);
     const int x0 = bx * kConvTcTW, y0 = by * kConvTcTH;
     const bf16* inb = in + (size_t)b * H * W * CH;
-    // input tile with halo: item (pixel, channel group), 16 bytes each (the previous tile's MMAs are done)
-    for (int i = tid; i < kConvTcHaloPix * 4; i += kConvTcThreads) {
+#pragma unroll
+    for (int j = 0; j < kConvTcPre; ++j) {
+      const int i = tid + j * kConvTcThreads;
       const int g = i & 3, pix = i >> 2;
       const int hy = pix / (kConvTcTW + 2), hx = pix - hy * (kConvTcTW + 2);
       const int gy = y0 + hy - 1, gx = x0 + hx - 1;
-      uint4 v = make_uint4(0u, 0u, 0u, 0u);
-      if (gy >= 0 && gy < H && gx >= 0 && gx < W)
-        v = __ldg(reinterpret_cast<const uint4*>(inb + ((size_t)gy * W + gx) * CH) + g);
-      asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(in_base + g * kConvTcGroup + 16 * pix), "r"(v.x),
-                   "r"(v.y), "r"(v.z), "r"(v.w)
-                   : "memory");
+      pre[j] = make_uint4(0u, 0u, 0u, 0u);
+      if (i < kConvTcItems && gy >= 0 && gy < H && gx >= 0 && gx < W)
+        pre[j] = __ldg(reinterpret_cast<const uint4*>(inb + ((size_t)gy * W + gx) * CH) + g);
+    }
+  };
+  bool ok = true;
+  int it = 0;
+  if (blockIdx.x < ntiles) fetch(blockIdx.x);
+  for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x, ++it) {
+    const int bx = t % ntx, by = (t / ntx) % nty, b = t / (ntx * nty);
+    const int x0 = bx * kConvTcTW, y0 = by * kConvTcTH;
+    // the tile buffer is free (the previous tile's MMAs and epilogue are done)
+#pragma unroll
+    for (int j = 0; j < kConvTcPre; ++j) {
+      const int i = tid + j * kConvTcThreads;
+      if (i < kConvTcItems)
+        asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(in_base + (i & 3) * kConvTcGroup + 16 * (i >> 2)),
+                     "r"(pre[j].x), "r"(pre[j].y), "r"(pre[j].z), "r"(pre[j].w)
+                     : "memory");
     }
     tc::fence_async_smem();
     tc::fence_before_sync();
@@ -141,6 +171,18 @@ __global__ void __launch_bounds__(kConvTcThreads) conv3x3_tc(const bf16* __restr
       }
       tc::mma_commit(bar);
     }
+    if (t + (int)gridDim.x < ntiles) fetch(t + gridDim.x);
+    const int m = 32 * q + lane, gy = y0 + (m >> 3), gx = x0 + (m & 7);  // row m = pixel (m % 8, m / 8)
+    const bool inside = gy < H && gx < W;
+    const size_t pix = ((size_t)b * H + gy) * W + gx;
+    float4 acc_in[4];  // the accumulated gradient, loaded while the MMAs run
+    if constexpr (EPI == EPI_ACC) {
+      if (inside) {
+        const float4* ap = reinterpret_cast<const float4*>(acc32 + pix * CH + 16 * h);
+#pragma unroll
+        for (int q4 = 0; q4 < 4; ++q4) acc_in[q4] = ap[q4];
+      }
+    }
     ok = tc::mbar_wait(bar, it & 1);  // every thread waits each phase in turn
     // after a give-up, wait once more (bounded) for MMAs still in flight before the tile buffer, the
     // accumulator and finally the tensor memory are released
@@ -148,29 +190,56 @@ __global__ void __launch_bounds__(kConvTcThreads) conv3x3_tc(const bf16* __restr
     tc::fence_after_sync();
     float v[16];
     tc::tmem_ld16(tmem + ((uint32_t)(32 * q) << 16) + 16 * h, v);
-    const int m = 32 * q + lane, gy = y0 + (m >> 3), gx = x0 + (m & 7);  // row m = pixel (m % 8, m / 8)
-    if (ok && gy < H && gx < W) {
-      const size_t pix = ((size_t)b * H + gy) * W + gx;
-      uint32_t o[8], zz[8];
+    if (ok && inside) {
+      uint32_t o[8], zz[8], res[8];
+      float bs[16];
+      if constexpr (EPI == EPI_RELU_RES) {
 #pragma unroll
-      for (int j = 0; j < 8; ++j) {
-        const int co = 16 * h + 2 * j;
-        float z0 = v[2 * j], z1 = v[2 * j + 1];
-        if (bias) {
-          z0 += bias[co];
-          z1 += bias[co + 1];
+        for (int q4 = 0; q4 < 4; ++q4) {
+          uint32_t r[4];
+          ld_shared_v4(tc::smem_addr(bias_s) + 64 * h + 16 * q4, r);
+#pragma unroll
+          for (int e = 0; e < 4; ++e) bs[4 * q4 + e] = __uint_as_float(r[e]);
         }
-        if constexpr (EPI == EPI_LINEAR) {
+      }
+      if constexpr (EPI == EPI_RELU_RES) {  // the residual input: this pixel's channels 16 h .. 16 h + 15 in the tile
+        const uint32_t hp = in_base + 16 * (((m >> 3) + 1) * (kConvTcTW + 2) + (m & 7) + 1);
+        ld_shared_v4(hp + 2 * h * kConvTcGroup, *reinterpret_cast<uint32_t(*)[4]>(&res[0]));
+        ld_shared_v4(hp + (2 * h + 1) * kConvTcGroup, *reinterpret_cast<uint32_t(*)[4]>(&res[4]));
+      }
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {  // output channels 16 h + 2 j, + 1
+        float z0 = v[2 * j], z1 = v[2 * j + 1];
+        if constexpr (EPI == EPI_RELU_RES) {
+          z0 += bs[2 * j];
+          z1 += bs[2 * j + 1];
+        }
+        if constexpr (EPI == EPI_ACC) {
           o[j] = pack_bf16(z0, z1);
         } else {
           zz[j] = pack_bf16(z0, z1);
-          const __nv_bfloat162 hv = reinterpret_cast<const __nv_bfloat162*>(in + pix * CH)[co / 2];
+          const __nv_bfloat162 hv = *reinterpret_cast<const __nv_bfloat162*>(&res[j]);
           o[j] = pack_bf16(__bfloat162float(hv.x) + fmaxf(z0, 0.f), __bfloat162float(hv.y) + fmaxf(z1, 0.f));
         }
       }
-      uint4* op = reinterpret_cast<uint4*>(out + pix * CH + 16 * h);
-      op[0] = make_uint4(o[0], o[1], o[2], o[3]);
-      op[1] = make_uint4(o[4], o[5], o[6], o[7]);
+      if constexpr (EPI == EPI_ACC) {
+        float4* ap = reinterpret_cast<float4*>(acc32 + pix * CH + 16 * h);
+#pragma unroll
+        for (int q4 = 0; q4 < 4; ++q4) {
+          float4 a = acc_in[q4];
+          const __nv_bfloat162 lo = *reinterpret_cast<const __nv_bfloat162*>(&o[2 * q4]);
+          const __nv_bfloat162 hi = *reinterpret_cast<const __nv_bfloat162*>(&o[2 * q4 + 1]);
+          a.x += __bfloat162float(lo.x);
+          a.y += __bfloat162float(lo.y);
+          a.z += __bfloat162float(hi.x);
+          a.w += __bfloat162float(hi.y);
+          ap[q4] = a;
+        }
+      } else {
+        uint4* op = reinterpret_cast<uint4*>(out + pix * CH + 16 * h);
+        op[0] = make_uint4(o[0], o[1], o[2], o[3]);
+        op[1] = make_uint4(o[4], o[5], o[6], o[7]);
+      }
       if constexpr (EPI == EPI_RELU_RES) {
         uint4* zp = reinterpret_cast<uint4*>(zsave + pix * CH + 16 * h);
         zp[0] = make_uint4(zz[0], zz[1], zz[2], zz[3]);
@@ -261,6 +330,9 @@ __global__ void __launch_bounds__(32 * TH) conv3x3_mma(const bf16* __restrict__ 
       if constexpr (EPI == EPI_F32) {
         out32[pix * COUT + co] = z0;
         out32[pix * COUT + co + 1] = z1;
+      } else if constexpr (EPI == EPI_F32_BF16) {
+        out32[pix * COUT + co] = __bfloat162float(__float2bfloat16(z0));
+        out32[pix * COUT + co + 1] = __bfloat162float(__float2bfloat16(z1));
       } else if constexpr (EPI == EPI_LINEAR) {
         reinterpret_cast<uint32_t*>(out + pix * COUT)[co / 2] = pack_bf16(z0, z1);
       } else {
@@ -654,18 +726,6 @@ __global__ void __launch_bounds__(32 * kConvInWarps) conv_in_wgrad_partial(const
   }
 }
 
-// g = gin * relu'(z)   (BF16 in and out)
-__global__ void relu_bwd(const bf16* __restrict__ gin, const bf16* __restrict__ z, size_t n, bf16* __restrict__ gout) {
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
-    gout[i] = __bfloat162float(z[i]) > 0.f ? gin[i] : __float2bfloat16(0.f);
-}
-
-// acc = acc + g  (FP32 accumulator of a residual stream's gradient, BF16 addend)
-__global__ void add_into(float* __restrict__ acc, const bf16* __restrict__ g, size_t n) {
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
-    acc[i] += __bfloat162float(g[i]);
-}
-
 // g = bf16(acc) * relu'(z): the residual stream's FP32 gradient rounded to BF16 (the same rounding as a
 // separate conversion) and masked by the ReLU's derivative, four elements per thread.
 __global__ void relu_bwd_acc(const float* __restrict__ acc, const bf16* __restrict__ z, size_t n, bf16* __restrict__ g) {
@@ -844,14 +904,34 @@ class WarmStartCnn {
       init_param(W_[l], w, l >= 1);
       init_param(B_[l], std::vector<float>(nb[l], 0.f), false);
     }
-    for (auto fn : {conv3x3_tc<EPI_LINEAR>, conv3x3_tc<EPI_RELU_RES>})
+    for (auto fn : {conv3x3_tc<EPI_ACC>, conv3x3_tc<EPI_RELU_RES>}) {
       PDT_CUDA_CHECK(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kConvTcSmem));
+      // all of the unified L1 / shared storage as shared memory, so that several CTAs fit on an SM
+      PDT_CUDA_CHECK(cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+    }
     PDT_CUDA_CHECK(cudaFuncSetAttribute(wgrad_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kWgSmem));
     err_.ensure(sizeof(int));
     PDT_CUDA_CHECK(cudaMemset(err_.p, 0, sizeof(int)));
     int dev = 0;
     PDT_CUDA_CHECK(cudaGetDevice(&dev));
     PDT_CUDA_CHECK(cudaDeviceGetAttribute(&sms_, cudaDevAttrMultiProcessorCount, dev));
+    // resident CTAs per SM from the register file, shared memory and thread limits (256-register allocation
+    // granules per warp, the per-block shared memory reservation)
+    int regs_sm = 0, smem_sm = 0, smem_rsv = 0, thr_sm = 0;
+    PDT_CUDA_CHECK(cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev));
+    PDT_CUDA_CHECK(cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
+    PDT_CUDA_CHECK(cudaDeviceGetAttribute(&smem_rsv, cudaDevAttrReservedSharedMemoryPerBlock, dev));
+    PDT_CUDA_CHECK(cudaDeviceGetAttribute(&thr_sm, cudaDevAttrMaxThreadsPerMultiProcessor, dev));
+    for (auto fn : {conv3x3_tc<EPI_ACC>, conv3x3_tc<EPI_RELU_RES>}) {
+      cudaFuncAttributes fa{};
+      PDT_CUDA_CHECK(cudaFuncGetAttributes(&fa, fn));
+      const int warp_regs = ((fa.numRegs * 32 + 255) / 256) * 256;
+      const int by_regs = regs_sm / (warp_regs * (kConvTcThreads / 32));
+      const int by_smem = smem_sm / ((int)kConvTcSmem + (int)fa.sharedSizeBytes + smem_rsv);
+      const int by_thr = thr_sm / kConvTcThreads;
+      conv_tc_per_sm_ = std::min({conv_tc_per_sm_, by_regs, by_smem, by_thr});
+    }
+    conv_tc_per_sm_ = std::max(conv_tc_per_sm_, 1);
   }
 
   // Raises (and clears) the error word of the tensor-core convolutions: set when an MMA completion wait
@@ -909,7 +989,7 @@ class WarmStartCnn {
     for (int l = 1; l <= 6; ++l) {
       conv3x3_tc<EPI_RELU_RES><<<tgrid, kConvTcThreads, kConvTcSmem, st>>>(h_[l - 1].as<bf16>(), W_[l].wb.as<bf16>(),
                                                                          B_[l].w.as<float>(), B, H, W, h_[l].as<bf16>(),
-                                                                         z_[l].as<bf16>(), err_.as<int>());
+                                                                         z_[l].as<bf16>(), err_.as<int>(), nullptr);
       PDT_LAUNCH_CHECK();
       count_launch();
     }
@@ -937,14 +1017,11 @@ class WarmStartCnn {
     pad8to16(go_.as<bf16>(), npix, st);
     flip_transpose<<<64, 256, 0, st>>>(W_[7].wb.as<bf16>(), 8, CH, 16, CH, wt_.as<bf16>());
     PDT_LAUNCH_CHECK();
-    conv3x3_mma<16, CH, EPI_LINEAR><<<grid, 32 * TH, 0, st>>>(go16_.as<bf16>(), wt_.as<bf16>(), nullptr, H, W,
-                                                              gtmp_.as<bf16>(), nullptr, nullptr);
+    // the residual stream's FP32 gradient starts as G = dh6 (the BF16 rounding of the convolution's output)
+    conv3x3_mma<16, CH, EPI_F32_BF16><<<grid, 32 * TH, 0, st>>>(go16_.as<bf16>(), wt_.as<bf16>(), nullptr, H, W,
+                                                                nullptr, nullptr, gacc_.as<float>());
     PDT_LAUNCH_CHECK();
     count_launch(3);  // mse_loss, flip_transpose, conv3x3_mma (the bias gradient counts its own)
-    // residual stream gradient G (FP32): G = dh6
-    zero_acc(npix * CH, st);
-    add_into<<<grid_for(npix * CH), 256, 0, st>>>(gacc_.as<float>(), gtmp_.as<bf16>(), npix * CH);
-    PDT_LAUNCH_CHECK();
     for (int l = 6; l >= 1; --l) {
       // h_l = h_{l-1} + relu(z_l), z_l = conv_l(h_{l-1}):  dz = G * relu'(z_l); dh_{l-1} = G + conv_l^T(dz)
       relu_bwd_acc<<<grid_for(npix * CH / 4), 256, 0, st>>>(gacc_.as<float>(), z_[l].as<bf16>(), npix * CH,
@@ -953,11 +1030,11 @@ class WarmStartCnn {
       wgrad(CH, h_[l - 1].as<bf16>(), gz_.as<bf16>(), B, H, W, W_[l].g.as<float>(), st);
       bias_gradient(gz_.as<bf16>(), npix, CH, B_[l].g.as<float>(), st);
       flip_transpose<<<64, 256, 0, st>>>(W_[l].wb.as<bf16>(), CH, CH, CH, CH, wt_.as<bf16>());
-      conv3x3_tc<EPI_LINEAR><<<tgrid, kConvTcThreads, kConvTcSmem, st>>>(gz_.as<bf16>(), wt_.as<bf16>(), nullptr, B, H, W,
-                                                                       gtmp_.as<bf16>(), nullptr, err_.as<int>());
-      add_into<<<grid_for(npix * CH), 256, 0, st>>>(gacc_.as<float>(), gtmp_.as<bf16>(), npix * CH);
+      // dh_{l-1} += conv_l^T(dz), added into the FP32 residual gradient in the convolution's epilogue
+      conv3x3_tc<EPI_ACC><<<tgrid, kConvTcThreads, kConvTcSmem, st>>>(gz_.as<bf16>(), wt_.as<bf16>(), nullptr, B, H, W,
+                                                                    nullptr, nullptr, err_.as<int>(), gacc_.as<float>());
       PDT_LAUNCH_CHECK();
-      count_launch(4);  // relu_bwd_acc, flip_transpose, conv3x3_tc, add_into
+      count_launch(3);  // relu_bwd_acc, flip_transpose, conv3x3_tc
     }
     // conv_in: h1 = relu(z_0): dz0 = G * relu'(z0)
     relu_bwd_acc<<<grid_for(npix * CH / 4), 256, 0, st>>>(gacc_.as<float>(), z_[0].as<bf16>(), npix * CH,
@@ -1057,7 +1134,7 @@ class WarmStartCnn {
   // persistent tensor-core convolutions: three CTAs per SM (66 KB of shared memory each), at most one tile each
   int conv_tc_grid(int B, int H, int W) const {
     const long long tiles = (long long)((W + kConvTcTW - 1) / kConvTcTW) * ((H + kConvTcTH - 1) / kConvTcTH) * B;
-    return (int)std::min<long long>(tiles, 3LL * sms_);
+    return (int)std::min<long long>(tiles, (long long)conv_tc_per_sm_ * sms_);
   }
   void refresh_bf16(CnnParam& p, cudaStream_t st) {
     to_bf16<<<grid_for(p.n), 256, 0, st>>>(p.w.as<float>(), p.n, p.wb.as<bf16>());
@@ -1074,8 +1151,6 @@ class WarmStartCnn {
     o_.ensure(npix * 8 * sizeof(float));
     go_.ensure(npix * 8 * sizeof(bf16));
     go16_.ensure(npix * 16 * sizeof(bf16));
-    gtmp_.ensure(npix * CH * sizeof(bf16));
-    gbf_.ensure(npix * CH * sizeof(bf16));
     gz_.ensure(npix * CH * sizeof(bf16));
     gacc_.ensure(npix * CH * sizeof(float));
     wt_.ensure(NTAP * CH * CH * sizeof(bf16));
@@ -1083,7 +1158,6 @@ class WarmStartCnn {
     H_n_ = H;
     W_n_ = W;
   }
-  void zero_acc(size_t n, cudaStream_t st) { PDT_CUDA_CHECK(cudaMemsetAsync(gacc_.p, 0, n * sizeof(float), st)); }
   void pad8to16(const bf16* g8, size_t npix, cudaStream_t st) {
     PDT_CUDA_CHECK(cudaMemsetAsync(go16_.p, 0, npix * 16 * sizeof(bf16), st));
     PDT_CUDA_CHECK(cudaMemcpy2DAsync(go16_.p, 16 * sizeof(bf16), g8, 8 * sizeof(bf16), 8 * sizeof(bf16), npix,
@@ -1111,7 +1185,7 @@ class WarmStartCnn {
   }
 
   CnnParam W_[kLayers], B_[kLayers];
-  DevBuf x_, h_[7], z_[7], o_, go_, go16_, gtmp_, gbf_, gz_, gacc_, wt_, wpart_, part_, t_, sc_, err_, bpart_, wtmp_;
+  DevBuf x_, h_[7], z_[7], o_, go_, go16_, gz_, gacc_, wt_, wpart_, part_, t_, sc_, err_, bpart_, wtmp_;
 
   // Bias gradient db[c] = sum over pixels of dy[p][c] (C = 8 or 32): chunked partial sums, then the
   // partials in block order.
@@ -1127,6 +1201,7 @@ class WarmStartCnn {
     count_launch(2);
   }
   int sms_ = 1;
+  int conv_tc_per_sm_ = 8;  // resident conv3x3_tc CTAs per SM (each holds 32 TMEM columns: 8 x 32 <= 512)
   int B_n_ = 0, H_n_ = 0, W_n_ = 0;
   long step_ = 0;
 };
