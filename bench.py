@@ -957,6 +957,42 @@ def run_ncu_case(args):
         torch.cuda.profiler.stop()
         print(json.dumps({"ncu_case": "warmstart_cnn_train_step_4x320x320", "steps": args.ncu_iters}), flush=True)
         return
+    if args.ncu_workload == "batched":
+        # the config-3 batch: --batch-cases mixed problems (the bench's batched leg), one batched solve of
+        # --ncu-iters iterations per problem between the profiler marks
+        import concurrent.futures
+        import multiprocessing
+
+        from primaldualtoolbox import warmstart
+
+        specs = _batch_specs(args.batch_cases)
+        with concurrent.futures.ProcessPoolExecutor(max(1, min(16, (os.cpu_count() or 2) - 1)),
+                                                    mp_context=multiprocessing.get_context("spawn")) as pool:
+            cases = list(pool.map(warmstart._case, specs, chunksize=1))
+        opts = []
+        for case in cases:
+            op = pdt.mri.MriCartesianOperator()
+            op.setCoilSens(case["sens"])
+            op.setMask(case["mask"])
+            opt = pdt.mri.TgvMriOptimizer_2c3c()
+            prm = opt.getParameters()
+            prm.max_iter, prm.reduction, prm.alpha1 = args.ncu_iters - 1, REDUCTION, case["alpha1"]
+            prm.alpha0 = 2 * prm.alpha1
+            opt.setOperator(op)
+            opt.setNoisyData(case["rawdata"])
+            opts.append(opt)
+        del cases
+        batch = pdt.batch.BatchSolver(opts)
+        for _ in range(3):
+            batch.solve(stream=stream)
+        torch.cuda.synchronize()
+        torch.cuda.profiler.start()
+        batch.solve(stream=stream)
+        torch.cuda.synchronize()
+        torch.cuda.profiler.stop()
+        print(json.dumps({"ncu_case": f"batch_{args.batch_cases}_cartesian_tgv2_mixed", "iterations": args.ncu_iters,
+                          "shapes": [[s["C"], s["H"], s["W"]] for s in specs]}), flush=True)
+        return
     if args.ncu_workload == "radial":
         op, f, a1 = _radial_problem(pdt, seed=0)
         opt = pdt.mri.TgvMriOptimizer_2c2c()
@@ -1052,9 +1088,9 @@ def main():
     ap.add_argument("--radial-iters", type=int, default=200, help="radial leg: iterations per slice")
     ap.add_argument("--batch-cases", type=int, default=64, help="batched leg: independent problems (0 skips)")
     ap.add_argument("--batch-iters", type=int, default=200, help="batched leg: iterations per problem and step")
-    ap.add_argument("--ncu-workload", default="cartesian", choices=["cartesian", "radial", "cnn"],
-                    help="profiling mode: the config-2 Cartesian problem, the config-5 radial slice or one "
-                         "training step of the warm-start network")
+    ap.add_argument("--ncu-workload", default="cartesian", choices=["cartesian", "radial", "cnn", "batched"],
+                    help="profiling mode: the config-2 Cartesian problem, the config-5 radial slice, one "
+                         "training step of the warm-start network or the config-3 batch (--batch-cases)")
     ap.add_argument("--ncu-iters", type=int, default=0,
                     help="profiling mode: one solve of this many iterations between cudaProfilerStart/Stop")
     args = ap.parse_args()

@@ -280,22 +280,43 @@ __global__ void __launch_bounds__(32 * WPB) fl_cols64(CartDev d, int mode, const
   }
 }
 
+// Asynchronous global -> shared copies (cp.async; completion per thread by commit groups).
+__device__ __forceinline__ void cp_async8(void* dst, const void* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)), "l"(src)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)), "l"(src)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
 // Phase 3: per block of R image rows and coil group g, IFFT along W of the sampled columns, conj(sens_c)
 // multiply and the coil sum, accumulated in shared memory (each lane always owns the same pixels).
 // With use_cluster the G coil groups of a row block form a cluster (grid.y = G) and reduce their rows
 // through distributed shared memory in rank order (deterministic) into one K^H r plane; otherwise each
 // block writes its group's partial sum to out + g * gstride.
+// With `staged`, the sampled columns of the next coil and the coil-map rows of the current coil arrive in
+// shared memory by asynchronous copies (two column stages, one map buffer) while the current coil's rows
+// are transformed, so neither load's latency sits between the transforms; the arithmetic and its order
+// are the same as without.
 template <int M, int L, int WPB>
 __global__ void __launch_bounds__(32 * WPB, 16 / WPB) fl_rows_adj(CartDev d, const float2* __restrict__ t2,
                                                         float2* __restrict__ out, int use_cluster, int G,
-                                                        long long gstride) {
+                                                        long long gstride, int staged) {
   using F = LaneFft<M, L>;
   constexpr int W = F::n, R = WPB * (32 / L);
-  extern __shared__ float2 sm[];
-  float2* tw = sm;
-  float2* stage = tw + W;                    // [ns][R]
-  float2* red = stage + (size_t)d.ns * R;    // [R][W]
-  int* as2s = reinterpret_cast<int*>(red + (size_t)R * W);
+  extern __shared__ __align__(16) float2 sm_adj[];
+  float2* tw = sm_adj;
+  float2* stage = tw + W;                                                 // [1 or 2][ns][R]
+  float2* red = stage + (size_t)(staged ? 2 : 1) * d.ns * R;              // [R][W]
+  float2* smap = red + (size_t)R * W;                                     // [R][W] (staged, with coil maps)
+  const bool map_staged = staged && d.sens != nullptr;
+  int* as2s = reinterpret_cast<int*>(smap + (map_staged ? (size_t)R * W : 0));
   const int g = blockIdx.y;
   for (int i = threadIdx.x; i < W; i += blockDim.x) {
     tw[i] = d.twW[i];
@@ -313,6 +334,51 @@ __global__ void __launch_bounds__(32 * WPB, 16 / WPB) fl_rows_adj(CartDev d, con
   const int yi = yi0 + rc;
   const int c_begin = (int)((long long)g * d.C / G), c_end = (int)((long long)(g + 1) * d.C / G);
   const int kb = M * lane_brev<L>(t);
+  if (staged) {
+    // group order per coil c: [maps of c], [columns of c + 1]; the columns of c_begin before the loop
+    auto copy_cols = [&](int c, float2* dst) {
+      for (int i = threadIdx.x; i < d.ns * nr; i += blockDim.x) {
+        const int s = i / nr, rr = i - s * nr;
+        cp_async8(dst + s * R + rr, t2 + ((size_t)c * d.ns + s) * d.Hi + yi0 + rr);
+      }
+    };
+    if (c_begin < c_end) copy_cols(c_begin, stage);
+    cp_async_commit();
+    for (int c = c_begin; c < c_end; ++c) {
+      const int k = c - c_begin;
+      float2* cur = stage + (size_t)(k & 1) * d.ns * R;
+      __syncthreads();  // the map buffer and the other column stage are free (and the tables ready)
+      if (map_staged) {  // rows yi0 .. yi0 + nr - 1 of coil c, 16-byte pieces (W even: rows 16-byte aligned)
+        const float2* src = d.sens + ((size_t)c * d.Hf + yi0 + d.y0) * W;
+        for (int i = threadIdx.x; i < nr * (W / 2); i += blockDim.x) cp_async16(smap + 2 * i, src + 2 * i);
+      }
+      cp_async_commit();
+      if (c + 1 < c_end) copy_cols(c + 1, stage + (size_t)((k + 1) & 1) * d.ns * R);
+      cp_async_commit();
+      cp_async_wait<2>();  // this thread's copies of coil c's columns landed
+      __syncthreads();
+      float2 v[M];
+#pragma unroll
+      for (int k1 = 0; k1 < M; ++k1) {
+        const int s = as2s[k1 + kb];
+        v[k1] = s >= 0 ? cur[s * R + rc] : c2(0.f, 0.f);
+      }
+      F::inv(v, t, tw);
+      cp_async_wait<1>();  // this thread's copies of coil c's map rows landed
+      __syncthreads();
+      if (ok) {
+        const float2* srow = map_staged ? smap + (size_t)r * W : nullptr;
+        float2* rrow = red + (size_t)r * W;
+#pragma unroll
+        for (int j = 0; j < M; ++j) {
+          int x = t + L * j + d.oxW;  // IFFT slot t + L j lands on image column (slot + n/2) mod W
+          if (x >= W) x -= W;
+          rrow[x] += srow ? cmulc(v[j], srow[x]) : v[j];
+        }
+      }
+    }
+    cp_async_wait<0>();
+  } else {
   // register prefetch of the next coil's sampled columns (ns * nr values spread over the block)
   constexpr int PF = 8;
   float2 pf[PF];
@@ -365,6 +431,7 @@ __global__ void __launch_bounds__(32 * WPB, 16 / WPB) fl_rows_adj(CartDev d, con
       }
     }
   }
+  }
   if (use_cluster) {
     cg::cluster_group cluster = cg::this_cluster();
     cluster.sync();  // every block's coil-group rows complete
@@ -386,7 +453,7 @@ __global__ void __launch_bounds__(32 * WPB, 16 / WPB) fl_rows_adj(CartDev d, con
 typedef void (*FrRowsFwdFn)(CartDev, const float2*, float2*, int*);
 typedef void (*FrColsFn)(CartDev, int, const float2*, float2*, float2*, const float2*, const float2*, float2*, float,
                          float);
-typedef void (*FrRowsAdjFn)(CartDev, const float2*, float2*, int, int, long long);
+typedef void (*FrRowsAdjFn)(CartDev, const float2*, float2*, int, int, long long, int);
 
 constexpr int kWpbChoices[3] = {2, 4, 8};
 
@@ -491,9 +558,10 @@ size_t fast_rows_smem(const CartDev& d, const FastRowKernels& k, int wpb) {
   const size_t n = (size_t)k.M * k.L, R = (size_t)k.rows_per_block(wpb);
   return sizeof(float2) * (n + (size_t)d.ns * R) + sizeof(int) * n;
 }
-size_t fast_rows_adj_smem(const CartDev& d, const FastRowKernels& k, int wpb) {
+size_t fast_rows_adj_smem(const CartDev& d, const FastRowKernels& k, int wpb, bool staged = false) {
   const size_t n = (size_t)k.M * k.L, R = (size_t)k.rows_per_block(wpb);
-  return fast_rows_smem(d, k, wpb) + sizeof(float2) * R * n;
+  const size_t extra = staged ? (size_t)d.ns * R + (d.sens ? R * n : 0) : 0;  // second column stage, map rows
+  return fast_rows_smem(d, k, wpb) + sizeof(float2) * (R * n + extra);
 }
 size_t fast_cols_smem(const FastColKernels& k, int wpb) {
   const size_t n = (size_t)k.M * k.L;

@@ -312,7 +312,8 @@ class CartesianOp : public OpImpl, public SolverHooks {
          << ",coil_sum_on_chip)";
     else if (frow_.ok())
       os << " rows_adj=lane_fft(warps=" << kWpbChoices[tune_.wa] << ",coil_groups=" << G_
-         << (tune_.cluster ? ",cluster" : ",partials") << ")";
+         << (tune_.cluster ? ",cluster" : ",partials")
+         << (rows_adj_staged(frow_, kWpbChoices[tune_.wa]) ? ",staged" : "") << ")";
     else
       os << " rows_adj=stockham(coil_groups=" << G_ << ")";
     if (fcol_.ok())
@@ -462,6 +463,7 @@ class CartesianOp : public OpImpl, public SolverHooks {
     int tcf = 0, tca = 0;        // 1: tensor-core DFT rows (forward / adjoint) instead of the FFT kernels
     int ks = 4, nr = 4;          // tensor-core forward K split (cluster size), adjoint N ranges
     int wfc = 1;  // warps-per-block index of the concurrent forward-row split (4 warps; 2 and 4 measured alike)
+    int sst = 1;  // 1: the FFT adjoint rows stage columns and coil maps by asynchronous copies (where they fit)
   };
 
   int tc_adj_nb(int nr) const { return std::min(kTcAdjMaxNB, ((2 * dev_.W + nr - 1) / nr + 15) & ~15); }
@@ -575,6 +577,13 @@ class CartesianOp : public OpImpl, public SolverHooks {
     PDT_LAUNCH_CHECK();
     count_launch();
   }
+  // The staged FFT adjoint rows where chosen and where their larger shared-memory footprint fits
+  // (PDT_ROWS_ADJ_STAGED=0 / 1 overrides the choice).
+  bool rows_adj_staged(const FastRowKernels& k, int wpb) const {
+    static const char* env = std::getenv("PDT_ROWS_ADJ_STAGED");
+    const bool want = (env && *env) ? std::atoi(env) != 0 : tune_.sst != 0;
+    return want && fast_rows_adj_smem(dev_, k, wpb, true) <= (size_t)g_max_smem;
+  }
   // K^H: G coil-group partial images (or, with a cluster, one reduced image) into out.
   void launch_rows_adj(const float2* t2, float2* out, int G, cudaStream_t st) {
     if (frow_.ok()) {
@@ -582,9 +591,11 @@ class CartesianOp : public OpImpl, public SolverHooks {
       const int wpb = kWpbChoices[tune_.wa];
       const bool cl = tune_.cluster && G > 1;
       const int R = k.rows_per_block(wpb);
-      LaunchEx lx(dim3((dev_.Hi + R - 1) / R, G), dim3(32 * wpb), fast_rows_adj_smem(dev_, k, wpb), st, cl ? G : 0);
+      const bool stg = rows_adj_staged(k, wpb);
+      LaunchEx lx(dim3((dev_.Hi + R - 1) / R, G), dim3(32 * wpb), fast_rows_adj_smem(dev_, k, wpb, stg), st,
+                  cl ? G : 0);
       PDT_CUDA_CHECK(cudaLaunchKernelEx(&lx.cfg, k.adj[tune_.wa], dev_, t2, out, cl ? 1 : 0, G,
-                                        (long long)dev_.Hi * dev_.W));
+                                        (long long)dev_.Hi * dev_.W, stg ? 1 : 0));
       count_launch();
       return;
     }
@@ -852,6 +863,12 @@ class CartesianOp : public OpImpl, public SolverHooks {
             if (ms < ba) ba = ms, best.wa = w, best.cluster = cl != 0, bestG = g;
           }
       G_ = bestG;
+      // the chosen shape with register-prefetched columns and global coil-map loads instead of staging
+      tune_.wa = best.wa;
+      tune_.cluster = best.cluster;
+      tune_.sst = 0;
+      if (const float ms = time([&] { launch_rows_adj(t, kh.as<float2>(), G_, st); }); ms < ba) ba = ms, best.sst = 0;
+      tune_.sst = best.sst;
     } else if (tcf_ok_) {
       bt = time([&] { launch_rows_fwd(ub.as<float2>(), t, nullptr, st); });
     }
