@@ -1,5 +1,6 @@
 // pdt_capi.cu -- C ABI (include/pdt.h): operator and optimizer handles, the solver loops and error
 // mapping. Status codes and thread-local messages replace the reference's IuException.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -285,6 +286,9 @@ class OptImpl {
   bool with_op() const { return kind_ == PDT_OPT_TV_OP || kind_ == PDT_OPT_TGV_OP || kind_ == PDT_OPT_TGV_MRI; }
   bool tgv() const { return kind_ == PDT_OPT_TGV || kind_ == PDT_OPT_TGV_OP || kind_ == PDT_OPT_TGV_MRI; }
   size_t pix() const { return cplx_ ? 8 : 4; }
+  // Relative cost of one iteration, for spreading a batch over worker streams: the data's elements (coils x
+  // k-space samples with an operator) plus the image's pixels.
+  size_t work_estimate() const { return numel_of(fsize_) + (size_t)W_ * H_; }
 
   pdt_params params_;
   // Step sizes of the with-operator solves when positive (pdt_opt_set_steps); 0: the reference's.
@@ -1075,8 +1079,15 @@ class BatchImpl {
   static constexpr int kBatchIters = 10;  // even: every replay returns each problem to its parity
   static constexpr int kMaxStreams = 32;
 
+  // Worker streams: one per problem up to kMaxStreams (PDT_BATCH_STREAMS overrides, 1 .. 128). With more
+  // problems than streams, problems go to streams longest first, each to the stream with the least work
+  // so far (the graph's critical path is the most loaded stream).
   void ensure_streams() {
-    const size_t want = std::min<size_t>(opts_.size(), kMaxStreams);
+    static const int env_streams = [] {
+      const char* e = std::getenv("PDT_BATCH_STREAMS");
+      return (e && *e) ? std::max(1, std::min(128, std::atoi(e))) : kMaxStreams;
+    }();
+    const size_t want = std::min<size_t>(opts_.size(), (size_t)env_streams);
     if (!cap_) PDT_CUDA_CHECK(cudaStreamCreateWithFlags(&cap_, cudaStreamNonBlocking));
     while (workers_.size() < want) {
       cudaStream_t s;
@@ -1088,14 +1099,28 @@ class BatchImpl {
       PDT_CUDA_CHECK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
       events_.push_back(e);
     }
+    const size_t P = std::min(want, workers_.size());
+    owner_.assign(opts_.size(), 0);
+    std::vector<size_t> order(opts_.size());
+    for (size_t i = 0; i < order.size(); ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t b) {
+      return opts_[a]->work_estimate() > opts_[b]->work_estimate();
+    });
+    std::vector<size_t> load(P, 0);
+    for (size_t i : order) {
+      const size_t w = (size_t)(std::min_element(load.begin(), load.end()) - load.begin());
+      owner_[i] = w;
+      load[w] += opts_[i]->work_estimate();
+    }
+    nworkers_ = P;
   }
   // Runs fn(problem, worker stream) for every problem on worker streams forked from and joined back into `on`.
   template <class F>
   void fork_join(cudaStream_t on, F&& fn) {
-    const size_t P = std::min(workers_.size(), opts_.size());
+    const size_t P = nworkers_;
     PDT_CUDA_CHECK(cudaEventRecord(events_[0], on));
     for (size_t w = 0; w < P; ++w) PDT_CUDA_CHECK(cudaStreamWaitEvent(workers_[w], events_[0], 0));
-    for (size_t i = 0; i < opts_.size(); ++i) fn(i, workers_[i % P]);
+    for (size_t i = 0; i < opts_.size(); ++i) fn(i, workers_[owner_[i]]);
     for (size_t w = 0; w < P; ++w) {
       PDT_CUDA_CHECK(cudaEventRecord(events_[w + 1], workers_[w]));
       PDT_CUDA_CHECK(cudaStreamWaitEvent(on, events_[w + 1], 0));
@@ -1105,6 +1130,8 @@ class BatchImpl {
   std::vector<OptImpl*> opts_;
   std::vector<cudaStream_t> workers_;
   std::vector<cudaEvent_t> events_;
+  std::vector<size_t> owner_;  // worker stream of each problem
+  size_t nworkers_ = 0;
   cudaStream_t cap_ = nullptr;
   IterGraph graph_;
 };
