@@ -18,6 +18,7 @@ from __future__ import annotations
 import argparse
 import json
 import os
+import re
 import subprocess
 import sys
 import threading
@@ -673,8 +674,10 @@ def run_batched(pdt, torch, n_cases, iters, steps, warmup):
         opt.setNoisyData(case["rawdata"])
         ns = int((case["mask"] != 0).any(axis=0).sum())
         tuning = op.tuning()
-        G = _khr_planes(tuning)
-        adj = "tensor_dft" if "rows_adj=tensor_dft" in tuning else "lane_fft"
+        # in a batch the operator runs its lane-FFT rows where its solo choice was the tensor-core rows
+        m = re.search(r"batch_adj_groups=(\d+)(,cluster|,partials)", tuning)
+        G = (1 if m.group(2) == ",cluster" else int(m.group(1))) if m else _khr_planes(tuning)
+        adj = "tensor_dft" if "rows_adj=tensor_dft" in tuning and not m else "lane_fft"
         adj_rows[adj] = adj_rows.get(adj, 0) + 1
         nbytes += sum(_phase_bytes_case(spec["C"], spec["H"], spec["W"], ns, G, False).values())
         pix += spec["H"] * spec["W"]

@@ -324,6 +324,8 @@ class CartesianOp : public OpImpl, public SolverHooks {
     if (tune_.tca && dev_.ns > 0 && fuse_dual_ && dual_rows() > 0)
       os << " solver_dual=adjoint_launch(" << dual_rows() * ((2 * dev_.W + tc_adj_nb(tune_.nr) - 1) / tc_adj_nb(tune_.nr))
          << "_blocks)";
+    if ((tune_.tca || tune_.tcf) && frow_.ok())  // what a batched solve runs instead (tca(), tcf())
+      os << " in_batch=lane_fft_rows(batch_adj_groups=" << G_ << (tune_.cluster ? ",cluster" : ",partials") << ")";
     return os.str();
   }
   Dims natural_input_size() override {
@@ -358,7 +360,7 @@ class CartesianOp : public OpImpl, public SolverHooks {
   }
   int groups() override {
     prepare();
-    if (tune_.tca) return 1;                         // the tensor-core adjoint rows sum the coils on chip
+    if (tca()) return 1;                         // the tensor-core adjoint rows sum the coils on chip
     return (frow_.ok() && tune_.cluster) ? 1 : G_;  // a cluster reduces its coil groups on chip
   }
   long long group_stride() override { return (long long)dev_.Hi * dev_.W; }
@@ -375,7 +377,7 @@ class CartesianOp : public OpImpl, public SolverHooks {
   void set_concurrent(bool on) override { concurrent_ = on; }
   bool can_fuse_dual(int W, int H) override {
     prepare();
-    return tune_.tca && dev_.ns > 0 && fuse_dual_ && W == dev_.W && H == dev_.Hi && dual_rows() > 0;
+    return tca() && dev_.ns > 0 && fuse_dual_ && W == dev_.W && H == dev_.Hi && dual_rows() > 0;
   }
   void round(const float2* ubar, float2* r, const float2* fc, float sigma, float lambda, float2* khr, int* tick,
              cudaStream_t st, PhaseMarker* mk, const DualStep* dual) override {
@@ -392,7 +394,7 @@ class CartesianOp : public OpImpl, public SolverHooks {
     if (mk) mk->mark("cart_rows_fwd", st);
     launch_cols(COL_SOLVE, t, t, r, fc, nullptr, nullptr, sigma, lambda, st);
     if (mk) mk->mark("cart_cols_prox", st);
-    if (tune_.tca)
+    if (tca())
       launch_tc_rows_adj(t, khr, st, dual);  // the coil sum on chip: one K^H r plane
     else
       launch_rows_adj(t, khr, G_, st);
@@ -406,7 +408,7 @@ class CartesianOp : public OpImpl, public SolverHooks {
     }
     float2* t = scratch_.as<float2>();
     launch_cols(COL_ADJ_COMPACT, nullptr, t, nullptr, fc, nullptr, nullptr, 0.f, 0.f, st);
-    if (tune_.tca)
+    if (tca())
       launch_tc_rows_adj(t, img, st);
     else
       launch_rows_adj(t, img, 1, st);
@@ -448,7 +450,7 @@ class CartesianOp : public OpImpl, public SolverHooks {
     }
     float2* t = scratch_.as<float2>();
     launch_cols(COL_ADJ_DENSE, nullptr, t, nullptr, nullptr, src, nullptr, 0.f, 0.f, st);
-    if (tune_.tca)
+    if (tca())
       launch_tc_rows_adj(t, dst, st);
     else
       launch_rows_adj(t, dst, 1, st);
@@ -540,8 +542,13 @@ class CartesianOp : public OpImpl, public SolverHooks {
     return e;
   }
 
+  // The tensor-core row passes take one 198 KB CTA per SM and are chosen by timing the operator alone;
+  // among the concurrent problems of a batch the lane-FFT rows, which share SMs, run instead.
+  bool tca() const { return tune_.tca && !(concurrent_ && frow_.ok()); }
+  bool tcf() const { return tune_.tcf && !(concurrent_ && frow_.ok()); }
+
   void launch_rows_fwd(const float2* ubar, float2* t1, int* tick, cudaStream_t st) {
-    if (tune_.tcf) {
+    if (tcf()) {
       launch_tc_rows_fwd(ubar, t1, tick, st);
       return;
     }
