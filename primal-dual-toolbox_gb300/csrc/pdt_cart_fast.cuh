@@ -280,21 +280,6 @@ __global__ void __launch_bounds__(32 * WPB) fl_cols64(CartDev d, int mode, const
   }
 }
 
-// Asynchronous global -> shared copies (cp.async; completion per thread by commit groups).
-__device__ __forceinline__ void cp_async8(void* dst, const void* src) {
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)), "l"(src)
-               : "memory");
-}
-__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)), "l"(src)
-               : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() {
-  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
-}
-
 // Phase 3: per block of R image rows and coil group g, IFFT along W of the sampled columns, conj(sens_c)
 // multiply and the coil sum, accumulated in shared memory (each lane always owns the same pixels).
 // With use_cluster the G coil groups of a row block form a cluster (grid.y = G) and reduce their rows

@@ -30,10 +30,26 @@ __host__ __device__ __forceinline__ float2 conjf2(float2 a) { return c2(a.x, -a.
 // launched while its predecessor in the stream finishes; pdl_wait() blocks until the predecessor grid
 // has completed and its writes are visible (it returns at once for an ordinary launch).
 __device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 // Lets the next kernel in the stream launch once every block of this grid has executed it (or exited), so
 // that its blocks take SMs as they free up and run their set-up before their own pdl_wait(). Called right
 // after pdl_wait(): only the next grid is launched early, and it still waits for this one to complete.
 __device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
+// Asynchronous global -> shared copies (cp.async; completion per thread by commit groups).
+__device__ __forceinline__ void cp_async8(void* dst, const void* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)), "l"(src)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)), "l"(src)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
 #endif
 
 // |z|^2 of a pixel (real or complex).

@@ -6,7 +6,8 @@
 //   rl_rows_fwd   image rows . sens_c / deap -> FFT along x           -> T[c][gx][image row]
 //   rl_cols       FFT along y of each grid column (input on N rows)   -> F[c][gx][gy]
 //   rl_cols_inv   IFFT along y of each grid column, keep the N rows   -> T[c][gx][image row]
-//   rl_rows_inv   IFFT along x, crop, / deap, conj(sens_c) . and the coil-group sum
+//   rl_rows_inv   IFFT along x, crop, / deap, conj(sens_c) . and the coil-group sum (the next coil's grid
+//                 rows and this coil's map rows arrive by asynchronous copies during the transform)
 // Row passes stage R = WPB * 32 / L rows per block in shared memory so that T is written / read in runs
 // of R rows; column passes stage one grid column per lane group so that F is written / read whole.
 #pragma once
@@ -137,15 +138,18 @@ __global__ void __launch_bounds__(32 * kRadWpb) rl_rows_inv(RadDev d, const floa
                                                             float2* __restrict__ out, int G_, long long gstride) {
   using F = LaneFft<M, L>;
   constexpr int G = F::n, R = kRadWpb * (32 / L);
-  extern __shared__ float2 sm[];
-  float2* tw = sm;
-  float2* stage = tw + G;      // [G][R]
-  float2* acc = stage + G * R;  // [R][N]
+  extern __shared__ __align__(16) float2 sm_ri[];
+  float2* tw = sm_ri;
+  float2* stage = tw + G;                 // [2][G][R]: this coil's grid rows and the next coil's
+  float2* acc = stage + 2 * G * R;        // [R][N]
+  float2* smap = acc + (size_t)R * d.N;   // [R][N] coil-map rows of this coil
+  float* sdeap = reinterpret_cast<float*>(smap + (size_t)R * d.N);  // [N]
   const int y0 = blockIdx.x * R, g = blockIdx.y;
   const int nr = min(R, d.N - y0);
   const int c_begin = (int)((long long)g * d.C / G_), c_end = (int)((long long)(g + 1) * d.C / G_);
   for (int i = threadIdx.x; i < G; i += blockDim.x) tw[i] = d.tw[i];
   for (int i = threadIdx.x; i < R * d.N; i += blockDim.x) acc[i] = c2(0.f, 0.f);
+  for (int i = threadIdx.x; i < d.N; i += blockDim.x) sdeap[i] = d.deap[i];
   const int lane = threadIdx.x & 31, t = lane & (L - 1);
   const int r = (threadIdx.x >> 5) * (32 / L) + lane / L;
   const bool ok = r < nr;
@@ -153,32 +157,51 @@ __global__ void __launch_bounds__(32 * kRadWpb) rl_rows_inv(RadDev d, const floa
   const int y = y0 + rc;
   const int kb = M * lane_brev<L>(t);
   const float dy = d.deap[y];
-  for (int c = c_begin; c < c_end; ++c) {
-    __syncthreads();  // stage free (and, the first time, tw and acc ready)
+  // asynchronous copies, one commit group each per coil c: [map rows of c], [grid rows of c + 1]; the
+  // grid rows of c_begin before the loop, so that both loads overlap the transform before them
+  auto copy_rows = [&](int c, float2* dst) {
     for (int i = threadIdx.x; i < G * nr; i += blockDim.x) {
       const int gx = i / nr, rr = i - gx * nr;
-      stage[gx * R + rr] = T[((size_t)c * G + gx) * d.N + y0 + rr];
+      cp_async8(dst + gx * R + rr, T + ((size_t)c * G + gx) * d.N + y0 + rr);
     }
+  };
+  if (c_begin < c_end) copy_rows(c_begin, stage);
+  cp_async_commit();
+  for (int c = c_begin; c < c_end; ++c) {
+    const int k = c - c_begin;
+    float2* cur = stage + (size_t)(k & 1) * G * R;
+    __syncthreads();  // the map buffer and the other stage are free (and, the first time, the tables ready)
+    if (d.sens) {
+      const float2* src = d.sens + ((size_t)c * d.N + y0) * d.N;  // rows y0 .. y0 + nr - 1 of coil c
+      for (int i = threadIdx.x; i < nr * d.N; i += blockDim.x) cp_async8(smap + i, src + i);
+    }
+    cp_async_commit();
+    if (c + 1 < c_end) copy_rows(c + 1, stage + (size_t)((k + 1) & 1) * G * R);
+    cp_async_commit();
+    cp_async_wait<2>();  // this thread's copies of coil c's grid rows landed
     __syncthreads();
     float2 v[M];
 #pragma unroll
-    for (int k1 = 0; k1 < M; ++k1) v[k1] = stage[(k1 + kb) * R + rc];
+    for (int k1 = 0; k1 < M; ++k1) v[k1] = cur[(k1 + kb) * R + rc];
     F::inv(v, t, tw);
+    cp_async_wait<1>();  // this thread's copies of coil c's map rows landed
+    __syncthreads();
     if (ok) {
-      const float2* srow = d.sens ? d.sens + ((size_t)c * d.N + y) * d.N : nullptr;
+      const float2* srow = d.sens ? smap + (size_t)r * d.N : nullptr;
       float2* arow = acc + (size_t)r * d.N;
 #pragma unroll
       for (int j = 0; j < M; ++j) {
         int x = t + L * j + d.off;
         if (x >= G) x -= G;
         if (x < d.N) {
-          float2 val = v[j] * (d.scale / (d.deap[x] * dy));
+          float2 val = v[j] * (d.scale / (sdeap[x] * dy));
           if (srow) val = cmulc(val, srow[x]);
           arow[x] += val;
         }
       }
     }
   }
+  cp_async_wait<0>();
   __syncthreads();
   float2* og = out + (size_t)g * gstride;
   for (int i = threadIdx.x; i < nr * d.N; i += blockDim.x) {
@@ -230,7 +253,9 @@ size_t rad_fast_rows_smem(const RadFastKernels& k) {
   return sizeof(float2) * (G + G * k.per_block());
 }
 size_t rad_fast_rows_inv_smem(const RadFastKernels& k, int N) {
-  return rad_fast_rows_smem(k) + sizeof(float2) * (size_t)k.per_block() * N;
+  // second grid-row stage, partial sums and coil-map rows (R x N each), deapodisation table
+  const size_t G = (size_t)k.M * k.L, R = (size_t)k.per_block();
+  return rad_fast_rows_smem(k) + sizeof(float2) * (G * R + 2 * R * N) + sizeof(float) * N;
 }
 size_t rad_fast_cols_smem(const RadFastKernels& k) {
   const size_t G = (size_t)k.M * k.L;
