@@ -113,17 +113,20 @@ __global__ void __launch_bounds__(kRT) rad_cols(RadDev d, const float2* __restri
 
 // Degridding. mode 0: kout[c][j] = A u. mode 1 (solver): r <- (r + sigma (A u - f)) / (1 + sigma lambda),
 // s[j][c] = w_j r (the weighted values the adjoint grids, sample-major). blockIdx.y selects a chunk of MAXC
-// coils, fully unrolled, so that a sample's tap loads of the chunk are all in flight at once.
-template <int MAXC>
+// coils, fully unrolled, so that a sample's tap loads of the chunk are all in flight at once; KW > 0 fixes
+// the kernel width at compile time so that the taps unroll too (KW = 0: d.kw at run time).
+template <int MAXC, int KW>
 __global__ void __launch_bounds__(kRT) rad_degrid(RadDev d, int mode, const float2* __restrict__ F,
                                                   float2* __restrict__ kout, float2* __restrict__ r,
                                                   const float2* __restrict__ f, float2* __restrict__ s,
                                                   float sigma, float lambda) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= d.Ns) return;
-  const int kw = d.kw;
+  static_assert(KW >= 0 && KW <= kMaxKw, "kernel width");
+  const int kw = KW > 0 ? KW : d.kw;
   float wx[kMaxKw], wy[kMaxKw];
   int gxs[kMaxKw], gys[kMaxKw];
+#pragma unroll
   for (int t = 0; t < kw; ++t) {
     wx[t] = d.wt[((size_t)j * 2 + 0) * kw + t];
     wy[t] = d.wt[((size_t)j * 2 + 1) * kw + t];
@@ -138,10 +141,12 @@ __global__ void __launch_bounds__(kRT) rad_degrid(RadDev d, int mode, const floa
     float2 a[MAXC];
 #pragma unroll
     for (int c = 0; c < MAXC; ++c) a[c] = c2(0.f, 0.f);
+#pragma unroll
     for (int tx = 0; tx < kw; ++tx) {
       float2 col[MAXC];
 #pragma unroll
       for (int c = 0; c < MAXC; ++c) col[c] = c2(0.f, 0.f);
+#pragma unroll
       for (int ty = 0; ty < kw; ++ty) {
         const float2* Fp = F + (size_t)cbase * plane + (size_t)gxs[tx] * d.G + gys[ty];
 #pragma unroll
@@ -449,8 +454,12 @@ class RadialOp : public OpImpl, public SolverHooks {
                      cudaStream_t st) {
     constexpr int kDegridCoils = 4;  // coils per thread; the chunks are spread over grid.y
     const dim3 nb((dev_.Ns + kRT - 1) / kRT, (dev_.C + kDegridCoils - 1) / kDegridCoils);
-    rad_degrid<kDegridCoils><<<nb, kRT, 0, st>>>(dev_, mode, grid_.as<float2>(), kout, r, fc, svals_.as<float2>(),
-                                                 sigma, lambda);
+    if (dev_.kw == 3)
+      rad_degrid<kDegridCoils, 3><<<nb, kRT, 0, st>>>(dev_, mode, grid_.as<float2>(), kout, r, fc, svals_.as<float2>(),
+                                                      sigma, lambda);
+    else
+      rad_degrid<kDegridCoils, 0><<<nb, kRT, 0, st>>>(dev_, mode, grid_.as<float2>(), kout, r, fc, svals_.as<float2>(),
+                                                      sigma, lambda);
     PDT_LAUNCH_CHECK();
     count_launch();
   }
