@@ -324,8 +324,9 @@ class CartesianOp : public OpImpl, public SolverHooks {
     if (tune_.tca && dev_.ns > 0 && fuse_dual_ && dual_rows() > 0)
       os << " solver_dual=adjoint_launch(" << dual_rows() * ((2 * dev_.W + tc_adj_nb(tune_.nr) - 1) / tc_adj_nb(tune_.nr))
          << "_blocks)";
-    if ((tune_.tca || tune_.tcf) && frow_.ok())  // what a batched solve runs instead (tca(), tcf())
-      os << " in_batch=lane_fft_rows(batch_adj_groups=" << G_ << (tune_.cluster ? ",cluster" : ",partials") << ")";
+    if (frow_.ok())  // what a batched solve runs (tca(), tcf(), groups_run())
+      os << " in_batch=lane_fft_rows(batch_adj_groups=" << std::min(G_, batch_groups())
+         << (tune_.cluster ? ",cluster" : ",partials") << ")";
     return os.str();
   }
   Dims natural_input_size() override {
@@ -361,7 +362,7 @@ class CartesianOp : public OpImpl, public SolverHooks {
   int groups() override {
     prepare();
     if (tca()) return 1;                         // the tensor-core adjoint rows sum the coils on chip
-    return (frow_.ok() && tune_.cluster) ? 1 : G_;  // a cluster reduces its coil groups on chip
+    return (frow_.ok() && tune_.cluster) ? 1 : groups_run();  // a cluster reduces its coil groups on chip
   }
   long long group_stride() override { return (long long)dev_.Hi * dev_.W; }
   // The dual update rides in the tensor-core adjoint launch when its row tiles leave at least
@@ -385,7 +386,7 @@ class CartesianOp : public OpImpl, public SolverHooks {
     if (dual && !can_fuse_dual(dual->W, dual->H))
       throw Error(PDT_ERR_STATE, name_ + ": round() given a dual update it cannot run");
     if (dev_.ns == 0) {
-      launch_fill_zero(khr, sizeof(float2) * (size_t)G_ * dev_.Hi * dev_.W, st);
+      launch_fill_zero(khr, sizeof(float2) * (size_t)groups_run() * dev_.Hi * dev_.W, st);
       if (tick) launch_tick(tick, st);
       return;
     }
@@ -397,7 +398,7 @@ class CartesianOp : public OpImpl, public SolverHooks {
     if (tca())
       launch_tc_rows_adj(t, khr, st, dual);  // the coil sum on chip: one K^H r plane
     else
-      launch_rows_adj(t, khr, G_, st);
+      launch_rows_adj(t, khr, groups_run(), st);
     if (mk) mk->mark("cart_rows_adj", st);
   }
   void adjoint_compact(const float2* fc, float2* img, cudaStream_t st) override {
@@ -545,6 +546,18 @@ class CartesianOp : public OpImpl, public SolverHooks {
   // The tensor-core row passes take one 198 KB CTA per SM and are chosen by timing the operator alone;
   // among the concurrent problems of a batch the lane-FFT rows, which share SMs, run instead.
   bool tca() const { return tune_.tca && !(concurrent_ && frow_.ok()); }
+  // Coil groups of the FFT adjoint rows: the tuned count alone; in a batch at most batch_groups() (2;
+  // PDT_BATCH_GROUPS overrides), since each group adds a K^H r partial image that the adjoint writes and
+  // the primal step reads, and the other problems supply the parallelism that more groups would (64 mixed
+  // problems: 26.9k problem-iterations/s uncapped, 29.1k at 4, 30.6-31.2k at 2, 30.8k at 1)
+  static int batch_groups() {
+    static const int cap = [] {
+      const char* e = std::getenv("PDT_BATCH_GROUPS");
+      return (e && *e) ? std::max(1, std::atoi(e)) : 2;
+    }();
+    return cap;
+  }
+  int groups_run() const { return concurrent_ ? std::min(G_, batch_groups()) : G_; }
   bool tcf() const { return tune_.tcf && !(concurrent_ && frow_.ok()); }
 
   void launch_rows_fwd(const float2* ubar, float2* t1, int* tick, cudaStream_t st) {

@@ -1,7 +1,10 @@
 """Batched solves: uneven problems (size, coils, acceleration, mask kind, optimizer, iteration count)
 advanced together must give exactly what solving each alone gives (where the batch launches the same
-kernels; widths with a separate forward-row split for concurrent launches, and operators whose solo
-tuning chose the tensor-core rows, which a batch replaces by the lane-FFT rows, agree to FP32 rounding)."""
+kernels; widths with a separate forward-row split for concurrent launches, operators whose solo tuning
+chose the tensor-core rows, which a batch replaces by the lane-FFT rows, and operators whose adjoint rows
+run with fewer coil groups in a batch agree to FP32 rounding)."""
+import re
+
 import numpy as np
 import pytest
 
@@ -54,14 +57,23 @@ def test_batch_equals_individual_solves(pdt, oracle):
     ref_den.solve()
     bs = pdt.batch.BatchSolver(batched + [den])
     bs.solve()
-    solo_tc = []
+
+    def same_kernels(tuning):
+        """The batch launches what the solo solve launched: lane-FFT rows with the same coil groups."""
+        if "tensor_dft" in tuning:
+            return False
+        solo_g = re.search(r"coil_groups=(\d+)", tuning)
+        batch_g = re.search(r"batch_adj_groups=(\d+)", tuning)
+        return solo_g is None or batch_g is None or solo_g.group(1) == batch_g.group(1)
+
+    same = []
     for i, c in enumerate(CASES):
         o, _ = _make(pdt, *c, seed=i)
-        solo_tc.append("tensor_dft" in o.op_ref.tuning())
-    for o, want, c, tc in zip(batched, solo, CASES, solo_tc):
-        # batched rounds take the 23 x 16 forward-row split at width 368 (alone: 46 x 8) and the lane-FFT
-        # rows where the solo tuning chose the tensor-core rows: FP32 rounding
-        if c[2] == 368 or tc:
+        same.append(same_kernels(o.op_ref.tuning()))
+    for o, want, c, sk in zip(batched, solo, CASES, same):
+        # batched rounds take the 23 x 16 forward-row split at width 368 (alone: 46 x 8), the lane-FFT rows
+        # where the solo tuning chose the tensor-core rows, and at most two coil groups: FP32 rounding
+        if c[2] == 368 or not sk:
             assert rel_l2(o.getResult(), want) <= 1e-5
         else:
             assert np.array_equal(o.getResult(), want)
