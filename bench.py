@@ -579,6 +579,16 @@ def _khr_planes(tuning):
     return 1 if m.group(2) == ",cluster" else int(m.group(1))
 
 
+def _batch_khr_planes(tuning):
+    """(K^H r planes, lane-FFT rows) of an operator inside a batch: its `in_batch=lane_fft_rows(
+    batch_adj_groups=G,partials|cluster)` report where it has lane-FFT rows (a batch runs those, with at
+    most two coil groups), else the solo figures."""
+    m = re.search(r"batch_adj_groups=(\d+)(,cluster|,partials)", tuning)
+    if not m:
+        return _khr_planes(tuning), False
+    return (1 if m.group(2) == ",cluster" else int(m.group(1))), True
+
+
 FP64_FIXTURE = os.path.join(ROOT, "tests", "golden", "config2_fp64.npz")
 
 
@@ -674,10 +684,8 @@ def run_batched(pdt, torch, n_cases, iters, steps, warmup):
         opt.setNoisyData(case["rawdata"])
         ns = int((case["mask"] != 0).any(axis=0).sum())
         tuning = op.tuning()
-        # in a batch the operator runs its lane-FFT rows where its solo choice was the tensor-core rows
-        m = re.search(r"batch_adj_groups=(\d+)(,cluster|,partials)", tuning)
-        G = (1 if m.group(2) == ",cluster" else int(m.group(1))) if m else _khr_planes(tuning)
-        adj = "tensor_dft" if "rows_adj=tensor_dft" in tuning and not m else "lane_fft"
+        G, lane_in_batch = _batch_khr_planes(tuning)
+        adj = "tensor_dft" if "rows_adj=tensor_dft" in tuning and not lane_in_batch else "lane_fft"
         adj_rows[adj] = adj_rows.get(adj, 0) + 1
         nbytes += sum(_phase_bytes_case(spec["C"], spec["H"], spec["W"], ns, G, False).values())
         pix += spec["H"] * spec["W"]
