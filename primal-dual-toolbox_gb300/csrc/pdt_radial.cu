@@ -230,29 +230,28 @@ __global__ void __launch_bounds__(kRT) rad_grid(RadDev d, const float2* __restri
     float2 acc[MAXC];
 #pragma unroll
     for (int c = 0; c < MAXC; ++c) acc[c] = c2(0.f, 0.f);
-    int e = beg;
-    for (; e + 4 <= end; e += 4) {
-      const float2* s0 = s + (size_t)d.cell_idx[e] * d.C + cbase;
-      const float2* s1 = s + (size_t)d.cell_idx[e + 1] * d.C + cbase;
-      const float2* s2 = s + (size_t)d.cell_idx[e + 2] * d.C + cbase;
-      const float2* s3 = s + (size_t)d.cell_idx[e + 3] * d.C + cbase;
-      const float w0 = d.cell_w[e], w1 = d.cell_w[e + 1], w2 = d.cell_w[e + 2], w3 = d.cell_w[e + 3];
+    // four entries at a time, the last group predicated (most cells have fewer than four), so that a
+    // group's index and weight loads, then its sample loads, are each in flight together
+    for (int e = beg; e < end; e += 4) {
+      const int m = end - e;  // entries e .. e + min(m, 4) - 1 are this cell's
+      const float2* sp[4];
+      float w[4];
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        sp[k] = s + (size_t)(k < m ? d.cell_idx[e + k] : 0) * d.C + cbase;
+        w[k] = k < m ? d.cell_w[e + k] : 0.f;
+      }
 #pragma unroll
       for (int c = 0; c < MAXC; ++c)
-        if (c < nc) {
-          const float2 a0 = s0[c], a1 = s1[c], a2 = s2[c], a3 = s3[c];
-          acc[c] += a0 * w0;
-          acc[c] += a1 * w1;
-          acc[c] += a2 * w2;
-          acc[c] += a3 * w3;
+        if (c < nc) {  // loads only for this cell's entries, added in entry order as one at a time
+          const float2 z = c2(0.f, 0.f);
+          const float2 a0 = sp[0][c], a1 = m > 1 ? sp[1][c] : z, a2 = m > 2 ? sp[2][c] : z,
+                       a3 = m > 3 ? sp[3][c] : z;
+          acc[c] += a0 * w[0];
+          if (m > 1) acc[c] += a1 * w[1];
+          if (m > 2) acc[c] += a2 * w[2];
+          if (m > 3) acc[c] += a3 * w[3];
         }
-    }
-    for (; e < end; ++e) {
-      const float2* sj = s + (size_t)d.cell_idx[e] * d.C + cbase;
-      const float wgt = d.cell_w[e];
-#pragma unroll
-      for (int c = 0; c < MAXC; ++c)
-        if (c < nc) acc[c] += sj[c] * wgt;
     }
 #pragma unroll
     for (int c = 0; c < MAXC; ++c)
