@@ -48,8 +48,6 @@ __device__ __forceinline__ void mma16816(float (&d)[4], const uint32_t (&a)[4], 
 }
 
 enum Epi {
-  EPI_LINEAR = 0,    // out = z (BF16)
-  EPI_RELU = 1,      // zsave = z, out = relu(z)
   EPI_RELU_RES = 2,  // zsave = z, out = in + relu(z)   (CIN == COUT)
   EPI_F32 = 3,       // out32 = z (FP32)
   EPI_ACC = 4,       // acc32 += bf16(z)  (a residual stream's FP32 gradient; the BF16 rounding of a stored z)
@@ -257,14 +255,16 @@ __global__ void __launch_bounds__(kConvTcThreads, 4) conv3x3_tc(const bf16* __re
   }
 }
 
-// 3 x 3 convolution as an implicit GEMM. in: [B][H][W][CIN] BF16; w: [9][COUT][CIN] BF16; bias: [COUT] FP32
-// (may be null). Each block computes a 16 x 8 pixel tile; warp w owns tile row w (16 pixels = one M tile).
+// 3 x 3 convolution as an implicit GEMM on warp-level MMAs, for the layers tcgen05 does not take (N = 8
+// output channels; the 16-channel padded output gradient): in: [B][H][W][CIN] BF16; w: [9][COUT][CIN] BF16;
+// bias: [COUT] FP32 (may be null); FP32 output. Each block computes a 16 x 8 pixel tile; warp w owns tile
+// row w (16 pixels = one M tile).
 template <int CIN, int COUT, int EPI>
 __global__ void __launch_bounds__(32 * TH) conv3x3_mma(const bf16* __restrict__ in, const bf16* __restrict__ w,
                                                        const float* __restrict__ bias, int H, int W,
-                                                       bf16* __restrict__ out, bf16* __restrict__ zsave,
                                                        float* __restrict__ out32) {
   static_assert(CIN % 16 == 0 && COUT % 8 == 0, "channel counts");
+  static_assert(EPI == EPI_F32 || EPI == EPI_F32_BF16, "epilogues of the 32 -> 8 layer and the first data gradient");
   constexpr int PS = CIN + 4;       // smem pixel stride (bf16): spreads the fragment loads over all banks
   constexpr int WS = CIN + 8;       // smem weight row stride (bf16)
   __shared__ __align__(16) bf16 s_in[(TH + 2) * (TW + 2) * PS];
@@ -330,20 +330,9 @@ __global__ void __launch_bounds__(32 * TH) conv3x3_mma(const bf16* __restrict__ 
       if constexpr (EPI == EPI_F32) {
         out32[pix * COUT + co] = z0;
         out32[pix * COUT + co + 1] = z1;
-      } else if constexpr (EPI == EPI_F32_BF16) {
+      } else {
         out32[pix * COUT + co] = __bfloat162float(__float2bfloat16(z0));
         out32[pix * COUT + co + 1] = __bfloat162float(__float2bfloat16(z1));
-      } else if constexpr (EPI == EPI_LINEAR) {
-        reinterpret_cast<uint32_t*>(out + pix * COUT)[co / 2] = pack_bf16(z0, z1);
-      } else {
-        reinterpret_cast<uint32_t*>(zsave + pix * COUT)[co / 2] = pack_bf16(z0, z1);
-        float r0 = fmaxf(z0, 0.f), r1 = fmaxf(z1, 0.f);
-        if constexpr (EPI == EPI_RELU_RES) {
-          const __nv_bfloat162 h = reinterpret_cast<const __nv_bfloat162*>(in + pix * CIN)[co / 2];
-          r0 += __bfloat162float(h.x);
-          r1 += __bfloat162float(h.y);
-        }
-        reinterpret_cast<uint32_t*>(out + pix * COUT)[co / 2] = pack_bf16(r0, r1);
       }
     }
   }
@@ -994,7 +983,7 @@ class WarmStartCnn {
       count_launch();
     }
     conv3x3_mma<CH, 8, EPI_F32><<<grid, 32 * TH, 0, st>>>(h_[6].as<bf16>(), W_[7].wb.as<bf16>(), B_[7].w.as<float>(),
-                                                          H, W, nullptr, nullptr, o_.as<float>());
+                                                          H, W, o_.as<float>());
     PDT_LAUNCH_CHECK();
     count_launch();
   }
@@ -1019,7 +1008,7 @@ class WarmStartCnn {
     PDT_LAUNCH_CHECK();
     // the residual stream's FP32 gradient starts as G = dh6 (the BF16 rounding of the convolution's output)
     conv3x3_mma<16, CH, EPI_F32_BF16><<<grid, 32 * TH, 0, st>>>(go16_.as<bf16>(), wt_.as<bf16>(), nullptr, H, W,
-                                                                nullptr, nullptr, gacc_.as<float>());
+                                                                gacc_.as<float>());
     PDT_LAUNCH_CHECK();
     count_launch(3);  // mse_loss, flip_transpose, conv3x3_mma (the bias gradient counts its own)
     for (int l = 6; l >= 1; --l) {
