@@ -15,6 +15,7 @@
 #include <sstream>
 
 #include "pdt_ops.h"
+#include "pdt_schedule.h"
 
 namespace pdt {
 
@@ -1100,18 +1101,9 @@ class BatchImpl {
       events_.push_back(e);
     }
     const size_t P = std::min(want, workers_.size());
-    owner_.assign(opts_.size(), 0);
-    std::vector<size_t> order(opts_.size());
-    for (size_t i = 0; i < order.size(); ++i) order[i] = i;
-    std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t b) {
-      return opts_[a]->work_estimate() > opts_[b]->work_estimate();
-    });
-    std::vector<size_t> load(P, 0);
-    for (size_t i : order) {
-      const size_t w = (size_t)(std::min_element(load.begin(), load.end()) - load.begin());
-      owner_[i] = w;
-      load[w] += opts_[i]->work_estimate();
-    }
+    std::vector<size_t> cost(opts_.size());
+    for (size_t i = 0; i < cost.size(); ++i) cost[i] = opts_[i]->work_estimate();
+    owner_ = assign_longest_first(cost, P);
     nworkers_ = P;
   }
   // Runs fn(problem, worker stream) for every problem on worker streams forked from and joined back into `on`.
